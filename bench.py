@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark: kMC events/s of the N_K=200 monodisperse melt on one GB300.
+
+Workload (the headline configuration): 65536 chains, N_K=200 Kuhn steps,
+beta=1, constraint dynamics on, equilibrium initial state, multi-tau G(t)
+correlator (p=64, m=8, levels for t_end=1e7 tau_K, sample every 1 tau_K) on
+the three shear stresses.  A "step" advances the whole ensemble by a window
+of --window tau_K (default 500) in steady state; inputs are already resident in
+HBM.  The ensemble state (~260 MB conformations + ~590 MB correlator) exceeds
+the 129 MB L2, so no explicit L2 flush is needed between steps.
+
+Also reported:
+  e2e           same metric through the C ABI with the conformations uploaded
+                from pinned host memory and read back every step (plus G(t))
+  roofline      SM-issue bound of the step kernel: lane-ops per event
+                L_eq(Z) = 2(Z-1) + 152 against 152 SMs x 128 lanes x f_max
+  cpu_baseline  the oracle (CPU restatement of the reference path) on the
+                host cores, bounded sample of the same workload
+  --impl reference  times that CPU restatement as the reference arm
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "kMC events/s on 1 GB300 (N_K=200); serve p50/p99 vs plain at G(t) err<=1%"
+UNIT = "events/s"
+N_CHAINS, NK, BETA = 65536, 200, 1.0
+T_END_RUN, SAMPLE_DT, CORR_P, CORR_M = 1.0e7, 1.0, 64, 8
+
+
+def config(window: float, n_gpus: int) -> dict:
+    return {"workload": f"equilibrium monodisperse melt: {N_CHAINS} chains x N_K={NK}, beta={BETA}, CD on, "
+                        f"G(t) multi-tau p={CORR_P} m={CORR_M} over xy/yz/xz (levels for t_end=1e7, dt=1)",
+            "n_chains_per_gpu": N_CHAINS, "nk": NK, "beta": BETA, "window_tau_per_step": window,
+            "l2": "inputs larger than L2 (state ~0.85 GB per GPU); no flush", "parallelism": f"chains x{n_gpus} (replicas)"}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_sample(target_s: float, threads: int = 0):
+    """Time the oracle (FP32 mirror, OpenMP over chains) on a bounded sample of the
+    workload: n chains of N_K=200 from the equilibrium state, advanced by a window
+    sized to ~target_s of CPU time after a short calibration."""
+    from oracle import oracle as orc
+
+    orc.build()
+    n = 256
+    o = orc.Oracle(nk=NK, n_chains=n, seed=1, corr=True, sync_dt=SAMPLE_DT, t_end=T_END_RUN, corr_p=CORR_P,
+                   corr_m=CORR_M, threads=threads)
+    o.init_equilibrium()
+    t0 = time.perf_counter()
+    ev = o.run(10.0)
+    dt = time.perf_counter() - t0
+    rate = ev / max(dt, 1e-6)
+    window = max(10.0, min(2000.0, target_s * rate / (n * 42.6)))
+    t0 = time.perf_counter()
+    ev = o.run(10.0 + window)
+    dt = time.perf_counter() - t0
+    return {"value": ev / dt, "unit": UNIT, "cores": o.threads, "kind": "port",
+            "sample": f"{n} chains x {window:.0f} tau_K of the N_K=200 workload (oracle FP32 mirror, "
+                      f"{ev} events in {dt:.1f} s)"}, o
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    per_step = max(3.0, 150.0 / max(1, args.steps + args.warmup))
+    base, o = cpu_sample(min(per_step, 20.0))
+    rates, t_cur = [], 2000.0 + 10.0
+    n = o.n
+    window = max(5.0, per_step * base["value"] / (n * 42.6))
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ev = o.run(t_cur + window)
+        dt = time.perf_counter() - t0
+        t_cur += window
+        if i >= args.warmup:
+            rates.append((ev, dt))
+    ev = sum(e for e, _ in rates)
+    dt = sum(d for _, d in rates)
+    v = ev / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic equilibrium melt",
+            "config": config(window, args.gpus), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": o.threads, "kind": "port",
+                             "sample": f"{n} chains x {window:.0f} tau_K per step of the N_K=200 workload "
+                                       f"(oracle, the reference's chain-step logic restated in C++/OpenMP; the "
+                                       f"reference GPU code does not compile with CUDA 13)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- GPU leg
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def profile_traffic() -> dict:
+    p = ROOT / "profiles" / "step_kernel_traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def run_gpu(args):
+    import torch
+    import gpu_dsm_gb300 as dsm
+    from gpu_dsm_gb300 import build as native
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if rank == 0:
+        native.build()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.set_device(local)
+
+    ens = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT, t_end=T_END_RUN,
+                       seed=1, stream=rank, device=local, corr_p=CORR_P, corr_m=CORR_M)
+    ens.init_equilibrium()
+    t = 0.0
+    for _ in range(args.warmup):
+        t += args.window
+        ens.advance(t)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    events, kms = 0, 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t += args.window
+        events += ens.advance(t)
+        kms += ens.last_window()["kernel_ms"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    lw = ens.last_window()
+    heads, qn, tau = ens.get_chains()
+    zmean = float(heads["Z"].mean())
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([kms, float(events)], dtype=torch.float64, device="cuda")
+        mx = tt.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+        kms_max, events_all = float(mx[0]), int(tt[1])
+    else:
+        kms_max, events_all = kms, events
+    value = events_all / (kms_max / 1e3)
+
+    # ---- e2e through the C ABI with host buffers (pinned), every step
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        cap = ens.z_max
+        h_heads = torch.empty(N_CHAINS * 16, dtype=torch.uint8, pin_memory=True)
+        h_qn = torch.empty(N_CHAINS * cap * 4, dtype=torch.float32, pin_memory=True)
+        h_tau = torch.empty(N_CHAINS * cap, dtype=torch.float32, pin_memory=True)
+        hv = h_heads.numpy().view(dsm.api.HEAD_DTYPE)
+        qv = h_qn.numpy().reshape(N_CHAINS, cap, 4)
+        tv = h_tau.numpy().reshape(N_CHAINS, cap)
+        hv[:] = heads
+        hv["time"] = 0.0
+        qv[:] = qn
+        tv[:] = tau
+        ens2 = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT,
+                            t_end=T_END_RUN, seed=2, device=local, corr_p=CORR_P, corr_m=CORR_M)
+        ev_e, t_e = 0, 0.0
+        npts = 0
+        for i in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            ens2.set_chains(hv, qv, tv)
+            ev = ens2.advance(args.window)
+            h2, q2, t2 = ens2.get_chains()
+            tg, g = ens2.gt()
+            torch.cuda.synchronize()
+            s1 = time.perf_counter()
+            npts = len(g)
+            if i > 0:  # first e2e step is a warm-up
+                ev_e += ev
+                t_e += s1 - s0
+        h2d = N_CHAINS * 16 + N_CHAINS * cap * 20
+        d2h = N_CHAINS * 16 + N_CHAINS * cap * 20 + npts * 8
+        e2e = {"value": ev_e / t_e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": args.e2e_steps, "host_buffers": "pinned (torch pin_memory)",
+               "calls": "dsm_set_chains + dsm_advance + dsm_get_chains + dsm_gt"}
+        ens2.close()
+
+    # ---- roofline: SM-issue bound (lane-ops per event) + HBM secondary
+    peaks = measured_peaks()
+    f_max = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    n_sm = 152
+    l_eq = 2.0 * (zmean - 1.0) + 152.0
+    peak_lane = n_sm * 128 * f_max
+    achieved_lane = value / world * l_eq
+    per_launch_events = events / max(1, args.steps)
+    tr = profile_traffic()
+    traffic = None
+    if tr.get("bytes_per_event"):
+        traffic = float(tr["bytes_per_event"]) * per_launch_events
+    roof = {"bound": "sm_issue", "achieved": achieved_lane / 1e9, "peak": peak_lane / 1e9, "unit": "Glane-op/s",
+            "frac": achieved_lane / peak_lane, "traffic": traffic,
+            "per_unit": f"L_eq(Z)=2(Z-1)+152 lane-ops per kMC event at <Z>={zmean:.1f}",
+            "peak_source": "152 SMs x 128 lanes x sm_max_mhz of MEASURED_PEAKS.json (of measured clock)"}
+    if peaks.get("hbm_gbs"):
+        # algorithmic HBM bytes per step: chain state in + out once per window, correlator levels
+        bytes_chain = N_CHAINS * (2 * (zmean * 20 + 64) + 2 * (CORR_P * 12 + 44) + CORR_P * 16)
+        samples = N_CHAINS * args.window / SAMPLE_DT
+        lvl_bytes = samples * sum((1.0 / CORR_M ** k) * (CORR_P * 12 + 12 + (CORR_P - CORR_P // CORR_M) * 16 + 44)
+                                  for k in range(1, 7))
+        gbs = (bytes_chain + lvl_bytes) / (kms / args.steps / 1e3) / 1e9
+        roof["hbm_secondary"] = {"achieved": gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
+                                 "frac": gbs / float(peaks["hbm_gbs"]), "note": "of measured"}
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu:
+        try:
+            cpu, _ = cpu_sample(args.cpu_seconds)
+        except Exception as e:  # the baseline is reported, never a fallback
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": kms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic equilibrium melt",
+            "config": config(args.window, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clocks, "gpu_launches": args.steps,
+            "detail": {"events": events_all, "wall_s": wall, "kernel_ms_total": kms, "mean_Z": zmean,
+                       "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"]}}
+    print(json.dumps(line))
+    ens.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--window", type=float, default=500.0, help="tau_K advanced per step")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,18 @@
+"""gpu_dsm_gb300 — GB300-native Discrete Slip-Link Model (DSM) kinetic Monte Carlo.
+
+Python binding (ctypes) of the native library ``libgpudsm.so`` whose C ABI is
+declared in ``include/dsm.h``.  The compute path is the hand-written sm_103a
+CUDA of ``csrc/dsm_kernels.cu``; this module only moves host arrays in the
+reference layout (ktaletsk/gpu_dsm common/chain.h:37-53) and calls the C ABI.
+There is no CPU fallback: if the native library is missing, importing the
+simulator raises.
+"""
+from .api import (  # noqa: F401
+    DSMError,
+    Ensemble,
+    StressPlus,
+    lib_path,
+    load_library,
+)
+
+__all__ = ["DSMError", "Ensemble", "StressPlus", "lib_path", "load_library"]

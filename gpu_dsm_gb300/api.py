@@ -1,0 +1,267 @@
+"""ctypes mirror of include/dsm.h.
+
+``Ensemble`` plays the role of the reference's ensemble / call-block API
+(common/ensemble.h:54-77, common/ensemble_call_block.h:55-75) for one
+ensemble on one GPU: equilibrium initialisation, conformation transfer in the
+reference layout, time evolution to a target time, flow stress and G(t).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_LIB: Optional[C.CDLL] = None
+
+DSM_OK = 0
+DSM_ABORTED = -1
+
+
+class DSMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dsm error {code}: {msg}")
+        self.code = code
+
+
+class DsmParams(C.Structure):
+    _fields_ = [
+        ("beta", C.c_float),
+        ("nk", C.c_int32),
+        ("n_chains", C.c_int32),
+        ("kappa", C.c_float * 9),
+        ("cd_flag", C.c_int32),
+        ("pd_flag", C.c_int32),
+        ("eq_type", C.c_int32),
+        ("sync_dt", C.c_double),
+        ("t_end", C.c_double),
+        ("seed", C.c_uint64),
+        ("device", C.c_int32),
+        ("z_max", C.c_int32),
+        ("corr_p", C.c_int32),
+        ("corr_m", C.c_int32),
+        ("corr_levels", C.c_int32),
+        ("stream", C.c_uint32),
+        ("nk_chain", C.c_void_p),
+        ("warps_per_block", C.c_int32),
+        ("s0", C.c_int32),
+    ]
+
+
+class ChainHead(C.Structure):
+    _fields_ = [("Z", C.c_int32), ("time", C.c_float), ("dummy", C.c_float), ("stall_flag", C.c_int32)]
+
+
+class StressPlus(C.Structure):
+    _fields_ = [(n, C.c_float) for n in ("xx", "yy", "zz", "xy", "yz", "zx", "Lpp", "Z")]
+
+    def as_array(self) -> np.ndarray:
+        return np.array([getattr(self, n) for n, _ in self._fields_], dtype=np.float64)
+
+
+HEAD_DTYPE = np.dtype([("Z", np.int32), ("time", np.float32), ("dummy", np.float32), ("stall_flag", np.int32)])
+
+
+def lib_path() -> Path:
+    return _PKG / "libgpudsm.so"
+
+
+def load_library() -> C.CDLL:
+    """Load libgpudsm.so (built in-tree by gpu_dsm_gb300/build.py).  Raises if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = lib_path()
+    if not p.exists():
+        raise DSMError(-6, f"native library {p} is missing: run gpu_dsm_gb300/build.py (nvcc, sm_103a)")
+    lib = C.CDLL(str(p))
+    vp, i32, i64, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64
+    lib.dsm_create.argtypes = [C.POINTER(DsmParams), C.POINTER(vp)]
+    lib.dsm_create.restype = C.c_int
+    lib.dsm_destroy.argtypes = [vp]
+    lib.dsm_destroy.restype = None
+    lib.dsm_last_error.argtypes = [vp]
+    lib.dsm_last_error.restype = C.c_char_p
+    lib.dsm_init_equilibrium.argtypes = [vp]
+    lib.dsm_set_chains.argtypes = [vp, vp, vp, vp]
+    lib.dsm_get_chains.argtypes = [vp, vp, vp, vp]
+    lib.dsm_get_ext.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    lib.dsm_set_ext.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.dsm_advance.argtypes = [vp, C.c_double, i64, vp, vp]
+    lib.dsm_stress.argtypes = [vp, C.POINTER(StressPlus), C.POINTER(i32)]
+    lib.dsm_gt.argtypes = [vp, vp, vp, C.POINTER(i32)]
+    lib.dsm_gt_raw.argtypes = [vp, vp, vp]
+    lib.dsm_corr_shape.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
+    lib.dsm_last_window.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(u64), C.POINTER(i32), C.POINTER(i32)]
+    lib.dsm_last_window.restype = C.c_int
+    lib.dsm_save_file.argtypes = [vp, C.c_char_p]
+    lib.dsm_load_file.argtypes = [vp, C.c_char_p]
+    for fn in ("dsm_init_equilibrium", "dsm_set_chains", "dsm_get_chains", "dsm_get_ext", "dsm_set_ext",
+               "dsm_advance", "dsm_stress", "dsm_gt", "dsm_gt_raw", "dsm_corr_shape", "dsm_save_file",
+               "dsm_load_file"):
+        getattr(lib, fn).restype = C.c_int
+    _LIB = lib
+    return lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Ensemble:
+    """One DSM ensemble resident on one GPU.
+
+    Parameters mirror input.dat (common/main_cuda.cu:55-68): beta, nk, n_chains,
+    kappa (9, row-major), cd_flag, eq_type (1 = G(t)), sync_dt, t_end; plus
+    seed (job_ID), z_max (strand capacity, default nk), correlator p/m/levels,
+    stream (ensemble id for the RNG), nk_chain (polydisperse per-chain N_K).
+    """
+
+    def __init__(self, *, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[float] = (0.0,) * 9,
+                 cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
+                 device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
+                 stream: int = 0, nk_chain: Optional[np.ndarray] = None, warps_per_block: int = 0, s0: int = 0):
+        self._lib = load_library()
+        p = DsmParams()
+        p.beta = beta
+        p.nk = nk
+        p.n_chains = n_chains
+        for i, k in enumerate(kappa):
+            p.kappa[i] = k
+        p.cd_flag = cd_flag
+        p.pd_flag = 0
+        p.eq_type = eq_type
+        p.sync_dt = sync_dt
+        p.t_end = t_end
+        p.seed = seed
+        p.device = device
+        p.z_max = z_max
+        p.corr_p = corr_p
+        p.corr_m = corr_m
+        p.corr_levels = corr_levels
+        p.stream = stream
+        self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
+        p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
+        p.warps_per_block = warps_per_block
+        p.s0 = s0
+        self.params = p
+        self.n_chains = n_chains
+        self.z_max = z_max if z_max > 0 else nk
+        self.nk = nk
+        h = C.c_void_p()
+        rc = self._lib.dsm_create(C.byref(p), C.byref(h))
+        self._h = h
+        if rc != DSM_OK:
+            msg = self._lib.dsm_last_error(h).decode() if h else ""
+            self.close()
+            raise DSMError(rc, msg)
+
+    # ------------------------------------------------------------- plumbing
+    def _check(self, rc: int) -> int:
+        if rc not in (DSM_OK,):
+            raise DSMError(rc, self._lib.dsm_last_error(self._h).decode())
+        return rc
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dsm_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------- state
+    def init_equilibrium(self) -> None:
+        self._check(self._lib.dsm_init_equilibrium(self._h))
+
+    def get_chains(self):
+        """Returns (heads structured array, QN float32 [n, z_max, 4], tau float32 [n, z_max])."""
+        n, cap = self.n_chains, self.z_max
+        heads = np.zeros(n, dtype=HEAD_DTYPE)
+        qn = np.zeros((n, cap, 4), dtype=np.float32)
+        tau = np.zeros((n, cap), dtype=np.float32)
+        self._check(self._lib.dsm_get_chains(self._h, _ptr(heads), _ptr(qn), _ptr(tau)))
+        return heads, qn, tau
+
+    def set_chains(self, heads: np.ndarray, qn: np.ndarray, tau: np.ndarray) -> None:
+        heads = np.ascontiguousarray(heads, dtype=HEAD_DTYPE)
+        qn = np.ascontiguousarray(qn, dtype=np.float32)
+        tau = np.ascontiguousarray(tau, dtype=np.float32)
+        assert qn.shape == (self.n_chains, self.z_max, 4) and tau.shape == (self.n_chains, self.z_max)
+        self._check(self._lib.dsm_set_chains(self._h, _ptr(heads), _ptr(qn), _ptr(tau)))
+
+    def get_ext(self) -> dict:
+        n = self.n_chains
+        out = {"T": np.zeros(n, np.int64), "step": np.zeros(n, np.uint64), "dt_prev": np.zeros(n, np.float32),
+               "stall": np.zeros(n, np.int32), "S": np.zeros(n, np.int32), "hash": np.zeros(n, np.uint64)}
+        self._check(self._lib.dsm_get_ext(self._h, _ptr(out["T"]), _ptr(out["step"]), _ptr(out["dt_prev"]),
+                                          _ptr(out["stall"]), _ptr(out["S"]), _ptr(out["hash"])))
+        return out
+
+    def set_ext(self, T=None, step=None, dt_prev=None, stall=None, S=None) -> None:
+        conv = lambda a, t: None if a is None else np.ascontiguousarray(a, dtype=t)
+        T, step, dt_prev, stall, S = (conv(T, np.int64), conv(step, np.uint64), conv(dt_prev, np.float32),
+                                      conv(stall, np.int32), conv(S, np.int32))
+        self._check(self._lib.dsm_set_ext(self._h, _ptr(T), _ptr(step), _ptr(dt_prev), _ptr(stall), _ptr(S)))
+
+    # ------------------------------------------------------------- evolution
+    def advance(self, t_end: float, step_limit: int = -1, abort: Optional[np.ndarray] = None) -> int:
+        """Run all chains to time t_end (or step_limit events each).  Returns the events done.
+        Returns -1 if aborted through ``abort`` (an int32 numpy scalar array set non-zero)."""
+        ev = C.c_uint64(0)
+        rc = self._lib.dsm_advance(self._h, float(t_end), int(step_limit), _ptr(abort), C.byref(ev))
+        if rc == DSM_ABORTED:
+            return -1
+        self._check(rc)
+        return int(ev.value)
+
+    def last_window(self) -> dict:
+        """Step-kernel device time (ms, CUDA events on its stream), events and launch shape of the
+        last advance()."""
+        ms, ev, grid, bps = C.c_float(), C.c_uint64(), C.c_int32(), C.c_int32()
+        self._check(self._lib.dsm_last_window(self._h, C.byref(ms), C.byref(ev), C.byref(grid), C.byref(bps)))
+        return {"kernel_ms": float(ms.value), "events": int(ev.value), "grid": int(grid.value),
+                "blocks_per_sm": int(bps.value)}
+
+    def stress(self):
+        s = StressPlus()
+        cnt = C.c_int32(0)
+        self._check(self._lib.dsm_stress(self._h, C.byref(s), C.byref(cnt)))
+        return s.as_array(), int(cnt.value)
+
+    def corr_shape(self):
+        L, p, m = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._lib.dsm_corr_shape(self._h, C.byref(L), C.byref(p), C.byref(m)))
+        return L.value, p.value, m.value
+
+    def gt_raw(self):
+        L, p, _ = self.corr_shape()
+        g = np.zeros(L * p, np.float64)
+        c = np.zeros(L * p, np.int64)
+        self._check(self._lib.dsm_gt_raw(self._h, _ptr(g), _ptr(c)))
+        return g.reshape(L, p), c.reshape(L, p)
+
+    def gt(self):
+        n = C.c_int32(8192)
+        t = np.zeros(8192, np.float32)
+        g = np.zeros(8192, np.float32)
+        self._check(self._lib.dsm_gt(self._h, _ptr(t), _ptr(g), C.byref(n)))
+        return t[: n.value].copy(), g[: n.value].copy()
+
+    def save(self, path: str) -> None:
+        self._check(self._lib.dsm_save_file(self._h, os.fsencode(path)))
+
+    def load(self, path: str) -> None:
+        self._check(self._lib.dsm_load_file(self._h, os.fsencode(path)))

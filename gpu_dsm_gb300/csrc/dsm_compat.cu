@@ -1,0 +1,244 @@
+// Reference-compatible driver on top of the C ABI: main_cuda() with the
+// reference's signature (common/main_cuda.cu:34), the input.dat format
+// (common/main_cuda.cu:53-68, CLI/input.dat:1-22), tau/G output files
+// (common/main_cuda.cu:122-159, common/ensemble.cu:326-335), the job_ID file
+// suffix (common/job_ID.h:33-68) and the -distr histograms
+// (common/ensemble.cu:356-484).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "../../include/dsm.h"
+#include "dsm_compat.h"
+
+namespace dsmc {
+
+// common/job_ID.h:33-68: "<name>_<id>.dat", or "<name>.dat" for id 0
+std::string filename_ID(const std::string& name, int job_ID) {
+  if (job_ID != 0) return name + "_" + std::to_string(job_ID) + ".dat";
+  return name + ".dat";
+}
+
+// common/main_cuda.cu:53-68
+int read_input(const char* path, InputDat* in) {
+  std::ifstream f(path);
+  if (!f) return DSM_ERR_INVALID;
+  f >> in->beta >> in->nk >> in->n_chains;
+  for (int q = 0; q < 9; ++q) f >> in->kappa[q];
+  f >> in->cd_flag >> in->pd_flag >> in->eq_type >> in->sync_dt >> in->t_end;
+  if (!f) return DSM_ERR_INVALID;
+  return DSM_OK;
+}
+
+// common/ensemble.cu:356-392
+static void write_Z_distr(const std::string& fn, const std::vector<dsm_chain_head>& h, bool cumulative) {
+  std::ofstream f(fn);
+  if (!f) { std::cout << "file error\n"; return; }
+  int zmin = h[0].Z, zmax = h[0].Z;
+  for (auto& c : h) { zmin = std::min(zmin, c.Z); zmax = std::max(zmax, c.Z); }
+  const size_t n = h.size();
+  for (int j = zmin; j <= zmax; ++j) {
+    size_t cnt = 0;
+    for (auto& c : h) cnt += cumulative ? (c.Z <= j) : (c.Z == j);
+    f << j << "\t" << (float)cnt / (float)n << "\n";
+  }
+}
+
+// common/ensemble.cu:394-431
+static void write_N_distr(const std::string& fn, const std::vector<dsm_chain_head>& h,
+                          const std::vector<dsm_float4>& q, int cap, bool cumulative) {
+  std::ofstream f(fn);
+  if (!f) { std::cout << "file error\n"; return; }
+  int nmin = (int)q[0].w, nmax = (int)q[0].w;
+  long long nstr = 0;
+  for (size_t i = 0; i < h.size(); ++i) {
+    for (int j = 0; j < h[i].Z; ++j) {
+      const int v = (int)q[i * cap + j].w;
+      nmin = std::min(nmin, v); nmax = std::max(nmax, v);
+      if (v == 0) std::cout << "Zero length strand in chain " << i << ", #" << j << "\n";
+    }
+    nstr += h[i].Z;
+  }
+  std::vector<long long> hist(nmax + 2, 0);
+  for (size_t i = 0; i < h.size(); ++i)
+    for (int j = 0; j < h[i].Z; ++j) hist[(int)q[i * cap + j].w]++;
+  long long run = 0;
+  for (int n = nmin; n <= nmax; ++n) {
+    run += hist[n];
+    const long long cnt = cumulative ? run : hist[n];
+    f << n << "\t" << (float)cnt / (float)nstr << "\n";
+  }
+}
+
+// common/ensemble.cu:439-484 (cumulative |Q| distribution of internal strands)
+static void write_Q_distr(const std::string& fn, const std::vector<dsm_chain_head>& h,
+                          const std::vector<dsm_float4>& q, int cap) {
+  std::ofstream f(fn);
+  if (!f) { std::cout << "file error\n"; return; }
+  std::vector<float> Q;
+  for (size_t i = 0; i < h.size(); ++i)
+    for (int j = 1; j < h[i].Z - 1; ++j) {
+      const dsm_float4 v = q[i * cap + j];
+      Q.push_back(std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
+    }
+  std::sort(Q.begin(), Q.end());
+  const size_t n = Q.size();
+  std::vector<float> P(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (i != 0 && Q[i] == Q[i - 1]) P[i - 1] = (float)i / (float)n;
+    P[i] = (float)i / (float)n;
+  }
+  const size_t quant = 10;
+  for (size_t i = 0; i < n / quant; ++i) f << Q[i * quant] << "\t" << P[i * quant] << "\n";
+}
+
+int write_distributions(dsm_sim* sim, int n_chains, int cap, bool cd_flag) {
+  std::vector<dsm_chain_head> h(n_chains);
+  std::vector<dsm_float4> q((size_t)n_chains * cap);
+  int rc = dsm_get_chains(sim, h.data(), q.data(), nullptr);
+  if (rc) return rc;
+  // common/main_cuda.cu:169-180
+  const std::string sfx = cd_flag ? "" : "_";
+  write_Z_distr("distr_Z" + sfx + ".dat", h, false);
+  write_N_distr("distr_N" + sfx + ".dat", h, q, cap, false);
+  write_Q_distr("distr_Q" + sfx + ".dat", h, q, cap);
+  return DSM_OK;
+}
+
+}  // namespace dsmc
+
+using namespace dsmc;
+
+extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID, bool distr,
+                         int* progress_bar) {
+  if (job_ID != 0) {
+    std::cout << "job_ID: " << job_ID << '\n';
+    std::cout << "using " << job_ID << " as a seed for random number generator\n";
+    std::cout << "\"_" << job_ID << "\" will be appended to filename for all files generated\n\n";
+  }
+  InputDat in;
+  if (read_input("input.dat", &in) != DSM_OK) {
+    std::cout << "cannot read input.dat\n";
+    return DSM_ERR_INVALID;
+  }
+  dsm_params p;
+  std::memset(&p, 0, sizeof(p));
+  p.beta = in.beta; p.nk = in.nk; p.n_chains = in.n_chains;
+  for (int q = 0; q < 9; ++q) p.kappa[q] = in.kappa[q];
+  p.cd_flag = in.cd_flag; p.pd_flag = in.pd_flag; p.eq_type = in.eq_type;
+  p.sync_dt = in.sync_dt; p.t_end = in.t_end;
+  p.seed = (uint64_t)(uint32_t)job_ID;
+  p.device = device_ID;
+  const bool flow = std::any_of(in.kappa, in.kappa + 9, [](float k) { return k != 0.0f; });
+  const int s_levels = (int)std::ceil(std::log(in.t_end / in.sync_dt / 64.0) / std::log(8.0)) + 1;
+
+  std::cout << "\nsimulation parameters:\n";
+  std::cout << "NK\tBeta\tN_cha" << "\n";
+  std::cout << in.nk << '\t' << in.beta << '\t' << in.n_chains << "\n";
+  std::cout << "deformation tensor:" << "\n";
+  std::cout << in.kappa[0] << '\t' << in.kappa[1] << '\t' << in.kappa[2] << '\n' << in.kappa[3] << '\t'
+            << in.kappa[4] << '\t' << in.kappa[5] << '\n' << in.kappa[6] << '\t' << in.kappa[7] << '\t'
+            << in.kappa[8] << '\n';
+  if (in.eq_type == 1) std::cout << "G(t) calculation is on\n";
+  else if (in.eq_type == 2) std::cout << "MSD(t) calculation is on\n";
+  std::cout << "simulation time, sync time" << "\n";
+  std::cout << in.t_end << '\t' << in.sync_dt << '\n';
+  std::cout << "number of correlator levels" << '\t' << s_levels << '\n' << '\n';
+
+  dsm_sim* sim = nullptr;
+  int rc = dsm_create(&p, &sim);
+  if (rc != DSM_OK) {
+    std::cout << "setup failed: " << dsm_last_error(sim) << "\n";
+    dsm_destroy(sim);
+    return rc;
+  }
+  if (loadfile != nullptr) {
+    std::cout << "loading chain conformations from " << loadfile << "..";
+    rc = dsm_load_file(sim, loadfile);
+    std::cout << (rc == DSM_OK ? "done.\n" : "failed.\n");
+  } else {
+    std::cout << "generating equilibrium chain conformations on device..";
+    rc = dsm_init_equilibrium(sim);
+    std::cout << "done\n";
+  }
+  if (rc != DSM_OK) {
+    std::cout << dsm_last_error(sim) << "\n";
+    dsm_destroy(sim);
+    return rc;
+  }
+  volatile int32_t abort_word = 0;
+  auto poll = [&]() { if (run_flag && !*run_flag) abort_word = 1; };
+  const auto t0 = std::chrono::steady_clock::now();
+  if (flow) {
+    std::ofstream tau_file(filename_ID("tau", job_ID));
+    std::cout << "output file: " << filename_ID("tau", job_ID) << '\n';
+    std::cout << "performing time evolution for the ensemble..\n";
+    std::cout << "time\tstress tensor(xx yy zz xy yz xz)\t<Lpp>\t<Z>\n";
+    for (double t_step = 0; t_step < in.t_end; t_step += in.sync_dt) {
+      poll();
+      rc = dsm_advance(sim, t_step + in.sync_dt, -1, &abort_word, nullptr);
+      if (rc == DSM_ABORTED) { dsm_destroy(sim); return -1; }
+      if (rc != DSM_OK) { std::cout << dsm_last_error(sim) << "\n"; dsm_destroy(sim); return rc; }
+      dsm_stress_plus sp;
+      dsm_stress(sim, &sp, nullptr);
+      std::cout << t_step + in.sync_dt << '\t' << sp.xx << ' ' << sp.yy << ' ' << sp.zz << ' ' << sp.xy << ' '
+                << sp.yz << ' ' << sp.zx << ' ' << sp.Lpp << ' ' << sp.Z << '\n';
+      tau_file << t_step + in.sync_dt << '\t' << sp.xx << ' ' << sp.yy << ' ' << sp.zz << ' ' << sp.xy << ' '
+               << sp.yz << ' ' << sp.zx << ' ' << sp.Lpp << ' ' << sp.Z << '\n';
+      tau_file.flush();
+      if (progress_bar) *progress_bar = (int)(100.0 * (t_step + in.sync_dt) / in.t_end);
+    }
+    std::cout << "time evolution done.\n";
+  } else if (in.eq_type == 1) {
+    std::cout << "G(t) calc...\n";
+    if (progress_bar) *progress_bar = 1;
+    // windows of at most 1e5 tau_K (max_sync_interval, ensemble_call_block.cu:24)
+    const double win = std::max(in.sync_dt, 1.0e5);
+    for (double t = 0; t < in.t_end;) {
+      const double te = std::min(in.t_end, t + win);
+      poll();
+      rc = dsm_advance(sim, te, -1, &abort_word, nullptr);
+      if (rc == DSM_ABORTED) { dsm_destroy(sim); return -1; }
+      if (rc != DSM_OK) { std::cout << dsm_last_error(sim) << "\n"; dsm_destroy(sim); return rc; }
+      t = te;
+      if (progress_bar) *progress_bar = (int)(100.0 * t / in.t_end);
+      std::cout << "\r" << (int)(100.0 * t / in.t_end) << "%\t ";
+    }
+    int32_t n = 4096;
+    std::vector<float> tt(n), gg(n);
+    rc = dsm_gt(sim, tt.data(), gg.data(), &n);
+    if (rc != DSM_OK) { std::cout << dsm_last_error(sim) << "\n"; dsm_destroy(sim); return rc; }
+    std::ofstream gf(filename_ID("G", job_ID));
+    std::cout << "\n";
+    for (int j = 0; j < n; ++j) {
+      std::cout << tt[j] << '\t' << gg[j] << '\n';
+      gf << tt[j] << '\t' << gg[j] << '\n';
+    }
+  } else if (in.eq_type == 2) {
+    std::cout << "MSD(t) calculation is not available in this build\n";
+  } else {
+    std::cout << "There are no flow and no equilibrium quantity to calculate. Exiting... \n";
+  }
+  if (savefile != nullptr) {
+    std::cout << "saving chain conformations to " << savefile << "..";
+    rc = dsm_save_file(sim, savefile);
+    std::cout << (rc == DSM_OK ? "done.\n" : "failed.\n");
+  }
+  if (distr) {
+    std::cout << "Saving distribution to file...";
+    int32_t zmax = 0;
+    (void)zmax;
+    write_distributions(sim, in.n_chains, in.nk, in.cd_flag != 0);
+  }
+  dsm_destroy(sim);
+  const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  std::cout << "Calculation time: " << ms << " milliseconds\n";
+  return 0;
+}

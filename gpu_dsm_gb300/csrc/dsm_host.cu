@@ -1,0 +1,576 @@
+// Host runtime of the C ABI (include/dsm.h): owns one ensemble on one GPU,
+// builds the per-N rate tables and the lifetime-law constants, launches the
+// sm_103a kernels of dsm_kernels.cu and moves conformations in the reference
+// layout.  Replaces the process-global ensemble / call-block machinery of the
+// reference (common/ensemble.cu, common/ensemble_call_block.cu).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/dsm.h"
+#include "dsm_host.h"
+#include "dsm_internal.h"
+
+using namespace dsm;
+
+// ------------------------------------------------------------------ p_cd
+// common/pcd_tau.h:32-66 evaluated in double; device form gpu_random.cu:78-99
+HostPcd dsm::make_pcd(double Be, double Nk) {
+  HostPcd p{};
+  const double z = (Nk + Be) / (Be + 1.0);
+  p.g = 0.667;
+  if ((float)Be != 1.0f) {
+    p.alpha = (0.053 * std::log(Be) + 0.31) * std::pow(z, -0.012 * std::log(Be) - 0.024);
+    p.tau_0 = 0.285 * std::pow(Be + 2.0, 0.515);
+    p.tau_max = (Nk < 2) ? p.tau_0 : 0.025 * std::pow(Be + 2.0, 2.6) * std::pow(z, 2.83);
+    p.tau_d = (Nk < 2) ? p.tau_0 : 0.036 * std::pow(Be + 2.0, 3.07) * std::pow(z - 1.0, 3.02);
+  } else {
+    p.alpha = 0.267096 - 0.375571 * std::exp(-0.0838237 * Nk);
+    p.tau_0 = 0.460277 + 0.298913 * std::exp(-0.0705314 * Nk);
+    p.tau_max = (Nk < 4) ? p.tau_0 : 0.0156137 * std::pow(Nk, 3.18849);
+    p.tau_d = (Nk < 4) ? p.tau_0 : 0.0740131 * std::pow(Nk, 3.18363);
+  }
+  p.c1 = std::pow(p.tau_max, p.alpha) - std::pow(p.tau_0, p.alpha);
+  p.cm1 = std::pow(p.tau_max, p.alpha - 1.0) - std::pow(p.tau_0, p.alpha - 1.0);
+  p.rcm1c1 = (p.c1 == 0.0) ? (p.alpha - 1.0) / p.alpha / p.tau_0 : p.cm1 / p.c1;
+  p.At = 1.0 - p.g;
+  p.Adt = p.At * p.alpha / (p.alpha - 1.0);
+  p.Bdt = p.Adt * p.rcm1c1;
+  p.normdt = p.Bdt + p.g / p.tau_d;
+  PcdDev& d = p.dev;
+  d.At_ = (float)(p.c1 / p.At);
+  d.Dt_ = (float)std::pow(p.tau_0, p.alpha);
+  d.Ct_ = (float)(-1.0 / p.alpha);
+  d.Adt_ = (float)(p.normdt * p.c1 / p.Adt);
+  d.Bdt_ = (float)(p.Bdt / p.normdt);
+  d.Cdt_ = (float)(-1.0 / (p.alpha - 1.0));
+  d.Ddt_ = (float)std::pow(p.tau_0, p.alpha - 1.0);
+  d.tau_d_inv = (float)(1.0 / p.tau_d);
+  d.one_minus_g = (float)(1.0 - p.g);
+  d.normdt = (float)p.normdt;
+  d.pad_[0] = d.pad_[1] = 0.f;
+  return p;
+}
+
+// Per-N factors of the sliding rates (ensemble_kernel.cu:153-178,219-260)
+// in double, rounded to float.  x^0.75 = sqrt(x)*sqrt(sqrt(x)).
+static double pow075(double x) { return std::sqrt(x) * std::sqrt(std::sqrt(x)); }
+
+void dsm::make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off) {
+  const size_t n = (size_t)nmax + 2;
+  off.SIGP = 0; off.SIGM = n; off.PWP = 2 * n; off.PWM = 3 * n; off.SDC = 4 * n; off.SDD2 = 5 * n;
+  off.SDDN = 6 * n; off.CDC = 7 * n; off.INV3N = 8 * n; off.FRIC = 9 * n;
+  const size_t nf = 8 * n + 8;
+  buf.assign(9 * n + nf, 0.f);
+  for (size_t N = 1; N < n; ++N) {
+    const double d = (double)N;
+    buf[off.SIGP + N] = (float)(0.75 / (d * (d + 1.0)));
+    buf[off.SIGM + N] = N >= 2 ? (float)(0.75 / (d * (d - 1.0))) : 0.f;
+    buf[off.PWP + N] = (float)pow075(d / (d + 1.0));
+    buf[off.PWM + N] = N >= 2 ? (float)pow075(d / (d - 1.0)) : 0.f;
+    buf[off.SDC + N] = (float)(2.0 / (beta_f * (d + 0.5)));
+    buf[off.SDD2 + N] = (float)(1.0 / (0.75 + (d + 0.25)));
+    buf[off.SDDN + N] = (float)(1.0 / (0.75 + 0.5 * d));
+    buf[off.CDC + N] = (float)((double)prefact * (d - 1.0));
+    buf[off.INV3N + N] = (float)(3.0 / d);
+  }
+  for (size_t i = 1; i < nf; ++i) buf[off.FRIC + i] = (float)(4.0 / (double)i);
+}
+
+// ------------------------------------------------------------------ helpers
+static int fail(dsm_sim* s, int code, const std::string& msg) {
+  if (s) s->err = msg;
+  return code;
+}
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(s, DSM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+int dsm::corr_levels_for(double t_end, double dt, int p, int m) {
+  // main_cuda.cu:70
+  const double v = std::ceil(std::log(t_end / dt / p) / std::log((double)m)) + 1.0;
+  return v < 1.0 ? 1 : (int)v;
+}
+
+static bool is_flow(const float* k) {
+  for (int q = 0; q < 9; ++q) if (k[q] != 0.0f) return true;
+  return false;
+}
+
+// ------------------------------------------------------------------ lifecycle
+extern "C" int dsm_create(const dsm_params* p, dsm_sim** out) {
+  if (!p || !out) return DSM_ERR_INVALID;
+  *out = nullptr;
+  dsm_sim* s = new dsm_sim();
+  s->P = *p;
+  const int rc = dsm::sim_setup(s);
+  if (rc != DSM_OK) {
+    // keep the handle so that dsm_last_error can report; caller destroys it
+    *out = s;
+    return rc;
+  }
+  *out = s;
+  return DSM_OK;
+}
+
+int dsm::sim_setup(dsm_sim* s) {
+  dsm_params& P = s->P;
+  if (P.nk < 1 || P.n_chains < 1 || !(P.beta > 0.0f)) return fail(s, DSM_ERR_INVALID, "invalid nk / n_chains / beta");
+  if (P.pd_flag != 0) return fail(s, DSM_ERR_INVALID, "GEX background polydispersity (pd_flag=1) is not supported");
+  s->flow = is_flow(P.kappa);
+  s->cap = P.z_max > 0 ? P.z_max : P.nk;
+  if (s->cap < 1) return fail(s, DSM_ERR_INVALID, "z_max");
+  if (s->cap > 4096) return fail(s, DSM_ERR_INVALID, "z_max above 4096 strands per chain");
+  s->poly = P.nk_chain != nullptr;
+  s->nk_chain.assign(P.n_chains, P.nk);
+  int nkmax = P.nk;
+  if (s->poly) {
+    nkmax = 0;
+    for (int i = 0; i < P.n_chains; ++i) {
+      if (P.nk_chain[i] < 1) return fail(s, DSM_ERR_INVALID, "nk_chain entry < 1");
+      s->nk_chain[i] = P.nk_chain[i];
+      nkmax = std::max(nkmax, P.nk_chain[i]);
+    }
+  }
+  P.nk_chain = nullptr;
+  s->nkmax = nkmax;
+  const double be = (double)P.beta;
+  s->pcd = make_pcd(be, (double)P.nk);
+  if (s->poly) {
+    s->pcd_by_nk.assign(nkmax + 1, PcdDev{});
+    std::vector<char> seen(nkmax + 1, 0);
+    std::vector<double> normdt(nkmax + 1, 0.0);
+    for (int v : s->nk_chain)
+      if (!seen[v]) { seen[v] = 1; HostPcd h = make_pcd(be, v); s->pcd_by_nk[v] = h.dev; normdt[v] = h.normdt; }
+    double acc = 0.0;
+    for (int v : s->nk_chain) acc += normdt[v];
+    s->prefact = (float)((acc / P.n_chains) / be);
+  } else {
+    s->prefact = (float)(s->pcd.normdt / be);  // ensemble.cu:148
+  }
+  s->corr = (!s->flow) && P.eq_type == 1 && P.sync_dt > 0 && P.t_end > 0;
+  s->cp = P.corr_p > 0 ? P.corr_p : 64;
+  s->cm = P.corr_m > 0 ? P.corr_m : 8;
+  if (s->cp % s->cm != 0 || s->cp > 256) return fail(s, DSM_ERR_INVALID, "correlator p must be a multiple of m and <= 256");
+  s->levels = P.corr_levels > 0 ? P.corr_levels : (s->corr ? corr_levels_for(P.t_end, P.sync_dt, s->cp, s->cm) : 1);
+  s->nsamples = s->corr ? (int64_t)std::ceil(P.t_end / P.sync_dt) : 0;
+
+  CK(cudaSetDevice(P.device));
+  CK(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, P.device));
+  s->sm_count = prop.multiProcessorCount;
+
+  // device memory budget
+  const size_t n = (size_t)P.n_chains, cap = (size_t)s->cap;
+  size_t need = n * cap * (16 + 4) + n * sizeof(ChainState) + n * 8 * 4;
+  if (s->corr) need += n * s->levels * ((size_t)s->cp * (12 + 8) + 12 + 16);
+  size_t fre = 0, tot = 0;
+  CK(cudaMemGetInfo(&fre, &tot));
+  if (need + (64ull << 20) > fre) return fail(s, DSM_ERR_MEMORY, "ensemble needs " + std::to_string(need >> 20) + " MiB of device memory, " + std::to_string(fre >> 20) + " MiB free");
+  s->bytes = need;
+
+  // tables
+  std::vector<float> tb;
+  TableOffsets to;
+  make_tables(nkmax, be, s->prefact, tb, to);
+  CK(cudaMalloc(&s->d_tables, tb.size() * sizeof(float)));
+  CK(cudaMemcpy(s->d_tables, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+  // state
+  CK(cudaMalloc(&s->d_QN, n * cap * sizeof(float4)));
+  CK(cudaMalloc(&s->d_tau, n * cap * sizeof(float)));
+  CK(cudaMalloc(&s->d_cs, n * sizeof(ChainState)));
+  CK(cudaMalloc(&s->d_stress, n * 8 * sizeof(float)));
+  CK(cudaMemset(s->d_QN, 0, n * cap * sizeof(float4)));
+  CK(cudaMemset(s->d_tau, 0, n * cap * sizeof(float)));
+  CK(cudaMemset(s->d_cs, 0, n * sizeof(ChainState)));
+  CK(cudaMemset(s->d_stress, 0, n * 8 * sizeof(float)));
+  if (s->corr) {
+    const size_t L = s->levels, pp = s->cp;
+    CK(cudaMalloc(&s->d_cshift, n * L * pp * 3 * sizeof(float)));
+    CK(cudaMalloc(&s->d_cacc, n * L * pp * sizeof(double)));
+    CK(cudaMalloc(&s->d_cavg, n * L * 3 * sizeof(float)));
+    CK(cudaMalloc(&s->d_ccnt, n * L * sizeof(int4)));
+    CK(cudaMalloc(&s->d_gsum, L * pp * sizeof(double)));
+    CK(cudaMalloc(&s->d_gcnt, L * pp * sizeof(long long)));
+  }
+  if (s->poly) {
+    CK(cudaMalloc(&s->d_pcd_by_nk, s->pcd_by_nk.size() * sizeof(PcdDev)));
+    CK(cudaMemcpy(s->d_pcd_by_nk, s->pcd_by_nk.data(), s->pcd_by_nk.size() * sizeof(PcdDev), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&s->d_nk_chain, n * sizeof(int32_t)));
+    CK(cudaMemcpy(s->d_nk_chain, s->nk_chain.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
+  CK(cudaMalloc(&s->d_ens, sizeof(EnsDev)));
+  CK(cudaMalloc(&s->d_prefix, 2 * sizeof(long long)));
+  CK(cudaMalloc(&s->d_work, sizeof(unsigned int)));
+  CK(cudaMalloc(&s->d_status, sizeof(int)));
+  CK(cudaMalloc(&s->d_counters, 4 * sizeof(unsigned long long)));
+  CK(cudaMalloc(&s->d_red, 16 * sizeof(double)));
+  CK(cudaEventCreate(&s->ev0));
+  CK(cudaEventCreate(&s->ev1));
+  CK(cudaHostAlloc(&s->h_abort, sizeof(int), cudaHostAllocMapped));
+  *s->h_abort = 0;
+  CK(cudaHostGetDevicePointer((void**)&s->d_abort, (void*)s->h_abort, 0));
+  const long long pre[2] = {0, (long long)P.n_chains};
+  CK(cudaMemcpy(s->d_prefix, pre, sizeof(pre), cudaMemcpyHostToDevice));
+
+  // device descriptor
+  EnsDev& E = s->h;
+  std::memset(&E, 0, sizeof(E));
+  E.n_chains = P.n_chains; E.cap = s->cap; E.nk = P.nk; E.cd_flag = P.cd_flag ? 1 : 0;
+  E.flow = s->flow ? 1 : 0; E.s0 = P.s0 > 0 ? P.s0 : 40; E.poly = s->poly ? 1 : 0;
+  E.corr_type = s->corr ? 0 : -1; E.corr_p = s->cp; E.corr_m = s->cm; E.corr_levels = s->levels;
+  E.beta = P.beta; E.prefact = s->prefact; E.beta_d = (double)P.beta;
+  for (int q = 0; q < 9; ++q) E.kap[q] = P.kappa[q];
+  E.seed_lo = (uint32_t)P.seed; E.seed_hi = (uint32_t)(P.seed >> 32); E.stream = P.stream;
+  E.dt_sample_ticks = s->corr ? (int64_t)std::llrint(P.sync_dt * TICKS) : 0;
+  E.nsamples = s->nsamples;
+  E.t_end_ticks = 0; E.step_limit = INT64_MAX; E.watchdog_events = INT64_MAX;
+  E.pcd = s->pcd.dev;
+  E.pcd_by_nk = s->d_pcd_by_nk; E.nk_chain = s->d_nk_chain;
+  E.SIGP = s->d_tables + to.SIGP; E.SIGM = s->d_tables + to.SIGM; E.PWP = s->d_tables + to.PWP;
+  E.PWM = s->d_tables + to.PWM; E.FRIC = s->d_tables + to.FRIC; E.SDC = s->d_tables + to.SDC;
+  E.SDD2 = s->d_tables + to.SDD2; E.SDDN = s->d_tables + to.SDDN; E.CDC = s->d_tables + to.CDC;
+  E.INV3N = s->d_tables + to.INV3N;
+  E.QN = s->d_QN; E.tau = s->d_tau; E.cs = s->d_cs;
+  E.corr_shift = s->d_cshift; E.corr_acc = s->d_cacc; E.corr_avg = s->d_cavg; E.corr_cnt = s->d_ccnt;
+  E.out_stress = s->d_stress; E.counters = s->d_counters;
+  CK(cudaMemcpy(s->d_ens, &E, sizeof(E), cudaMemcpyHostToDevice));
+
+  // launch shape
+  s->cfg.slot_cap = s->cap;
+  s->cfg.pmax = s->corr ? s->cp : 0;
+  s->cfg.warps_per_block = P.warps_per_block > 0 ? P.warps_per_block : 4;
+  if (s->cfg.warps_per_block > 4) s->cfg.warps_per_block = 4;  // __launch_bounds__(128)
+  const size_t smem = step_slot_bytes(s->cfg.slot_cap, s->cfg.pmax) * s->cfg.warps_per_block;
+  if (smem > (size_t)prop.sharedMemPerBlockOptin)
+    return fail(s, DSM_ERR_INVALID, "chain capacity z_max=" + std::to_string(s->cap) + " does not fit one shared-memory slot");
+  const int bps = step_max_blocks_per_sm(s->flow, s->corr, s->cfg);
+  if (bps < 1) return fail(s, DSM_ERR_CUDA, "step kernel cannot be resident (occupancy 0)");
+  s->blocks_per_sm = bps;
+  const long long want = ((long long)P.n_chains + s->cfg.warps_per_block - 1) / s->cfg.warps_per_block;
+  s->grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
+  s->ready = true;
+  return DSM_OK;
+}
+
+extern "C" void dsm_destroy(dsm_sim* s) {
+  if (!s) return;
+  if (s->st) cudaStreamSynchronize(s->st);
+  void* ptrs[] = {s->d_tables, s->d_QN, s->d_tau, s->d_cs, s->d_stress, s->d_cshift, s->d_cacc, s->d_cavg,
+                  s->d_ccnt, s->d_gsum, s->d_gcnt, s->d_pcd_by_nk, s->d_nk_chain, s->d_ens, s->d_prefix,
+                  s->d_work, s->d_status, s->d_counters, s->d_red};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  if (s->h_abort) cudaFreeHost((void*)s->h_abort);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+}
+
+extern "C" const char* dsm_last_error(const dsm_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+extern "C" int dsm_corr_shape(const dsm_sim* s, int32_t* levels, int32_t* p, int32_t* m) {
+  if (!s) return DSM_ERR_INVALID;
+  if (levels) *levels = s->corr ? s->levels : 0;
+  if (p) *p = s->cp;
+  if (m) *m = s->cm;
+  return DSM_OK;
+}
+
+static int reset_corr(dsm_sim* s) {
+  if (!s->corr) return DSM_OK;
+  const size_t n = s->P.n_chains, L = s->levels, pp = s->cp;
+  CK(cudaMemsetAsync(s->d_cshift, 0, n * L * pp * 3 * sizeof(float), s->st));
+  CK(cudaMemsetAsync(s->d_cacc, 0, n * L * pp * sizeof(double), s->st));
+  CK(cudaMemsetAsync(s->d_cavg, 0, n * L * 3 * sizeof(float), s->st));
+  CK(cudaMemsetAsync(s->d_ccnt, 0, n * L * sizeof(int4), s->st));
+  return DSM_OK;
+}
+
+extern "C" int dsm_init_equilibrium(dsm_sim* s) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  CK(cudaMemsetAsync(s->d_QN, 0, (size_t)s->P.n_chains * s->cap * sizeof(float4), s->st));
+  CK(cudaMemsetAsync(s->d_tau, 0, (size_t)s->P.n_chains * s->cap * sizeof(float), s->st));
+  int rc = reset_corr(s);
+  if (rc) return rc;
+  CK(launch_init(s->d_ens, s->h, s->cap, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return DSM_OK;
+}
+
+// ------------------------------------------------------------------ state transfer
+extern "C" int dsm_set_chains(dsm_sim* s, const dsm_chain_head* heads, const dsm_float4* QN, const float* tau) {
+  if (!s || !s->ready || !heads || !QN || !tau) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains, cap = s->cap;
+  std::vector<ChainState> cs(n);
+  for (size_t i = 0; i < n; ++i) {
+    const int Z = heads[i].Z;
+    if (Z < 1 || Z > (int)cap) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": Z out of [1, z_max]");
+    long long sumN = 0;
+    for (int k = 0; k < Z; ++k) {
+      const float w = QN[i * cap + k].w;
+      if (!(w >= 1.0f) || w != std::floor(w)) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": strand with N < 1 or fractional N");
+      sumN += (long long)w;
+    }
+    if (sumN != s->nk_chain[i]) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": sum of N differs from N_K");
+    ChainState& c = cs[i];
+    std::memset(&c, 0, sizeof(c));
+    c.Z = Z; c.stall = heads[i].stall_flag; c.S = s->h.s0; c.dt_prev = 0.f;
+    c.T = (int64_t)std::llrint((double)heads[i].time * TICKS);
+    c.step = 0; c.hash = 0xCBF29CE484222325ull; c.k_next = 0; c.nk = s->nk_chain[i];
+  }
+  CK(cudaMemcpyAsync(s->d_QN, QN, n * cap * sizeof(float4), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->d_tau, tau, n * cap * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(s->d_cs, cs.data(), n * sizeof(ChainState), cudaMemcpyHostToDevice, s->st));
+  int rc = reset_corr(s);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s->st));
+  return DSM_OK;
+}
+
+extern "C" int dsm_get_chains(dsm_sim* s, dsm_chain_head* heads, dsm_float4* QN, float* tau) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains, cap = s->cap;
+  if (QN) CK(cudaMemcpyAsync(QN, s->d_QN, n * cap * sizeof(float4), cudaMemcpyDeviceToHost, s->st));
+  if (tau) CK(cudaMemcpyAsync(tau, s->d_tau, n * cap * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+  std::vector<ChainState> cs(heads ? n : 0);
+  if (heads) CK(cudaMemcpyAsync(cs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (heads)
+    for (size_t i = 0; i < n; ++i) {
+      heads[i].Z = cs[i].Z;
+      heads[i].time = (float)((double)cs[i].T / TICKS);
+      heads[i].dummy = 0.f;
+      heads[i].stall_flag = cs[i].stall;
+    }
+  // slots beyond Z are not maintained on the device; clear them in the copy
+  if (QN || tau) {
+    std::vector<ChainState> zs(n);
+    if (heads) for (size_t i = 0; i < n; ++i) zs[i].Z = heads[i].Z;
+    else {
+      CK(cudaMemcpy(zs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost));
+    }
+    for (size_t i = 0; i < n; ++i) {
+      const int Z = zs[i].Z;
+      for (size_t k = (size_t)std::max(Z, 0); k < cap; ++k) {
+        if (QN) QN[i * cap + k] = dsm_float4{0.f, 0.f, 0.f, 0.f};
+        if (tau) tau[i * cap + k] = 0.f;
+      }
+      if (tau && Z >= 1) tau[i * cap + Z - 1] = 0.f;
+    }
+  }
+  return DSM_OK;
+}
+
+extern "C" int dsm_get_ext(dsm_sim* s, int64_t* T, uint64_t* steps, float* dt_prev, int32_t* stall,
+                           int32_t* scale, uint64_t* hash) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains;
+  std::vector<ChainState> cs(n);
+  CK(cudaMemcpyAsync(cs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  for (size_t i = 0; i < n; ++i) {
+    if (T) T[i] = cs[i].T;
+    if (steps) steps[i] = cs[i].step;
+    if (dt_prev) dt_prev[i] = cs[i].dt_prev;
+    if (stall) stall[i] = cs[i].stall;
+    if (scale) scale[i] = cs[i].S;
+    if (hash) hash[i] = cs[i].hash;
+  }
+  return DSM_OK;
+}
+
+extern "C" int dsm_set_ext(dsm_sim* s, const int64_t* T, const uint64_t* steps, const float* dt_prev,
+                           const int32_t* stall, const int32_t* scale) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains;
+  std::vector<ChainState> cs(n);
+  CK(cudaMemcpyAsync(cs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  for (size_t i = 0; i < n; ++i) {
+    if (T) cs[i].T = T[i];
+    if (steps) cs[i].step = steps[i];
+    if (dt_prev) cs[i].dt_prev = dt_prev[i];
+    if (stall) cs[i].stall = stall[i];
+    if (scale) cs[i].S = scale[i];
+  }
+  CK(cudaMemcpyAsync(s->d_cs, cs.data(), n * sizeof(ChainState), cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return DSM_OK;
+}
+
+// ------------------------------------------------------------------ time evolution
+int dsm::sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit) {
+  EnsDev& E = s->h;
+  E.t_end_ticks = (int64_t)std::llrint(t_end * TICKS);
+  E.step_limit = step_limit < 0 ? INT64_MAX : step_limit;
+  E.watchdog_events = s->watchdog_events > 0 ? s->watchdog_events : INT64_MAX;
+  CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
+  CK(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st));
+  CK(cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), s->st));
+  CK(cudaEventRecord(s->ev0, s->st));
+  CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->corr, s->cfg,
+                 s->d_abort, s->d_status, s->grid, s->st));
+  CK(cudaEventRecord(s->ev1, s->st));
+  return DSM_OK;
+}
+
+int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
+  unsigned long long cnt[4];
+  int status = 0;
+  CK(cudaMemcpyAsync(cnt, s->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  if (s->flow) CK(launch_stress_reduce_dev(s->d_ens, s->d_red, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaGetLastError());
+  if (events) *events = cnt[0];
+  s->events_total += cnt[0];
+  s->last_events = cnt[0];
+  CK(cudaEventElapsedTime(&s->last_kernel_ms, s->ev0, s->ev1));
+  if (status & 1) return DSM_ABORTED;
+  return DSM_OK;
+}
+
+extern "C" int dsm_advance(dsm_sim* s, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
+                           uint64_t* events) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  if (!(t_end >= 0.0) || t_end * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
+  *s->h_abort = (abort_flag && *abort_flag) ? 1 : 0;
+  int rc = sim_launch_window(s, t_end, step_limit);
+  if (rc) return rc;
+  if (abort_flag) {
+    // forward the caller's flag into the mapped word the kernel polls
+    while (cudaStreamQuery(s->st) == cudaErrorNotReady) {
+      if (*abort_flag) *s->h_abort = 1;
+      std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+  }
+  rc = sim_finish_window(s, events);
+  *s->h_abort = 0;
+  return rc;
+}
+
+extern "C" int dsm_stress(dsm_sim* s, dsm_stress_plus* out, int32_t* count) {
+  if (!s || !s->ready || !out) return DSM_ERR_INVALID;
+  if (!s->flow) {
+    // equilibrium ensembles: evaluate the stress of the current state with a
+    // zero-length flow-free pass (same kernel path as a window end)
+    return fail(s, DSM_ERR_INVALID, "dsm_stress is defined for flow ensembles (kappa != 0)");
+  }
+  double r[9];
+  CK(cudaMemcpyAsync(r, s->d_red, sizeof(r), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  const double c = r[8];
+  const double d = c > 0 ? c : 1.0;
+  out->xx = (float)(r[0] / d); out->yy = (float)(r[1] / d); out->zz = (float)(r[2] / d);
+  out->xy = (float)(r[3] / d); out->yz = (float)(r[4] / d); out->zx = (float)(r[5] / d);
+  out->Lpp = (float)(r[6] / d); out->Z = (float)(r[7] / d);
+  if (count) *count = (int32_t)c;
+  return DSM_OK;
+}
+
+extern "C" int dsm_gt_raw(dsm_sim* s, double* gsum, int64_t* count) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  if (!s->corr) return fail(s, DSM_ERR_INVALID, "no correlator in this simulation (eq_type != 1 or flow)");
+  const size_t m = (size_t)s->levels * s->cp;
+  CK(launch_gt_reduce_dev(s->d_ens, s->levels, s->cp, s->d_gsum, s->d_gcnt, s->st));
+  std::vector<long long> c(m);
+  if (gsum) CK(cudaMemcpyAsync(gsum, s->d_gsum, m * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(c.data(), s->d_gcnt, m * sizeof(long long), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (count) for (size_t i = 0; i < m; ++i) count[i] = c[i];
+  return DSM_OK;
+}
+
+// G(t) points in the order and count gpu_Gt_PCS writes them
+// (ensemble.cu:298-335, correlator.cu:242-257)
+extern "C" int dsm_gt(dsm_sim* s, float* t, float* G, int32_t* n) {
+  if (!s || !n) return DSM_ERR_INVALID;
+  const int L = s->levels, p = s->cp, m = s->cm, dmin = p / m;
+  std::vector<double> gs((size_t)L * p);
+  int rc = dsm_gt_raw(s, gs.data(), nullptr);
+  if (rc) return rc;
+  const double res = s->P.sync_dt;
+  const long long np = p + (long long)(L - 1) * (p - dmin);
+  long long actual = np - p + (long long)std::floor(s->P.t_end / (res * std::pow((double)m, L - 1)));
+  if (actual > np) actual = np;
+  if (actual < 0) actual = 0;
+  if (*n < actual) { *n = (int32_t)actual; return fail(s, DSM_ERR_INVALID, "output capacity too small"); }
+  long long im = 0;
+  const double inv = 1.0 / (3.0 * s->P.n_chains);
+  for (int k = 0; k < L && im < actual; ++k)
+    for (int j = (k == 0 ? 0 : dmin); j < p && im < actual; ++j) {
+      if (t) t[im] = (float)(long long)((double)j * std::pow((double)m, k));
+      if (G) G[im] = (float)(gs[(size_t)k * p + j] * inv);
+      ++im;
+    }
+  *n = (int32_t)im;
+  return DSM_OK;
+}
+
+// ------------------------------------------------------------------ reference files
+extern "C" int dsm_save_file(dsm_sim* s, const char* path) {
+  if (!s || !path) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains, cap = s->cap;
+  std::vector<dsm_chain_head> h(n);
+  std::vector<dsm_float4> q(n * cap);
+  std::vector<float> t(n * cap);
+  int rc = dsm_get_chains(s, h.data(), q.data(), t.data());
+  if (rc) return rc;
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return fail(s, DSM_ERR_INVALID, std::string("cannot open ") + path);
+  const int32_t nc = (int32_t)n;
+  f.write((const char*)&nc, 4);  // ensemble.cu:346
+  for (size_t i = 0; i < n; ++i) {  // chain.cu:304-310
+    f.write((const char*)&h[i], sizeof(dsm_chain_head));
+    f.write((const char*)&q[i * cap], (std::streamsize)(sizeof(dsm_float4) * h[i].Z));
+    f.write((const char*)&t[i * cap], (std::streamsize)(sizeof(float) * h[i].Z));
+  }
+  return f ? DSM_OK : fail(s, DSM_ERR_INVALID, "write failed");
+}
+
+extern "C" int dsm_load_file(dsm_sim* s, const char* path) {
+  if (!s || !path) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains, cap = s->cap;
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return fail(s, DSM_ERR_INVALID, std::string("cannot open ") + path);
+  int32_t nc = 0;
+  f.read((char*)&nc, 4);
+  if (nc != (int32_t)n) return fail(s, DSM_ERR_INVALID, "ensemble size mismatch");  // ensemble.cu:493-496
+  std::vector<dsm_chain_head> h(n);
+  std::vector<dsm_float4> q(n * cap, dsm_float4{0, 0, 0, 0});
+  std::vector<float> t(n * cap, 0.f);
+  for (size_t i = 0; i < n; ++i) {  // chain.cu:312-318
+    f.read((char*)&h[i], sizeof(dsm_chain_head));
+    if (!f || h[i].Z < 1 || h[i].Z > (int)cap) return fail(s, DSM_ERR_INVALID, "corrupt conformation file");
+    f.read((char*)&q[i * cap], (std::streamsize)(sizeof(dsm_float4) * h[i].Z));
+    f.read((char*)&t[i * cap], (std::streamsize)(sizeof(float) * h[i].Z));
+    if (!f) return fail(s, DSM_ERR_INVALID, "truncated conformation file");
+  }
+  return dsm_set_chains(s, h.data(), q.data(), t.data());
+}
+
+extern "C" int dsm_last_window(const dsm_sim* s, float* kernel_ms, uint64_t* events, int32_t* grid,
+                               int32_t* blocks_per_sm) {
+  if (!s) return DSM_ERR_INVALID;
+  if (kernel_ms) *kernel_ms = s->last_kernel_ms;
+  if (events) *events = s->last_events;
+  if (grid) *grid = s->grid;
+  if (blocks_per_sm) *blocks_per_sm = s->blocks_per_sm;
+  return DSM_OK;
+}

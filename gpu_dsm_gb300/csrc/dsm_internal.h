@@ -1,0 +1,94 @@
+// Internal layouts shared by the host runtime (dsm_host.cu) and the sm_103a
+// kernels (dsm_kernels.cu).  Not part of the public C ABI (include/dsm.h).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dsm {
+
+constexpr int LIMIT_E = 47;            // fixed-point rate components stay below 2^48
+constexpr int S_HYST = 16;             // flow: raise the scale again when 2^16 headroom is free
+constexpr double TICKS = 4294967296.0; // chain time unit: 2^-32 tau_K
+
+// Event codes (also folded into the per-chain event hash)
+enum Ev : int { CDD = 0, SDP = 1, SDM = 2, CDC_MID = 3, CDC_TAIL = 4, SDC_HEAD = 5,
+                SDC_TAIL = 6, SDD_HEAD = 7, SDD_TAIL = 8, NULL_FLAG = 16 };
+
+// Stall / status codes kept per chain (reference: ensemble_kernel.cu:265-270)
+enum Stall : int { ST_OK = 0, ST_DT_ZERO = 1, ST_NAN = 2, ST_INF = 3, ST_WATCHDOG = 5 };
+
+// Device form of the lifetime law of a partner chain (gpu_random.cu:78-99)
+struct PcdDev {
+  float At_, Dt_, Ct_, Adt_, Bdt_, Cdt_, Ddt_, tau_d_inv, one_minus_g;
+  float normdt;
+  float pad_[2];
+};
+
+// Per-chain scalar state, 64 bytes, array of structs in HBM.
+struct ChainState {
+  int32_t Z;          // strands
+  int32_t stall;      // stall code
+  int32_t S;          // fixed-point scale exponent of the rate components
+  float dt_prev;      // previous dt (flow deformation is applied at the next step)
+  int64_t T;          // chain time in ticks (2^-32 tau_K)
+  uint64_t step;      // kMC events done by this chain (Philox counter)
+  uint64_t hash;      // running FNV-style hash of the event sequence
+  int64_t k_next;     // next stress-sample index
+  int32_t nk;         // Kuhn steps of this chain
+  int32_t pad_[3];
+};
+static_assert(sizeof(ChainState) == 64, "ChainState layout");
+
+// Everything one kernel needs to know about one ensemble (device copy).
+struct EnsDev {
+  int32_t n_chains, cap, nk, cd_flag;
+  int32_t flow, s0, poly, corr_type;
+  int32_t corr_p, corr_m, corr_levels, pad0_;
+  float beta, prefact;
+  double beta_d;
+  float kap[9];
+  uint32_t seed_lo, seed_hi, stream;
+  int64_t dt_sample_ticks, nsamples;
+  // window of the current launch
+  int64_t t_end_ticks;       // chains stop when T >= t_end_ticks
+  int64_t step_limit;        // ... or when step >= step_limit
+  int64_t watchdog_events;   // max events per chain per launch (stall 5 beyond)
+  PcdDev pcd;                // monodisperse partner law
+  const PcdDev* pcd_by_nk;   // polydisperse: partner law by N_K
+  const int32_t* nk_chain;   // polydisperse: N_K of every chain
+  // per-N tables
+  const float *SIGP, *SIGM, *PWP, *PWM, *FRIC, *SDC, *SDD2, *SDDN, *CDC, *INV3N;
+  // state (reference layout: float4 {Qx,Qy,Qz,N} x cap per chain; tau rate x cap)
+  float4* QN;
+  float* tau;
+  ChainState* cs;
+  // multi-tau correlator per chain: [chain][level][p][3] shift, [chain][level][p]
+  // FP64 correlation sums, [chain][level][3] block averages, [chain][level]
+  // counters {insert index, block count, values lo, values hi}
+  float* corr_shift;
+  double* corr_acc;
+  float* corr_avg;
+  int4* corr_cnt;
+  float* out_stress;               // [chain][8] stress at the end of the launch (flow)
+  unsigned long long* counters;    // [0] events this launch, [1] chains done
+};
+
+struct LaunchCfg {
+  int warps_per_block;
+  int slot_cap;        // strands per SMEM slot (max cap of the ensembles launched)
+  int pmax;            // correlator points per level (max over ensembles)
+};
+
+__host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax);
+
+// kernels (dsm_kernels.cu)
+cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
+cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
+                        unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
+                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st);
+int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg);
+cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
+                                 cudaStream_t st);
+cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st);
+
+}  // namespace dsm

@@ -1,0 +1,936 @@
+// sm_103a kernels of the DSM kinetic Monte Carlo path.
+//
+// Design (one GB300, one process):
+//   * Each chain is simulated by ONE WARP that keeps the whole chain in shared
+//     memory (SoA slot: Q+Q^2 float4, N int, tau rate float, quantised pair
+//     rate uint64) inside a persistent loop.  Warps pull chains from an atomic
+//     work counter, load them with coalesced float4 loads, run them to the end
+//     of the launch window and write them back: HBM is touched only at window
+//     boundaries (and by the long-lag correlator levels).
+//   * The event pick is exact integer arithmetic: every rate component is
+//     quantised to int64 fixed point (scale 2^S per chain), each lane sums a
+//     contiguous odd-width chunk of pair totals (bank-conflict free), a warp
+//     inclusive scan + ballot finds the lane, the lane walks its chunk.  The
+//     result does not depend on summation order, so the oracle reproduces it.
+//   * Equilibrium: only the <=3 pair rates touched by an event are recomputed
+//     (the reference recomputes all of them every step, ensemble_kernel.cu
+//     strent_kernel).  Flow: all strands are deformed and all rates
+//     recomputed every step, as in the reference.
+//   * Insert/remove of strands is a warp-cooperative memmove in shared memory
+//     (the reference defers it to the next step, ensemble_kernel.cu:64-102).
+//   * Randomness: Philox4x32-10; lane l computes the event words of step
+//     base+l, so one Philox evaluation serves 32 consecutive events.
+//   * No tensor cores: nothing on this path is a dense contraction.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dsm_internal.h"
+#include "dsm_math.cuh"
+
+namespace dsm {
+
+#define FULL_MASK 0xffffffffu
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ unsigned long long warp_incl_scan_u64(unsigned long long v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(FULL_MASK, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(FULL_MASK, v, o));
+  return v;
+}
+
+__device__ __forceinline__ int warp_max_i(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL_MASK, v, o));
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long quant(float x, float sf) {
+  return (unsigned long long)__float2ll_rn(__fmul_rn(x, sf));
+}
+
+// Philox words of one event / one creation (counter layout shared with the oracle)
+__device__ __forceinline__ U4 rng_at(const EnsDev& E, uint32_t purpose, uint64_t ctr, uint32_t hi24,
+                                     uint32_t chain) {
+  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain, E.stream, E.seed_lo, E.seed_hi);
+}
+
+// Lifetime samplers returning rates (gpu_random.cu:143-148, pcd_tau.h:67-82)
+__device__ __forceinline__ float rate_f_t(const PcdDev& p, float u) {
+  return (u < p.one_minus_g) ? m_pow(__fmaf_rn(u, p.At_, p.Dt_), p.Ct_) : p.tau_d_inv;
+}
+__device__ __forceinline__ float rate_f_dt(const PcdDev& p, float u) {
+  return (u < p.Bdt_) ? m_pow(__fmaf_rn(u, p.Adt_, p.Ddt_), p.Cdt_) : p.tau_d_inv;
+}
+__device__ __forceinline__ PcdDev partner_pcd(const EnsDev& E, uint32_t w) {
+  if (!E.poly) return E.pcd;
+  const uint32_t idx = __umulhi(w, (uint32_t)E.n_chains);
+  return E.pcd_by_nk[__ldg(&E.nk_chain[idx])];
+}
+
+// Components {CD destruction, shift N1+1, shift N1-1, CD creation} of the pair
+// (strand j, strand j+1): ensemble_kernel.cu:149-181,304-414.
+__device__ __forceinline__ void pair_comp(const EnsDev& E, int N1, float q1, int N2, float q2,
+                                          float taurate, float o[4]) {
+  const bool z1 = (q1 == 0.0f), z2 = (q2 == 0.0f);
+  float wp = 0.0f, wm = 0.0f;
+  if (N2 > 1) {
+    const int i = (z1 ? 4 * N1 + 1 : 2 * N1) + (z2 ? 4 * N2 - 1 : 2 * N2);
+    const float t2 = __fmul_rn(q2, __ldg(&E.SIGM[N2]));
+    const float arg = __fmaf_rn(q1, __ldg(&E.SIGP[N1]), -t2);
+    const float pw = __fmul_rn(z1 ? 1.0f : __ldg(&E.PWP[N1]), z2 ? 1.0f : __ldg(&E.PWM[N2]));
+    wp = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
+  }
+  if (N1 > 1) {
+    const int i = (z1 ? 4 * N1 - 1 : 2 * N1) + (z2 ? 4 * N2 + 1 : 2 * N2);
+    const float t1 = __fmul_rn(q1, __ldg(&E.SIGM[N1]));
+    const float arg = __fmaf_rn(q2, __ldg(&E.SIGP[N2]), -t1);
+    const float pw = __fmul_rn(z1 ? 1.0f : __ldg(&E.PWM[N1]), z2 ? 1.0f : __ldg(&E.PWP[N2]));
+    wm = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
+  }
+  o[0] = E.cd_flag ? taurate : 0.0f;
+  o[1] = wp;
+  o[2] = wm;
+  o[3] = E.cd_flag ? __ldg(&E.CDC[N1]) : 0.0f;
+}
+
+// Chain-end rate q (0 CD creation at the tail, 1 SD creation head, 2 SD
+// creation tail, 3 SD destruction head, 4 SD destruction tail):
+// ensemble_kernel.cu:219-260.
+__device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const int* sN, float wz1) {
+  const int Nh = sN[0], Nt = sN[Z - 1];
+  switch (q) {
+    case 0: return E.cd_flag ? __ldg(&E.CDC[Nt]) : 0.0f;
+    case 1: return Z == 1 ? wz1 : (Nh == 1 ? 0.0f : __ldg(&E.SDC[Nh]));
+    case 2: return Z == 1 ? wz1 : (Nt == 1 ? 0.0f : __ldg(&E.SDC[Nt]));
+    case 3: return (Z == 1 || Nh != 1) ? 0.0f : (Z == 2 ? __ldg(&E.SDD2[sN[1]]) : __ldg(&E.SDDN[sN[1]]));
+    case 4: return (Z == 1 || Nt != 1) ? 0.0f : (Z == 2 ? __ldg(&E.SDD2[sN[Z - 2]]) : __ldg(&E.SDDN[sN[Z - 2]]));
+    default: return 0.0f;
+  }
+}
+
+// status flags of a component: bit0 NaN, bit1 inf
+__device__ __forceinline__ int comp_bad(float x) {
+  return (x != x) ? 1 : ((__float_as_uint(x) == 0x7f800000u) ? 2 : 0);
+}
+
+// ------------------------------------------------------------------ SMEM slot
+struct Slot {
+  float4* Q;                // {Qx, Qy, Qz, Q^2} per strand
+  unsigned long long* R;    // quantised pair totals
+  int* N;                   // Kuhn steps per strand
+  float* T;                 // CD lifetime rates per entanglement
+  float* Csh;               // correlator level-0 shift register [p][3]
+  float2* Cacc;             // correlator level-0 compensated sums [p]
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax) {
+  const size_t n = (size_t)slot_cap + 1;
+  size_t b = n * 16 + n * 8 + n * 4 + n * 4;
+  b = align_up(b, 8) + (size_t)pmax * 12;
+  b = align_up(b, 8) + (size_t)pmax * 8;
+  return align_up(b, 16);
+}
+
+__device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int pmax) {
+  Slot s;
+  const size_t n = (size_t)slot_cap + 1;
+  s.Q = (float4*)base;
+  s.R = (unsigned long long*)(base + n * 16);
+  s.N = (int*)(base + n * 24);
+  s.T = (float*)(base + n * 28);
+  size_t off = align_up(n * 32, 8);
+  s.Csh = (float*)(base + off);
+  off = align_up(off + (size_t)pmax * 12, 8);
+  s.Cacc = (float2*)(base + off);
+  return s;
+}
+
+// warp-cooperative moves inside the slot
+template <class T>
+__device__ __forceinline__ void move_up(T* a, int lo, int hi, int lane) {  // [lo,hi) -> [lo+1,hi+1)
+  for (int top = hi - 1; top >= lo; top -= 32) {
+    const int s = top - lane;
+    T v;
+    const bool act = s >= lo;
+    if (act) v = a[s];
+    __syncwarp();
+    if (act) a[s + 1] = v;
+    __syncwarp();
+  }
+}
+template <class T>
+__device__ __forceinline__ void move_down(T* a, int lo, int hi, int lane) {  // [lo,hi) -> [lo-1,hi-1)
+  for (int bot = lo; bot < hi; bot += 32) {
+    const int s = bot + lane;
+    T v;
+    const bool act = s < hi;
+    if (act) v = a[s];
+    __syncwarp();
+    if (act) a[s - 1] = v;
+    __syncwarp();
+  }
+}
+
+// recompute quantised pair totals of pairs [p0, p0+cnt) (cnt <= 32) in
+// parallel; returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 overflow
+__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt,
+                                            int lane) {
+  int flags = 0;
+  const int p = p0 + lane;
+  if (lane < cnt && p >= 0 && p < Z - 1) {
+    float o[4];
+    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
+    const float sf = pow2f(S);
+    unsigned long long tot = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      flags |= comp_bad(o[q]);
+      if (fexp(o[q]) + S > LIMIT_E) flags |= 4;
+      tot += quant(o[q], sf);
+    }
+    sl.R[p] = tot;
+  }
+  __syncwarp();
+  return __reduce_or_sync(FULL_MASK, flags);
+}
+
+// full pass over all pairs: float components -> max exponent & flags, then
+// quantise with the scale chosen by the rule shared with the oracle.
+// Returns the new S; *flags gets NaN/inf bits.
+template <bool FLOW>
+__device__ int full_pairs(const EnsDev& E, Slot& sl, int Z, int S, float eval, int lane, int* flags_out) {
+  const int np = Z - 1;
+  int emax = -200, flags = 0;
+  for (int p = lane; p < np; p += 32) {
+    float o[4];
+    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int b = comp_bad(o[q]);
+      flags |= b;
+      if (!b) emax = max(emax, fexp(o[q]));
+    }
+  }
+  // chain-end components are part of the same scale decision
+  emax = max(emax, (lane < 5) ? fexp(eval) : -200);
+  emax = warp_max_i(emax);
+  flags = __reduce_or_sync(FULL_MASK, flags);
+  int Snew = S;
+  if (flags != 0) {
+    // the chain stalls before any event: keep the scale (oracle order)
+  } else if (emax + S > LIMIT_E) Snew = LIMIT_E - emax;
+  else if (FLOW && S < E.s0 && emax + S < LIMIT_E - S_HYST) Snew = min(E.s0, LIMIT_E - emax);
+  const float sf = pow2f(Snew);
+  for (int p = lane; p < np; p += 32) {
+    float o[4];
+    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
+    sl.R[p] = quant(o[0], sf) + quant(o[1], sf) + quant(o[2], sf) + quant(o[3], sf);
+  }
+  __syncwarp();
+  *flags_out = flags;
+  return Snew;
+}
+
+// ------------------------------------------------------------------ correlator
+// Level >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
+// push the block average w into level 1 and cascade while blocks complete.
+__device__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, int lane) {
+  const int L = E.corr_levels, p = E.corr_p, m = E.corr_m, dmin = p / m;
+  for (int k = 1; k < L; ++k) {
+    const size_t lk = (size_t)c * L + k;
+    int4* cntp = &E.corr_cnt[lk];
+    const int4 cnt = *cntp;
+    float* sh = &E.corr_shift[lk * p * 3];
+    float* av = &E.corr_avg[lk * 3];
+    double* acc = &E.corr_acc[lk * p];
+    const int ins = cnt.x;
+    const long long nins = (((long long)(unsigned)cnt.w) << 32 | (unsigned)cnt.z) + 1;
+    const float a0 = __fadd_rn(av[0], w0), a1 = __fadd_rn(av[1], w1), a2 = __fadd_rn(av[2], w2);
+    __syncwarp();
+    if (lane == 0) { sh[ins * 3 + 0] = w0; sh[ins * 3 + 1] = w1; sh[ins * 3 + 2] = w2; }
+    __syncwarp();
+    for (int j = dmin + lane; j < p; j += 32) {
+      if ((long long)j >= nins) break;
+      int i2 = ins - j;
+      if (i2 < 0) i2 += p;
+      const float pv = __fmaf_rn(w2, sh[i2 * 3 + 2], __fmaf_rn(w1, sh[i2 * 3 + 1], __fmul_rn(w0, sh[i2 * 3 + 0])));
+      acc[j] += (double)pv;
+    }
+    const int navg = cnt.y + 1;
+    const bool up = (navg == m);
+    __syncwarp();
+    if (lane == 0) {
+      if (up) { av[0] = 0.f; av[1] = 0.f; av[2] = 0.f; }
+      else { av[0] = a0; av[1] = a1; av[2] = a2; }
+      *cntp = make_int4(ins + 1 == p ? 0 : ins + 1, up ? 0 : navg, (int)(unsigned)(nins & 0xffffffffll),
+                        (int)(unsigned)(nins >> 32));
+    }
+    __syncwarp();
+    if (!up) break;
+    const float rm = (float)m;
+    w0 = __fdiv_rn(a0, rm); w1 = __fdiv_rn(a1, rm); w2 = __fdiv_rn(a2, rm);
+  }
+}
+
+struct Corr0 {  // level-0 counters kept in registers during a residency
+  int ins, navg;
+  long long nins;
+  float a0, a1, a2;
+};
+
+// shear-stress sample (eq_ensemble_kernel.cu:282-294) into correlator level 0
+__device__ void corr_sample(const EnsDev& E, Slot& sl, int Z, int c, Corr0& k0, int lane) {
+  float sxy = 0.f, syz = 0.f, sxz = 0.f;
+  for (int s = lane; s < Z; s += 32) {
+    const float4 q = sl.Q[s];
+    const float w = __ldg(&E.INV3N[sl.N[s]]);
+    sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
+    syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
+    sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
+  }
+  sxy = warp_sum_f(sxy); syz = warp_sum_f(syz); sxz = warp_sum_f(sxz);
+  const int p = E.corr_p, m = E.corr_m;
+  __syncwarp();
+  if (lane == 0) { sl.Csh[k0.ins * 3 + 0] = sxy; sl.Csh[k0.ins * 3 + 1] = syz; sl.Csh[k0.ins * 3 + 2] = sxz; }
+  __syncwarp();
+  const long long n0 = k0.nins + 1;
+  for (int j = lane; j < p; j += 32) {
+    if ((long long)j >= n0) break;
+    int i2 = k0.ins - j;
+    if (i2 < 0) i2 += p;
+    const float pv = __fmaf_rn(sxz, sl.Csh[i2 * 3 + 2], __fmaf_rn(syz, sl.Csh[i2 * 3 + 1], __fmul_rn(sxy, sl.Csh[i2 * 3 + 0])));
+    // Kahan-compensated FP32 accumulation
+    float2 a = sl.Cacc[j];
+    const float y = __fsub_rn(pv, a.y);
+    const float t = __fadd_rn(a.x, y);
+    a.y = __fsub_rn(__fsub_rn(t, a.x), y);
+    a.x = t;
+    sl.Cacc[j] = a;
+  }
+  k0.ins = (k0.ins + 1 == p) ? 0 : k0.ins + 1;
+  k0.nins = n0;
+  k0.a0 = __fadd_rn(k0.a0, sxy); k0.a1 = __fadd_rn(k0.a1, syz); k0.a2 = __fadd_rn(k0.a2, sxz);
+  if (++k0.navg == m) {
+    const float rm = (float)m;
+    const float w0 = __fdiv_rn(k0.a0, rm), w1 = __fdiv_rn(k0.a1, rm), w2 = __fdiv_rn(k0.a2, rm);
+    k0.a0 = k0.a1 = k0.a2 = 0.f;
+    k0.navg = 0;
+    if (E.corr_levels > 1) corr_push_levels(E, c, w0, w1, w2, lane);
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------------ step kernel
+template <bool FLOW, bool CORR>
+__global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, int n_ens,
+                                              const long long* __restrict__ prefix, long long total,
+                                              unsigned int* work, int slot_cap, int pmax,
+                                              const volatile int* abort_flag, int* status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  Slot sl = make_slot(smem + (size_t)wib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
+
+  for (;;) {
+    unsigned int item = 0;
+    if (lane == 0) item = atomicAdd(work, 1u);
+    item = __shfl_sync(FULL_MASK, item, 0);
+    if ((long long)item >= total) break;
+    if (abort_flag != nullptr && *abort_flag != 0) {
+      if (lane == 0) atomicOr(status, 1);
+      break;
+    }
+    int e = 0;
+    while (e + 1 < n_ens && prefix[e + 1] <= (long long)item) ++e;
+    const EnsDev& E = ens[e];
+    const int c = (int)((long long)item - prefix[e]);
+    const int cap = E.cap;
+
+    // ---- load chain into the slot
+    ChainState st = E.cs[c];
+    int Z = st.Z, S = st.S, stall = st.stall;
+    int64_t T = st.T;
+    uint64_t step = st.step, hash = st.hash;
+    float dt_prev = st.dt_prev;
+    int64_t k_next = st.k_next;
+    const uint64_t step0 = step;
+    const float4* gq = E.QN + (size_t)c * cap;
+    const float* gt = E.tau + (size_t)c * cap;
+    for (int s = lane; s < Z; s += 32) {
+      const float4 q = gq[s];
+      sl.Q[s] = make_float4(q.x, q.y, q.z, m_q2(q.x, q.y, q.z));
+      sl.N[s] = (int)q.w;
+      sl.T[s] = gt[s];
+    }
+    const float wz1 = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(E.beta_d, (double)st.nk)));
+    Corr0 k0{0, 0, 0, 0.f, 0.f, 0.f};
+    int64_t t_next_sample = 0;
+    if (CORR) {
+      const int p = E.corr_p;
+      const size_t l0 = (size_t)c * E.corr_levels;
+      for (int j = lane; j < p; j += 32) {
+        sl.Csh[j * 3 + 0] = E.corr_shift[l0 * p * 3 + j * 3 + 0];
+        sl.Csh[j * 3 + 1] = E.corr_shift[l0 * p * 3 + j * 3 + 1];
+        sl.Csh[j * 3 + 2] = E.corr_shift[l0 * p * 3 + j * 3 + 2];
+        sl.Cacc[j] = make_float2(0.f, 0.f);
+      }
+      const int4 cn = E.corr_cnt[l0];
+      k0.ins = cn.x; k0.navg = cn.y;
+      k0.nins = ((long long)(unsigned)cn.w) << 32 | (unsigned)cn.z;
+      k0.a0 = E.corr_avg[l0 * 3 + 0]; k0.a1 = E.corr_avg[l0 * 3 + 1]; k0.a2 = E.corr_avg[l0 * 3 + 2];
+      t_next_sample = k_next * E.dt_sample_ticks;
+    }
+    __syncwarp();
+
+    int pend = 0;  // bit0 NaN, bit1 inf, bit2 scale overflow (from incremental updates)
+    const int S_stored = S;
+    if (!FLOW) {
+      // equilibrium keeps quantised pair totals in the slot; recompute them
+      // (the overflow rule can only lower the scale; it is kept only if an
+      // event follows, as in the oracle where the rule runs inside a step)
+      const float ev = (lane < 5) ? end_comp(E, lane, Z, sl.N, wz1) : 0.f;
+      int fl;
+      S = full_pairs<false>(E, sl, Z, S, ev, lane, &fl);
+      pend = fl;
+    }
+
+    uint64_t rbase = ~0ull;
+    uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    long long done = 0;
+
+    for (;;) {
+      // (1) flow: deformation by the previous dt (ensemble_kernel.cu:135-146)
+      if (FLOW && dt_prev != 0.0f) {
+        float a[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a[q] = __fmul_rn(dt_prev, E.kap[q]);
+        for (int s = lane; s < Z; s += 32) {
+          const float4 q = sl.Q[s];
+          const float nx = __fmaf_rn(a[2], q.z, __fmaf_rn(a[1], q.y, __fmaf_rn(a[0], q.x, q.x)));
+          const float ny = __fmaf_rn(a[5], q.z, __fmaf_rn(a[4], q.y, __fmaf_rn(a[3], q.x, q.y)));
+          const float nz = __fmaf_rn(a[8], q.z, __fmaf_rn(a[7], q.y, __fmaf_rn(a[6], q.x, q.z)));
+          sl.Q[s] = make_float4(nx, ny, nz, m_q2(nx, ny, nz));
+        }
+        __syncwarp();
+      }
+      // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
+      if (CORR) {
+        while (k_next < E.nsamples && T > t_next_sample) {
+          corr_sample(E, sl, Z, c, k0, lane);
+          ++k_next;
+          t_next_sample += E.dt_sample_ticks;
+        }
+      }
+      // (3) reach / stall / window checks (ensemble_kernel.cu:199-207)
+      if (stall != 0 || T >= E.t_end_ticks || (int64_t)step >= E.step_limit) {
+        dt_prev = 0.0f;
+        break;
+      }
+      if ((long long)(step - step0) >= E.watchdog_events) {
+        stall = ST_WATCHDOG;
+        dt_prev = 0.0f;
+        break;
+      }
+      if (abort_flag != nullptr && ((step - step0) & 4095u) == 4095u && *abort_flag != 0) {
+        if (lane == 0) atomicOr(status, 1);
+        dt_prev = 0.0f;
+        break;
+      }
+      // (4) chain-end rates, lanes 0..4
+      const float ev = (lane < 5) ? end_comp(E, lane, Z, sl.N, wz1) : 0.f;
+      if (FLOW) {
+        int fl;
+        S = full_pairs<true>(E, sl, Z, S, ev, lane, &fl);
+        pend = fl;
+      } else {
+        const int over = (lane < 5 && fexp(ev) + S > LIMIT_E) ? 4 : 0;
+        pend |= __reduce_or_sync(FULL_MASK, over);
+        if (pend & 4) {
+          int fl;
+          S = full_pairs<false>(E, sl, Z, S, ev, lane, &fl);
+          pend = fl;
+        }
+      }
+      if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
+      if (pend & 2) { stall = ST_INF; dt_prev = 0.0f; break; }
+      const float sf = pow2f(S);
+      const unsigned long long qe = (lane < 5) ? quant(ev, sf) : 0ull;
+      // (5) sums: contiguous odd-width chunk per lane + warp scan
+      const int np = Z - 1;
+      const int cw = ((np + 31) >> 5) | 1;
+      const int j0 = lane * cw;
+      const int j1 = min(j0 + cw, np);
+      unsigned long long part = 0;
+      for (int j = j0; j < j1; ++j) part += sl.R[j];
+      const unsigned long long incl = warp_incl_scan_u64(part, lane);
+      const unsigned long long einc = warp_incl_scan_u64(qe, lane);
+      const unsigned long long pair_total = __shfl_sync(FULL_MASK, incl, 31);
+      const unsigned long long ends_total = __shfl_sync(FULL_MASK, einc, 4);
+      const unsigned long long tot = pair_total + ends_total;
+      // (6) dt = 1/sum W (ensemble_kernel.cu:262-272)
+      const float sumw = __fmul_rn(__ll2float_rn((long long)tot), pow2f(-S));
+      const float dt = __fdiv_rn(1.0f, sumw);
+      if (dt == 0.0f) { stall = ST_DT_ZERO; dt_prev = 0.0f; break; }
+      if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
+      const int64_t dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
+      // (7) Philox words of this event (one evaluation per 32 events)
+      if ((step & ~31ull) != rbase) {
+        rbase = step & ~31ull;
+        const uint64_t ctr = rbase + (uint64_t)lane;
+        const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
+        r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
+      }
+      const int src = (int)(step & 31ull);
+      const uint32_t w0 = __shfl_sync(FULL_MASK, r0, src);
+      const uint32_t w1 = __shfl_sync(FULL_MASK, r1, src);
+      const uint32_t w2 = __shfl_sync(FULL_MASK, r2, src);
+      const uint32_t w3 = __shfl_sync(FULL_MASK, r3, src);
+      // (8) pick (ensemble_kernel.cu:274-501): pr uniform in [0, tot)
+      const unsigned long long u64 = ((unsigned long long)w1 << 32) | w0;
+      const unsigned long long pr = __umul64hi(tot, u64);
+      int evn, j = -1;
+      unsigned long long rem = 0, wsel = 0;
+      if (pr < pair_total) {
+        const unsigned mask = __ballot_sync(FULL_MASK, incl > pr);
+        const int L = __ffs(mask) - 1;
+        int jj = 0;
+        unsigned long long r = 0;
+        if (lane == L) {
+          r = pr - (incl - part);
+          jj = j0;
+          while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
+        }
+        j = __shfl_sync(FULL_MASK, jj, L);
+        r = __shfl_sync(FULL_MASK, r, L);
+        float o[4];
+        pair_comp(E, sl.N[j], sl.Q[j].w, sl.N[j + 1], sl.Q[j + 1].w, sl.T[j], o);
+        const unsigned long long q0 = quant(o[0], sf), q1 = quant(o[1], sf), q2 = quant(o[2], sf),
+                                 q3 = quant(o[3], sf);
+        if (r < q0) evn = CDD;
+        else if ((r -= q0) < q1) evn = SDP;
+        else if ((r -= q1) < q2) evn = SDM;
+        else { r -= q2; evn = CDC_MID; rem = r; wsel = q3; }
+      } else {
+        const unsigned long long r = pr - pair_total;
+        const unsigned mask = __ballot_sync(FULL_MASK, lane < 5 && einc > r);
+        const int L = __ffs(mask) - 1;
+        const unsigned long long lo = __shfl_sync(FULL_MASK, einc - qe, L);
+        wsel = __shfl_sync(FULL_MASK, qe, L);
+        rem = r - lo;
+        evn = (L == 0) ? CDC_TAIL : (L == 1) ? SDC_HEAD : (L == 2) ? SDC_TAIL : (L == 3) ? SDD_HEAD : SDD_TAIL;
+      }
+      T += dtt;
+      // (9) apply
+      const bool create = (evn == CDC_MID || evn == CDC_TAIL || evn == SDC_HEAD || evn == SDC_TAIL);
+      uint32_t code = ((uint32_t)evn << 24) | (uint32_t)(j < 0 ? 0 : j);
+      int up0 = 0, upn = 0;  // pairs to recompute [up0, up0+upn)
+      if (create && Z >= cap) {
+        code |= (uint32_t)NULL_FLAG << 24;  // refused at capacity (ensemble_kernel.cu:380,423,451)
+      } else if (create) {
+        int newn = 0;
+        if (evn == CDC_MID || evn == CDC_TAIL) {
+          const int N1 = (evn == CDC_MID) ? sl.N[j] : sl.N[Z - 1];
+          const double x = floor(__dadd_rn(0.5, __ddiv_rn(__dmul_rn(__ull2double_rn(rem), (double)(N1 - 2)),
+                                                        __ull2double_rn(wsel))));
+          newn = (int)x + 1;
+          newn = max(1, min(N1 - 1, newn));
+        }
+        const U4 gr = rng_at(E, P_CREATE, step, (uint32_t)(step >> 32), (uint32_t)c);
+        float g0, g1, g2, g3;
+        m_gauss2(gr.x, gr.y, &g0, &g1);
+        m_gauss2(gr.z, gr.w, &g2, &g3);
+        const PcdDev pp = partner_pcd(E, w3);
+        const float u = u01(w2);
+        const float trate = E.cd_flag ? ((evn == CDC_MID || evn == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
+        if (evn == CDC_MID && j > 0) {
+          const int N1 = sl.N[j];
+          const float4 q1 = sl.Q[j];
+          __syncwarp();
+          move_up(sl.Q, j, Z, lane); move_up(sl.N, j, Z, lane);
+          move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane);
+          if (lane == 0) {
+            const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
+            const float ra = __fdiv_rn((float)newn, (float)N1);
+            const float x = __fmaf_rn(q1.x, ra, __fmul_rn(g0, sg));
+            const float y = __fmaf_rn(q1.y, ra, __fmul_rn(g1, sg));
+            const float z = __fmaf_rn(q1.z, ra, __fmul_rn(g2, sg));
+            sl.N[j] = newn; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+            const float x2 = __fsub_rn(q1.x, x), y2 = __fsub_rn(q1.y, y), z2 = __fsub_rn(q1.z, z);
+            sl.N[j + 1] = N1 - newn; sl.Q[j + 1] = make_float4(x2, y2, z2, m_q2(x2, y2, z2));
+            sl.T[j] = trate;
+          }
+          up0 = j - 1; upn = 3;
+        } else if ((evn == CDC_MID && j == 0) || evn == SDC_HEAD) {
+          const int N0 = sl.N[0];
+          const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
+          const int nd = (evn == SDC_HEAD) ? 1 : newn;
+          __syncwarp();
+          move_up(sl.Q, 0, Z, lane); move_up(sl.N, 0, Z, lane);
+          move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane);
+          if (lane == 0) {
+            const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+            const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+            sl.N[0] = nd; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+            sl.N[1] = nn; sl.Q[1] = make_float4(x, y, z, m_q2(x, y, z));
+            sl.T[0] = trate;
+          }
+          up0 = 0; upn = 2;
+        } else {  // CDC_TAIL, SDC_TAIL
+          const int Nt = sl.N[Z - 1];
+          const int nn = (evn == SDC_TAIL) ? Nt - 1 : newn;
+          const int nd = (evn == SDC_TAIL) ? 1 : Nt - newn;
+          __syncwarp();
+          if (lane == 0) {
+            const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+            const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+            sl.N[Z] = nd; sl.Q[Z] = make_float4(0.f, 0.f, 0.f, 0.f);
+            sl.N[Z - 1] = nn; sl.Q[Z - 1] = make_float4(x, y, z, m_q2(x, y, z));
+            sl.T[Z - 1] = trate;
+          }
+          up0 = Z - 2; upn = 2;
+        }
+        Z += 1;
+        code |= (uint32_t)newn << 8;
+      } else if (evn == SDP || evn == SDM) {
+        __syncwarp();
+        if (lane == 0) {
+          const int d = (evn == SDP) ? 1 : -1;
+          sl.N[j] += d; sl.N[j + 1] -= d;
+        }
+        up0 = j - 1; upn = 3;
+      } else if (evn == CDD) {
+        const int n = sl.N[j] + sl.N[j + 1];
+        const float4 a = sl.Q[j], b = sl.Q[j + 1];
+        const bool endp = (j == Z - 2) || (j == 0);
+        __syncwarp();
+        move_down(sl.Q, j + 2, Z, lane); move_down(sl.N, j + 2, Z, lane);
+        move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane);
+        if (lane == 0) {
+          const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
+          const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
+          const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
+          sl.N[j] = n; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+        }
+        Z -= 1;
+        up0 = j - 1; upn = 2;
+      } else if (evn == SDD_HEAD) {
+        const int n = sl.N[1] + 1;
+        __syncwarp();
+        move_down(sl.Q, 1, Z, lane); move_down(sl.N, 1, Z, lane);
+        move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane);
+        if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
+        Z -= 1;
+        up0 = 0; upn = 1;
+      } else {  // SDD_TAIL
+        __syncwarp();
+        if (lane == 0) { sl.N[Z - 2] += 1; sl.Q[Z - 2] = make_float4(0.f, 0.f, 0.f, 0.f); }
+        Z -= 1;
+        up0 = Z - 2; upn = 1;
+      }
+      __syncwarp();
+      if (!FLOW && upn > 0) pend |= update_pairs(E, sl, Z, S, up0, upn, lane);
+      hash = (hash ^ (uint64_t)code) * 0x100000001B3ull;
+      ++step;
+      ++done;
+      dt_prev = dt;
+    }
+
+    // ---- flow: stress at the end of the window (ensemble_kernel.cu:504-538)
+    if (FLOW) {
+      float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int i = lane; i < Z; i += 32) {
+        const float4 q = sl.Q[i];
+        const float w = __ldg(&E.INV3N[sl.N[i]]);
+        s[0] = __fmaf_rn(-__fmul_rn(q.x, q.x), w, s[0]);
+        s[1] = __fmaf_rn(-__fmul_rn(q.y, q.y), w, s[1]);
+        s[2] = __fmaf_rn(-__fmul_rn(q.z, q.z), w, s[2]);
+        s[3] = __fmaf_rn(-__fmul_rn(q.x, q.y), w, s[3]);
+        s[4] = __fmaf_rn(-__fmul_rn(q.y, q.z), w, s[4]);
+        s[5] = __fmaf_rn(-__fmul_rn(q.x, q.z), w, s[5]);
+        s[6] = __fadd_rn(s[6], __fsqrt_rn(q.w));
+      }
+#pragma unroll
+      for (int q = 0; q < 7; ++q) s[q] = warp_sum_f(s[q]);
+      if (lane == 0) {
+        float* o = E.out_stress + (size_t)c * 8;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) o[q] = s[q];
+        o[7] = (float)Z;
+      }
+    }
+    // ---- correlator level 0 back to HBM (compensated FP32 sums -> FP64)
+    if (CORR) {
+      const int p = E.corr_p;
+      const size_t l0 = (size_t)c * E.corr_levels;
+      for (int j = lane; j < p; j += 32) {
+        E.corr_shift[l0 * p * 3 + j * 3 + 0] = sl.Csh[j * 3 + 0];
+        E.corr_shift[l0 * p * 3 + j * 3 + 1] = sl.Csh[j * 3 + 1];
+        E.corr_shift[l0 * p * 3 + j * 3 + 2] = sl.Csh[j * 3 + 2];
+        const float2 a = sl.Cacc[j];
+        E.corr_acc[l0 * p + j] += (double)a.x - (double)a.y;
+      }
+      if (lane == 0) {
+        E.corr_cnt[l0] = make_int4(k0.ins, k0.navg, (int)(unsigned)(k0.nins & 0xffffffffll),
+                                   (int)(unsigned)(k0.nins >> 32));
+        E.corr_avg[l0 * 3 + 0] = k0.a0; E.corr_avg[l0 * 3 + 1] = k0.a1; E.corr_avg[l0 * 3 + 2] = k0.a2;
+      }
+    }
+    // ---- chain back to HBM
+    float4* wq = E.QN + (size_t)c * cap;
+    float* wt = E.tau + (size_t)c * cap;
+    for (int s = lane; s < Z; s += 32) {
+      const float4 q = sl.Q[s];
+      wq[s] = make_float4(q.x, q.y, q.z, (float)sl.N[s]);
+      wt[s] = (s < Z - 1) ? sl.T[s] : 0.0f;
+    }
+    if (lane == 0) {
+      st.Z = Z; st.S = (done > 0) ? S : S_stored; st.stall = stall; st.T = T; st.step = step; st.hash = hash;
+      st.dt_prev = dt_prev; st.k_next = k_next;
+      E.cs[c] = st;
+      atomicAdd(&E.counters[0], (unsigned long long)done);
+      atomicAdd(&E.counters[1], 1ull);
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ initialiser
+// Equilibrium chains (role of chain.cu:199-283): each of the NK-1 bonds between
+// Kuhn steps carries an entanglement with probability 1/(1+beta), which gives
+// Z-1 ~ Binomial(NK-1, 1/(1+beta)) with N uniform over compositions; Q ~ N(0,
+// N/3) for internal strands, 0 for dangling ends; tau rates from f_t.
+__global__ void __launch_bounds__(128) k_init(const EnsDev* __restrict__ ensp, int slot_cap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const EnsDev& E = *ensp;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int c = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (c >= E.n_chains) return;
+  int* pos = (int*)(smem + (size_t)wib * (size_t)(slot_cap + 1) * 8);
+  int* sN = pos + (slot_cap + 1);
+  const int nk = E.poly ? __ldg(&E.nk_chain[c]) : E.nk;
+  const int cap = E.cap;
+  const double pe = 1.0 / (1.0 + (double)E.beta);
+  double thr_d = floor(pe * 4294967296.0);
+  if (thr_d > 4294967295.0) thr_d = 4294967295.0;
+  const uint32_t thr = (uint32_t)thr_d;
+  const int nb = nk - 1;                  // bonds
+  const int nblk = (nb + 3) >> 2;         // Philox blocks of 4 bonds
+  int Zm1 = 0;
+  for (uint32_t att = 0; att < 64; ++att) {
+    int count = 0;
+    for (int b = lane; b < nblk; b += 32) {
+      const U4 r = rng_at(E, P_BONDS, (uint64_t)b, att, (uint32_t)c);
+      const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) count += (4 * b + q < nb && w[q] < thr) ? 1 : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(FULL_MASK, count, o);
+    Zm1 = count;
+    if (Zm1 + 1 <= cap || att == 63) {
+      // ordered positions: rounds of 32 blocks, exclusive scan of counts
+      int off = 0;
+      for (int base = 0; base < nblk; base += 32) {
+        const int b = base + lane;
+        uint32_t bits = 0;
+        if (b < nblk) {
+          const U4 r = rng_at(E, P_BONDS, (uint64_t)b, att, (uint32_t)c);
+          const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) if (4 * b + q < nb && w[q] < thr) bits |= 1u << q;
+        }
+        const int cnt = __popc(bits);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(FULL_MASK, incl, o);
+          if (lane >= o) incl += t;
+        }
+        int k = off + incl - cnt;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (bits & (1u << q)) { if (k < cap - 1) pos[k] = 4 * b + q; ++k; }
+        off += __shfl_sync(FULL_MASK, incl, 31);
+      }
+      break;
+    }
+  }
+  if (Zm1 > cap - 1) Zm1 = cap - 1;  // truncation after 64 rejected draws
+  __syncwarp();
+  const int Z = Zm1 + 1;
+  for (int i = lane; i < Z; i += 32) {
+    const int prev = (i == 0) ? -1 : pos[i - 1];
+    const int cur = (i == Z - 1) ? nk - 1 : pos[i];
+    sN[i] = cur - prev;
+  }
+  __syncwarp();
+  float4* gq = E.QN + (size_t)c * cap;
+  float* gt = E.tau + (size_t)c * cap;
+  float* gq2 = (float*)pos;  // reuse: Q^2 per strand (positions no longer needed)
+  __syncwarp();
+  for (int i = lane; i < Z; i += 32) {
+    const int N = sN[i];
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (i >= 1 && i <= Z - 2) {
+      const U4 r = rng_at(E, P_QINIT, (uint64_t)i, 0, (uint32_t)c);
+      float g0, g1, g2, g3;
+      m_gauss2(r.x, r.y, &g0, &g1);
+      m_gauss2(r.z, r.w, &g2, &g3);
+      const float sg = __fsqrt_rn(__fdiv_rn((float)N, 3.0f));
+      x = __fmul_rn(g0, sg); y = __fmul_rn(g1, sg); z = __fmul_rn(g2, sg);
+    }
+    gq[i] = make_float4(x, y, z, (float)N);
+    gq2[i] = m_q2(x, y, z);
+    float tr = 0.0f;
+    if (i < Z - 1) {
+      const U4 r = rng_at(E, P_TAUINIT, (uint64_t)i, 0, (uint32_t)c);
+      const PcdDev pp = partner_pcd(E, r.y);
+      tr = E.cd_flag ? rate_f_t(pp, u01(r.x)) : 0.0f;
+    }
+    gt[i] = tr;
+  }
+  __syncwarp();
+  // initial fixed-point scale: min(s0, 47 - max exponent of all rate components)
+  int emax = -200;
+  for (int p = lane; p < Z - 1; p += 32) {
+    float o[4];
+    pair_comp(E, sN[p], gq2[p], sN[p + 1], gq2[p + 1], gt[p], o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) emax = max(emax, fexp(o[q]));
+  }
+  if (lane < 5) {
+    const float wz1 = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(E.beta_d, (double)nk)));
+    emax = max(emax, fexp(end_comp(E, lane, Z, sN, wz1)));
+  }
+  emax = warp_max_i(emax);
+  if (lane == 0) {
+    ChainState st;
+    st.Z = Z; st.stall = 0; st.S = min(E.s0, LIMIT_E - emax); st.dt_prev = 0.f;
+    st.T = 0; st.step = 0; st.hash = 0xCBF29CE484222325ull; st.k_next = 0;
+    st.nk = nk; st.pad_[0] = st.pad_[1] = st.pad_[2] = 0;
+    E.cs[c] = st;
+  }
+}
+
+// ------------------------------------------------------------------ reductions
+// G(t) numerator per (level k, lag j): sum over chains of acc/count, FP64,
+// fixed tree order (deterministic).  count = values inserted at level k - j.
+__global__ void k_gt_reduce(const EnsDev* __restrict__ ensp, double* gsum, long long* gcount) {
+  const EnsDev& E = *ensp;
+  const int L = E.corr_levels, p = E.corr_p;
+  const int kj = blockIdx.x;
+  const int k = kj / p, j = kj % p;
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (int c = threadIdx.x; c < E.n_chains; c += blockDim.x) {
+    const int4 cn = E.corr_cnt[(size_t)c * L + k];
+    const long long nins = ((long long)(unsigned)cn.w) << 32 | (unsigned)cn.z;
+    const long long n = nins - j;
+    if (n > 0 && !(k > 0 && j < p / E.corr_m)) acc += E.corr_acc[((size_t)c * L + k) * p + j] / (double)n;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    gsum[kj] = red[0];
+    const int4 cn = E.corr_cnt[(size_t)0 * L + k];
+    const long long nins = ((long long)(unsigned)cn.w) << 32 | (unsigned)cn.z;
+    const long long n = nins - j;
+    gcount[kj] = (n > 0 && !(k > 0 && j < p / E.corr_m)) ? n : 0;
+  }
+}
+
+// Ensemble average of the window-end stress over non-stalled, non-NaN chains
+// (ensemble_call_block.cu:471-491), FP64, fixed tree order.  out[0..7] sums,
+// out[8] chain count.
+__global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
+  const EnsDev& E = *ensp;
+  __shared__ double red[9][256];
+  double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = threadIdx.x; c < E.n_chains; c += blockDim.x) {
+    const float* s = E.out_stress + (size_t)c * 8;
+    if (E.cs[c].stall != 0 || s[0] != s[0]) continue;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] += (double)s[q];
+    a[8] += 1.0;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) red[q][threadIdx.x] = a[q];
+  __syncthreads();
+  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 9) out[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// ------------------------------------------------------------------ launchers
+template <bool FLOW, bool CORR>
+static void* step_fn() { return (void*)k_step<FLOW, CORR>; }
+
+static void* pick_step(bool flow, bool corr) {
+  if (flow) return corr ? step_fn<true, true>() : step_fn<true, false>();
+  return corr ? step_fn<false, true>() : step_fn<false, false>();
+}
+
+int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg) {
+  const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
+  void* fn = pick_step(flow, corr);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, cfg.warps_per_block * 32, sm) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
+                        unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
+                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st) {
+  const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
+  void* fn = pick_step(flow, corr);
+  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (err != cudaSuccess) return err;
+  void* args[] = {(void*)&d_ens, (void*)&n_ens, (void*)&d_prefix, (void*)&total, (void*)&d_work,
+                  (void*)&cfg.slot_cap, (void*)&cfg.pmax, (void*)&abort_flag, (void*)&d_status};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(cfg.warps_per_block * 32), args, sm, st);
+}
+
+cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st) {
+  const int wpb = 4;
+  const size_t sm = (size_t)(slot_cap + 1) * 8 * wpb;
+  cudaError_t err = cudaFuncSetAttribute((void*)k_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (err != cudaSuccess) return err;
+  const int grid = (h_ens.n_chains + wpb - 1) / wpb;
+  k_init<<<grid, wpb * 32, sm, st>>>(d_ens, slot_cap);
+  return cudaGetLastError();
+}
+
+// launchers that need the device copy of the ensemble
+cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
+                                 cudaStream_t st) {
+  k_gt_reduce<<<levels * p, 256, 0, st>>>(d_ens, d_gsum, d_count);
+  return cudaGetLastError();
+}
+cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st) {
+  k_stress_reduce<<<1, 256, 0, st>>>(d_ens, d_out9);
+  return cudaGetLastError();
+}
+
+}  // namespace dsm

@@ -1,0 +1,154 @@
+/*
+ * gpu_dsm_gb300 — C ABI of the GB300-native Discrete Slip-Link Model (DSM)
+ * kinetic Monte Carlo simulator.
+ *
+ * Every entry point is extern "C" with plain pointers and sizes.  Host arrays
+ * use the reference's own layouts (ktaletsk/gpu_dsm):
+ *   - chain_head  {int Z; float time; float dummy; int stall_flag}  common/chain.h:45-53
+ *   - QN          n_chains * z_max float4 {Qx, Qy, Qz, N}            common/chain.h:37-42,
+ *                                                                    common/ensemble.cu:79-104
+ *   - tau_CD      n_chains * z_max float (rates 1/tau_CD)            common/chain.cu:243-246
+ *   - stress_plus {xx, yy, zz, xy, yz, zx, Lpp, Z}                   common/stress.h:23-29
+ * Status codes replace the reference's exit(-1) on CUDA errors
+ * (common/cuda_call.h:42-49); -1 keeps its meaning "aborted by run_flag".
+ */
+#ifndef GPU_DSM_GB300_DSM_H
+#define GPU_DSM_GB300_DSM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define DSM_BOOL bool
+extern "C" {
+#else
+#define DSM_BOOL _Bool
+#endif
+
+#define DSM_OK 0
+#define DSM_ABORTED (-1)        /* run_flag cleared (ensemble_call_block.cu:214,353) */
+#define DSM_ERR_CUDA (-2)       /* CUDA runtime error (reference: exit(-1)) */
+#define DSM_ERR_INVALID (-3)    /* invalid argument / input */
+#define DSM_ERR_MEMORY (-4)     /* device memory budget exceeded */
+#define DSM_ERR_WATCHDOG (-5)   /* a chain exceeded the per-launch event cap */
+#define DSM_ERR_NOT_BUILT (-6)  /* library built without the CUDA kernels */
+
+typedef struct dsm_float4 { float x, y, z, w; } dsm_float4;
+
+/* chain_head of the reference, same field order and size (16 bytes) */
+typedef struct dsm_chain_head {
+  int32_t Z;
+  float time;
+  float dummy;
+  int32_t stall_flag;
+} dsm_chain_head;
+
+/* stress_plus of the reference (32 bytes) */
+typedef struct dsm_stress_plus {
+  float xx, yy, zz, xy, yz, zx, Lpp, Z;
+} dsm_stress_plus;
+
+/*
+ * Simulation parameters.  The first block is the reference's input.dat
+ * (common/main_cuda.cu:55-68, CLI/input.dat:1-22); the rest are the
+ * reference's compile-time constants made runtime knobs.
+ */
+typedef struct dsm_params {
+  float beta;              /* input.dat 1: entanglement activity */
+  int32_t nk;              /* input.dat 2: Kuhn steps per chain (max for polydisperse) */
+  int32_t n_chains;        /* input.dat 3 */
+  float kappa[9];          /* input.dat 4: transpose of the velocity gradient, row-major */
+  int32_t cd_flag;         /* input.dat 5: 0 SD only, 1 SD+CD */
+  int32_t pd_flag;         /* input.dat 6: GEX background polydispersity (must be 0) */
+  int32_t eq_type;         /* input.dat 7: 1 G(t); other values: no correlator */
+  double sync_dt;          /* input.dat 8: sync / sample interval (tau_K) */
+  double t_end;            /* input.dat 9: total simulation time (tau_K) */
+  uint64_t seed;           /* job_ID: Philox key */
+  int32_t device;          /* CUDA device (-d) */
+  int32_t z_max;           /* strand capacity per chain; 0 = nk (ensemble.cu:99) */
+  int32_t corr_p;          /* correlator points per level; 0 = 64 (correlator.h:21) */
+  int32_t corr_m;          /* correlator averaging; 0 = 8 (correlator.h:22) */
+  int32_t corr_levels;     /* 0 = ceil(log(t_end/sync_dt/p)/log m)+1 (main_cuda.cu:70) */
+  uint32_t stream;         /* Philox counter word 3 (ensemble id) */
+  const int32_t* nk_chain; /* per-chain N_K (polydisperse melt) or NULL */
+  int32_t warps_per_block; /* step-kernel block size in warps; 0 = autotuned */
+  int32_t s0;              /* initial fixed-point scale exponent; 0 = 40 */
+} dsm_params;
+
+typedef struct dsm_sim dsm_sim;
+
+/* Lifecycle.  Replaces gpu_init/gpu_clean (common/ensemble.cu:118-208,506-539)
+ * with an owning handle instead of process globals. */
+int dsm_create(const dsm_params* params, dsm_sim** out);
+void dsm_destroy(dsm_sim* sim);
+const char* dsm_last_error(const dsm_sim* sim);
+
+/* Equilibrium initial state on the device, keyed by (seed, chain).
+ * Replaces host_chains_init/chain_init (common/ensemble.cu:106-115,
+ * common/chain.cu:199-283). */
+int dsm_init_equilibrium(dsm_sim* sim);
+
+/* Host <-> device conformations in the reference layout.  Replace
+ * get_chain_to_device_call_block / get_chain_from_device_call_block
+ * (common/ensemble_call_block.cu:402-450) and get_chains_from_device
+ * (common/ensemble.cu:231-236).  On set, heads[i].time is the chain time,
+ * stall_flag the stall code; pending flow dt, event counters and correlator
+ * state are reset. */
+int dsm_set_chains(dsm_sim* sim, const dsm_chain_head* heads, const dsm_float4* QN, const float* tau);
+int dsm_get_chains(dsm_sim* sim, dsm_chain_head* heads, dsm_float4* QN, float* tau);
+
+/* Extended per-chain scalars (time in 2^-32 tau_K ticks, event counter,
+ * pending flow dt, stall code, fixed-point scale, event-sequence hash).
+ * Any pointer may be NULL. */
+int dsm_get_ext(dsm_sim* sim, int64_t* time_ticks, uint64_t* steps, float* dt_prev, int32_t* stall,
+                int32_t* scale, uint64_t* hash);
+int dsm_set_ext(dsm_sim* sim, const int64_t* time_ticks, const uint64_t* steps, const float* dt_prev,
+                const int32_t* stall, const int32_t* scale);
+
+/* Advance every chain until its time reaches t_end (tau_K), or it has done
+ * step_limit events in total (step_limit < 0: no limit).  Replaces
+ * time_step_call_block / EQ_time_step_call_block
+ * (common/ensemble_call_block.cu:106-379) and gpu_time_step
+ * (common/ensemble.cu:223-229).  abort_flag: host int polled by the running
+ * kernel (mapped memory), non-zero aborts with DSM_ABORTED; may be NULL.
+ * events (may be NULL) receives the number of kMC events done. */
+int dsm_advance(dsm_sim* sim, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
+                uint64_t* events);
+
+/* Ensemble-average stress of the current state over non-stalled chains
+ * (flow output).  Replaces calc_stress / calc_stress_call_block
+ * (common/ensemble.cu:210-221, common/ensemble_call_block.cu:452-505). */
+int dsm_stress(dsm_sim* sim, dsm_stress_plus* out, int32_t* chain_count);
+
+/* Stress relaxation G(t) as written to G.dat by gpu_Gt_PCS
+ * (common/ensemble.cu:289-339, common/correlator.cu:146-187): t in sample
+ * units, G averaged over xy/yz/xz and chains.  n: in = capacity, out = points. */
+int dsm_gt(dsm_sim* sim, float* t, float* G, int32_t* n);
+/* Raw correlator sums: gsum[k*p+j] = sum over chains of C/count, count of chain 0 */
+int dsm_gt_raw(dsm_sim* sim, double* gsum, int64_t* count);
+
+/* Device time (CUDA events on the launching stream) and kMC events of the
+ * step kernel of the last dsm_advance, plus its launch shape. */
+int dsm_last_window(const dsm_sim* sim, float* kernel_ms, uint64_t* events, int32_t* grid,
+                    int32_t* blocks_per_sm);
+
+/* Correlator geometry of a simulation: levels, p, m */
+int dsm_corr_shape(const dsm_sim* sim, int32_t* levels, int32_t* p, int32_t* m);
+
+/* Reference-format checkpoint (common/ensemble.cu:342-354,486-504):
+ * int N_cha, then per chain chain_head, Z float4 QN, Z float tau. */
+int dsm_save_file(dsm_sim* sim, const char* path);
+int dsm_load_file(dsm_sim* sim, const char* path);
+
+/* ---------------------------------------------------------------------
+ * Reference driver entry point (common/main_cuda.cu:34), same signature and
+ * return convention (0 ok, -1 aborted): reads input.dat from the working
+ * directory, writes tau[_id].dat / G[_id].dat, honours -s/-l/-distr.
+ * --------------------------------------------------------------------- */
+int main_cuda(DSM_BOOL* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID,
+              DSM_BOOL distr, int* progress_bar);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPU_DSM_GB300_DSM_H */

@@ -1,0 +1,1078 @@
+// ORACLE — test infrastructure only.  Only tests/, __graft_entry__.smoke() and
+// bench.py (its cpu_baseline leg and the `--impl reference` arm) load this
+// library, and only as the checker / the timed CPU restatement.  The product
+// (gpu_dsm_gb300/) never links, imports or calls anything under oracle/.
+//
+// CPU restatement of the reference DSM (Discrete Slip-Link Model) kinetic Monte
+// Carlo path of ktaletsk/gpu_dsm, written in "immediate-apply" form: the
+// reference defers strand insertions/removals to the next step (delayed
+// dynamics, common/ensemble_kernel.cu:64-102); here an event is applied as soon
+// as it is picked, which yields the same state sequence.
+//
+// Two arithmetic modes:
+//   mode 0 (FP32 mirror): FP32 strand state, rates from per-N tables and the
+//       element-wise functions of orc_math.h, rates quantised to int64 fixed
+//       point so that the event pick is an exact integer computation.  This is
+//       the arithmetic the sm_103a kernel implements; integer state and Q must
+//       agree with it bit for bit.
+//   mode 1 (FP64 transcription): the reference formulas evaluated literally in
+//       double precision with libm (pow/exp/log/sin/cos), double state, double
+//       sums.  Used as the accuracy reference for statistics.
+// The measurement path (stress samples, multi-tau correlator, flow stress) is
+// accumulated in FP64 in both modes.
+//
+// Reference functions restated here (file:line in ktaletsk/gpu_dsm):
+//   p_cd constants ................ common/pcd_tau.h:32-66
+//   lifetime samplers ............. common/gpu_random.cu:78-99,143-148
+//   CD creation prefactor ......... common/ensemble.cu:136-150
+//   equilibrium initialiser ....... common/chain.cu:106-156,158-170,199-283
+//   flow deformation kappa() ...... common/ensemble_kernel.cu:105-110
+//   pair (shift + CD) rates ....... common/ensemble_kernel.cu:149-181,
+//                                   common/eq_ensemble_kernel.cu:97-127
+//   end rates, dt, pick, events ... common/ensemble_kernel.cu:199-501,
+//                                   common/eq_ensemble_kernel.cu:260-662
+//   stress sample ................. common/eq_ensemble_kernel.cu:281-296
+//   multi-tau correlator .......... common/eq_ensemble_kernel.cu:133-227,
+//                                   common/correlator.cu:104-187
+//   flow stress ................... common/ensemble_kernel.cu:504-538,
+//                                   common/ensemble_call_block.cu:452-505
+//   reach / sync semantics ........ common/ensemble_kernel.cu:199-207,
+//                                   common/eq_ensemble_kernel.cu:260-331
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "orc_math.h"
+
+using namespace orc;
+
+extern "C" {
+typedef struct orc_params {
+  double beta;           // entanglement activity (input.dat line 1)
+  int32_t nk;            // Kuhn steps per chain (input.dat line 2); max for polydisperse
+  int32_t n_chains;      // input.dat line 3
+  int32_t z_max;         // strand capacity per chain (reference: NK, ensemble.cu:99)
+  int32_t cd_flag;       // input.dat line 5
+  float kappa[9];        // velocity-gradient transpose, row-major (input.dat line 4)
+  int32_t mode;          // 0 FP32 mirror, 1 FP64 transcription
+  uint32_t stream;       // Philox counter word 3 (ensemble id)
+  uint64_t seed;         // Philox key (job_ID)
+  int32_t corr_type;     // -1 none, 0 stress G(t)
+  int32_t corr_p, corr_m, corr_levels;
+  double corr_dt;        // sample interval
+  int64_t corr_nsamples; // samples per chain over the run
+  const int32_t* nk_chain;  // per-chain Kuhn steps (NULL: all nk)
+  int32_t s0;            // initial fixed-point scale exponent (0 -> 40)
+  int32_t pad_;
+} orc_params;
+}
+
+namespace {
+
+constexpr double TICKS = 4294967296.0;  // time unit: 2^-32 tau_K
+constexpr int LIMIT_E = 47;             // components kept below 2^48 in fixed point
+
+// Event codes (shared with the kernel's event hash)
+enum Ev { CDD = 0, SDP = 1, SDM = 2, CDC_MID = 3, CDC_TAIL = 4, SDC_HEAD = 5,
+          SDC_TAIL = 6, SDD_HEAD = 7, SDD_TAIL = 8, NULL_FLAG = 16 };
+
+static inline uint64_t hash_step(uint64_t h, uint32_t code) {
+  return (h ^ (uint64_t)code) * 0x100000001B3ull;
+}
+
+// ------------------------------------------------------------------ p_cd
+struct PCD {
+  double alpha, tau_0, tau_max, tau_d, g, c1, cm1, rcm1c1, At, Adt, Bdt, normdt;
+  float At_, Dt_, Ct_, Adt_, Bdt_, Cdt_, Ddt_, tau_d_inv, one_minus_g;
+};
+
+// common/pcd_tau.h:32-66 (constants), common/gpu_random.cu:78-99 (device form)
+PCD make_pcd(double Be, double Nk) {
+  PCD p{};
+  const double z = (Nk + Be) / (Be + 1.0);
+  p.g = 0.667;
+  if ((float)Be != 1.0f) {
+    p.alpha = (0.053 * std::log(Be) + 0.31) * std::pow(z, -0.012 * std::log(Be) - 0.024);
+    p.tau_0 = 0.285 * std::pow(Be + 2.0, 0.515);
+    p.tau_max = (Nk < 2) ? p.tau_0 : 0.025 * std::pow(Be + 2.0, 2.6) * std::pow(z, 2.83);
+    p.tau_d = (Nk < 2) ? p.tau_0 : 0.036 * std::pow(Be + 2.0, 3.07) * std::pow(z - 1.0, 3.02);
+  } else {
+    p.alpha = 0.267096 - 0.375571 * std::exp(-0.0838237 * Nk);
+    p.tau_0 = 0.460277 + 0.298913 * std::exp(-0.0705314 * Nk);
+    p.tau_max = (Nk < 4) ? p.tau_0 : 0.0156137 * std::pow(Nk, 3.18849);
+    p.tau_d = (Nk < 4) ? p.tau_0 : 0.0740131 * std::pow(Nk, 3.18363);
+  }
+  p.c1 = std::pow(p.tau_max, p.alpha) - std::pow(p.tau_0, p.alpha);
+  p.cm1 = std::pow(p.tau_max, p.alpha - 1.0) - std::pow(p.tau_0, p.alpha - 1.0);
+  p.rcm1c1 = (p.c1 == 0.0) ? (p.alpha - 1.0) / p.alpha / p.tau_0 : p.cm1 / p.c1;
+  p.At = 1.0 - p.g;
+  p.Adt = p.At * p.alpha / (p.alpha - 1.0);
+  p.Bdt = p.Adt * p.rcm1c1;
+  p.normdt = p.Bdt + p.g / p.tau_d;
+  p.At_ = (float)(p.c1 / p.At);
+  p.Dt_ = (float)std::pow(p.tau_0, p.alpha);
+  p.Ct_ = (float)(-1.0 / p.alpha);
+  p.Adt_ = (float)(p.normdt * p.c1 / p.Adt);
+  p.Bdt_ = (float)(p.Bdt / p.normdt);
+  p.Cdt_ = (float)(-1.0 / (p.alpha - 1.0));
+  p.Ddt_ = (float)std::pow(p.tau_0, p.alpha - 1.0);
+  p.tau_d_inv = (float)(1.0 / p.tau_d);
+  p.one_minus_g = (float)(1.0 - p.g);
+  return p;
+}
+
+// Lifetime samplers, returning rates 1/tau (gpu_random.cu:143-148).
+// SD-created entanglement: f_t ; CD-created entanglement: f_d*t.
+static inline float rate_f_t(const PCD& p, float u) {
+  return (u < p.one_minus_g) ? m_pow(std::fmaf(u, p.At_, p.Dt_), p.Ct_) : p.tau_d_inv;
+}
+static inline float rate_f_dt(const PCD& p, float u) {
+  return (u < p.Bdt_) ? m_pow(std::fmaf(u, p.Adt_, p.Ddt_), p.Cdt_) : p.tau_d_inv;
+}
+// FP64 forms (pcd_tau.h:67-82 literally)
+static inline double rate_f_t_d(const PCD& p, double u) {
+  if (u < 1.0 - p.g) return 1.0 / std::pow(u * p.c1 / p.At + std::pow(p.tau_0, p.alpha), 1.0 / p.alpha);
+  return 1.0 / p.tau_d;
+}
+static inline double rate_f_dt_d(const PCD& p, double u) {
+  const double q = u * p.normdt;
+  if (q < p.Bdt) return 1.0 / std::pow(q * p.c1 / p.Adt + std::pow(p.tau_0, p.alpha - 1.0), 1.0 / (p.alpha - 1.0));
+  return 1.0 / p.tau_d;
+}
+
+// ------------------------------------------------------------------ tables
+// Per-N factors of the sliding rates (ensemble_kernel.cu:153-178), evaluated
+// once in double and rounded to float.  x^0.75 = sqrt(x)*sqrt(sqrt(x)).
+struct Tables {
+  int nmax = 0;
+  std::vector<float> SIGP, SIGM, PWP, PWM, FRIC, SDC, SDD2, SDDN, CDC;
+};
+static double pow075(double x) { return std::sqrt(x) * std::sqrt(std::sqrt(x)); }
+
+Tables make_tables(int nmax, double beta_f, float prefact) {
+  Tables t;
+  t.nmax = nmax;
+  const int n = nmax + 2;
+  t.SIGP.assign(n, 0.f); t.SIGM.assign(n, 0.f); t.PWP.assign(n, 0.f); t.PWM.assign(n, 0.f);
+  t.SDC.assign(n, 0.f); t.SDD2.assign(n, 0.f); t.SDDN.assign(n, 0.f); t.CDC.assign(n, 0.f);
+  t.FRIC.assign(8 * (size_t)n + 8, 0.f);
+  for (int N = 1; N < n; ++N) {
+    const double d = N;
+    t.SIGP[N] = (float)(0.75 / (d * (d + 1.0)));
+    t.SIGM[N] = N >= 2 ? (float)(0.75 / (d * (d - 1.0))) : 0.f;
+    t.PWP[N] = (float)pow075(d / (d + 1.0));
+    t.PWM[N] = N >= 2 ? (float)pow075(d / (d - 1.0)) : 0.f;
+    t.SDC[N] = (float)(2.0 / (beta_f * (d + 0.5)));
+    t.SDD2[N] = (float)(1.0 / (0.75 + (d + 0.25)));
+    t.SDDN[N] = (float)(1.0 / (0.75 + 0.5 * d));
+    t.CDC[N] = (float)((double)prefact * (d - 1.0));
+  }
+  for (size_t i = 1; i < t.FRIC.size(); ++i) t.FRIC[i] = (float)(4.0 / (double)i);
+  return t;
+}
+
+// Sliding + CD components of pair (strand i, strand i+1) in the order the
+// reference tests them inside a pair: CD destruction, shift N_i+1, shift
+// N_i-1, CD creation inside strand i (ensemble_kernel.cu:304-414).
+static inline void pair_rates_f(const Tables& T, int cd, int N1, float q1, int N2, float q2,
+                                float taurate, float out[4]) {
+  const bool z1 = (q1 == 0.0f), z2 = (q2 == 0.0f);
+  float wp = 0.0f, wm = 0.0f;
+  if (N2 > 1) {
+    const int i = (z1 ? 4 * N1 + 1 : 2 * N1) + (z2 ? 4 * N2 - 1 : 2 * N2);
+    const float t2 = q2 * T.SIGM[N2];
+    const float arg = std::fmaf(q1, T.SIGP[N1], -t2);
+    const float pw = (z1 ? 1.0f : T.PWP[N1]) * (z2 ? 1.0f : T.PWM[N2]);
+    wp = (T.FRIC[i] * pw) * m_exp(arg);
+  }
+  if (N1 > 1) {
+    const int i = (z1 ? 4 * N1 - 1 : 2 * N1) + (z2 ? 4 * N2 + 1 : 2 * N2);
+    const float t1 = q1 * T.SIGM[N1];
+    const float arg = std::fmaf(q2, T.SIGP[N2], -t1);
+    const float pw = (z1 ? 1.0f : T.PWM[N1]) * (z2 ? 1.0f : T.PWP[N2]);
+    wm = (T.FRIC[i] * pw) * m_exp(arg);
+  }
+  out[0] = cd ? taurate : 0.0f;
+  out[1] = wp;
+  out[2] = wm;
+  out[3] = cd ? T.CDC[N1] : 0.0f;
+}
+
+// FP64 literal transcription of the same rates
+static inline void pair_rates_d(double beta_unused, int cd, double prefact, int N1, double q1,
+                                int N2, double q2, double taurate, double out[4]) {
+  (void)beta_unused;
+  double wp = 0.0, wm = 0.0;
+  const double n1 = N1, n2 = N2;
+  if (N2 > 1) {
+    const double sig1 = 0.75 / (n1 * (n1 + 1)), sig2 = 0.75 / (n2 * (n2 - 1));
+    const double pf1 = (q1 == 0.0) ? 1.0 : n1 / (n1 + 1), pf2 = (q2 == 0.0) ? 1.0 : n2 / (n2 - 1);
+    const double f1 = (q1 == 0.0) ? 2.0 * n1 + 0.5 : n1, f2 = (q2 == 0.0) ? 2.0 * n2 - 0.5 : n2;
+    wp = 2.0 / (f1 + f2) * std::pow(pf1 * pf2, 0.75) * std::exp(q1 * sig1 - q2 * sig2);
+  }
+  if (N1 > 1) {
+    const double sig1 = 0.75 / (n1 * (n1 - 1)), sig2 = 0.75 / (n2 * (n2 + 1));
+    const double pf1 = (q1 == 0.0) ? 1.0 : n1 / (n1 - 1), pf2 = (q2 == 0.0) ? 1.0 : n2 / (n2 + 1);
+    const double f1 = (q1 == 0.0) ? 2.0 * n1 - 0.5 : n1, f2 = (q2 == 0.0) ? 2.0 * n2 + 0.5 : n2;
+    wm = 2.0 / (f1 + f2) * std::pow(pf1 * pf2, 0.75) * std::exp(-q1 * sig1 + q2 * sig2);
+  }
+  out[0] = cd ? taurate : 0.0;
+  out[1] = wp;
+  out[2] = wm;
+  out[3] = cd ? prefact * (n1 - 1.0) : 0.0;
+}
+
+// ------------------------------------------------------------------ chains
+template <class R>
+struct Chain {
+  int nk = 0, Z = 0, stall = 0, S = 40;
+  int64_t T = 0;          // ticks (mode 0); unused in mode 1
+  double Td = 0.0;        // time (mode 1)
+  uint64_t step = 0, hash = 0xCBF29CE484222325ull;
+  R dt_prev = 0;
+  int64_t k_next = 0;     // next sample index
+  std::vector<int32_t> N;
+  std::vector<R> Qx, Qy, Qz, q2, tau;
+  // multi-tau correlator (FP64), common/eq_ensemble_kernel.cu:133-227
+  std::vector<double> cshift, cacc, cavg;
+  std::vector<int64_t> cnins;
+  std::vector<int32_t> cins, cnavg;
+};
+
+struct Ensemble {
+  orc_params P{};
+  std::vector<int32_t> nk_chain;
+  PCD pcd{};                    // monodisperse / prefactor source
+  std::vector<PCD> pcd_by_nk;   // polydisperse partner laws (index = NK)
+  float prefact = 0.f;          // CD creation prefactor (ensemble.cu:136-148)
+  double prefact_d = 0.0;
+  Tables tab;
+  float kap[9]{};
+  int z_max = 0, s0 = 40;
+  int64_t dt_sample_ticks = 0;
+  std::vector<Chain<float>> cf;
+  std::vector<Chain<double>> cd;
+  bool poly = false;
+};
+
+static inline U4 rng(const Ensemble& E, uint32_t purpose, uint64_t ctr, uint32_t hi24, uint32_t chain) {
+  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain, E.P.stream,
+                (uint32_t)E.P.seed, (uint32_t)(E.P.seed >> 32));
+}
+static inline U4 rng_step(const Ensemble& E, uint32_t purpose, uint64_t step, uint32_t chain) {
+  return rng(E, purpose, step, (uint32_t)(step >> 32), chain);
+}
+
+// Partner law for a new entanglement: monodisperse -> the ensemble's p_cd;
+// polydisperse -> p_cd of a partner chain drawn uniformly from the ensemble
+// (role of the GEX background draw, common/chain.cu:209-217).
+static inline const PCD& partner_pcd(const Ensemble& E, uint32_t w) {
+  if (!E.poly) return E.pcd;
+  const uint32_t idx = (uint32_t)(((uint64_t)w * (uint64_t)E.P.n_chains) >> 32);
+  return E.pcd_by_nk[E.nk_chain[idx]];
+}
+
+template <class R>
+void corr_alloc(const Ensemble& E, Chain<R>& c) {
+  if (E.P.corr_type < 0) return;
+  const int L = E.P.corr_levels, p = E.P.corr_p;
+  c.cshift.assign((size_t)L * p * 3, 0.0);
+  c.cacc.assign((size_t)L * p, 0.0);
+  c.cavg.assign((size_t)L * 3, 0.0);
+  c.cnins.assign(L, 0);
+  c.cins.assign(L, 0);
+  c.cnavg.assign(L, 0);
+}
+
+// common/eq_ensemble_kernel.cu:133-227 (type 0: stress autocorrelation)
+template <class R>
+void corr_add(const Ensemble& E, Chain<R>& c, const double v[3], int k) {
+  const int L = E.P.corr_levels, p = E.P.corr_p, m = E.P.corr_m, dmin = p / m;
+  if (k >= L) return;
+  const int ins = c.cins[k];
+  double* sh = &c.cshift[((size_t)k * p) * 3];
+  sh[ins * 3 + 0] = v[0]; sh[ins * 3 + 1] = v[1]; sh[ins * 3 + 2] = v[2];
+  double* av = &c.cavg[(size_t)k * 3];
+  av[0] += v[0]; av[1] += v[1]; av[2] += v[2];
+  c.cnavg[k]++;
+  if (c.cnavg[k] == m) {
+    const double w[3] = {av[0] / m, av[1] / m, av[2] / m};
+    av[0] = av[1] = av[2] = 0.0;
+    c.cnavg[k] = 0;
+    corr_add(E, c, w, k + 1);
+  }
+  c.cnins[k]++;
+  double* acc = &c.cacc[(size_t)k * p];
+  for (int j = (k == 0 ? 0 : dmin); j < p; ++j) {
+    if ((int64_t)j >= c.cnins[k]) break;
+    int i2 = ins - j;
+    if (i2 < 0) i2 += p;
+    acc[j] += v[0] * sh[i2 * 3 + 0] + v[1] * sh[i2 * 3 + 1] + v[2] * sh[i2 * 3 + 2];
+  }
+  c.cins[k] = (ins + 1 == p) ? 0 : ins + 1;
+}
+
+// shear stress sample (xy, yz, xz) of common/eq_ensemble_kernel.cu:282-294
+template <class R>
+void stress_sample(const Chain<R>& c, double v[3]) {
+  double sxy = 0, syz = 0, sxz = 0;
+  for (int i = 0; i < c.Z; ++i) {
+    const double x = c.Qx[i], y = c.Qy[i], z = c.Qz[i], n = c.N[i];
+    sxy -= 3.0 * x * y / n;
+    syz -= 3.0 * y * z / n;
+    sxz -= 3.0 * x * z / n;
+  }
+  v[0] = sxy; v[1] = syz; v[2] = sxz;
+}
+
+// ------------------------------------------------------------------ initialiser
+// Equilibrium state of common/chain.cu:199-283: Z-1 ~ Binomial(NK-1, 1/(1+beta))
+// with N uniform over compositions (chain.cu:106-156) is generated as
+// independent entanglement of each of the NK-1 bonds with probability
+// 1/(1+beta); Q ~ N(0, N/3) for internal strands, 0 for the dangling ends
+// (chain.cu:158-170,247-249); tau_CD rates from f_t (chain.cu:207-226).
+template <class R>
+void init_chain(const Ensemble& E, Chain<R>& c, uint32_t ci) {
+  const int nk = c.nk;
+  const double pe = 1.0 / (1.0 + E.P.beta);
+  double thr_d = std::floor(pe * 4294967296.0);
+  if (thr_d > 4294967295.0) thr_d = 4294967295.0;
+  const uint32_t thr = (uint32_t)thr_d;
+  std::vector<int> pos;
+  for (uint32_t att = 0; att < 64; ++att) {
+    pos.clear();
+    for (int b = 0; b < nk - 1; b += 4) {
+      const U4 r = rng(E, P_BONDS, (uint64_t)(b >> 2), att, ci);
+      const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+      for (int q = 0; q < 4 && b + q < nk - 1; ++q)
+        if (w[q] < thr) pos.push_back(b + q);
+    }
+    if ((int)pos.size() + 1 <= E.z_max) break;
+  }
+  if ((int)pos.size() + 1 > E.z_max) pos.resize(E.z_max - 1);
+  c.Z = (int)pos.size() + 1;
+  const int cap = E.z_max;
+  c.N.assign(cap + 1, 0);
+  c.Qx.assign(cap + 1, 0); c.Qy.assign(cap + 1, 0); c.Qz.assign(cap + 1, 0);
+  c.q2.assign(cap + 1, 0); c.tau.assign(cap + 1, 0);
+  int prev = -1;
+  for (int i = 0; i < c.Z - 1; ++i) { c.N[i] = pos[i] - prev; prev = pos[i]; }
+  c.N[c.Z - 1] = nk - 1 - prev;
+  for (int i = 1; i < c.Z - 1; ++i) {
+    const U4 r = rng(E, P_QINIT, (uint64_t)i, 0, ci);
+    if (E.P.mode == 0) {
+      float g0, g1, g2, g3;
+      m_gauss2(r.x, r.y, &g0, &g1);
+      m_gauss2(r.z, r.w, &g2, &g3);
+      const float sg = std::sqrt((float)c.N[i] / 3.0f);
+      c.Qx[i] = (R)(g0 * sg); c.Qy[i] = (R)(g1 * sg); c.Qz[i] = (R)(g2 * sg);
+    } else {
+      const double u1a = ((r.x >> 8) + 1u) * (1.0 / 16777216.0), u2a = (r.y >> 8) * (1.0 / 16777216.0);
+      const double u1b = ((r.z >> 8) + 1u) * (1.0 / 16777216.0);
+      const double ra = std::sqrt(-2.0 * std::log(u1a)), rb = std::sqrt(-2.0 * std::log(u1b));
+      const double tha = 2.0 * M_PI * u2a, thb = 2.0 * M_PI * ((r.w >> 8) * (1.0 / 16777216.0));
+      const double sg = std::sqrt(c.N[i] / 3.0);
+      c.Qx[i] = (R)(ra * std::cos(tha) * sg); c.Qy[i] = (R)(ra * std::sin(tha) * sg);
+      c.Qz[i] = (R)(rb * std::cos(thb) * sg);
+    }
+  }
+  for (int i = 0; i < c.Z; ++i) {
+    if (E.P.mode == 0) c.q2[i] = (R)m_q2((float)c.Qx[i], (float)c.Qy[i], (float)c.Qz[i]);
+    else c.q2[i] = c.Qx[i] * c.Qx[i] + c.Qy[i] * c.Qy[i] + c.Qz[i] * c.Qz[i];
+  }
+  for (int k = 0; k < c.Z - 1; ++k) {
+    const U4 r = rng(E, P_TAUINIT, (uint64_t)k, 0, ci);
+    const PCD& pp = partner_pcd(E, r.y);
+    if (!E.P.cd_flag) { c.tau[k] = 0; continue; }
+    if (E.P.mode == 0) c.tau[k] = (R)rate_f_t(pp, u01(r.x));
+    else c.tau[k] = (R)rate_f_t_d(pp, ((r.x >> 8) + 1u) * (1.0 / 16777216.0));
+  }
+  c.T = 0; c.Td = 0; c.step = 0; c.dt_prev = 0; c.stall = 0; c.k_next = 0;
+  c.hash = 0xCBF29CE484222325ull;
+  c.S = E.s0;
+  corr_alloc(E, c);
+}
+
+// ------------------------------------------------------------------ structural edits
+template <class R>
+void insert_at(Chain<R>& c, int i) {  // open strand slot i and tau slot i
+  for (int s = c.Z; s > i; --s) {
+    c.N[s] = c.N[s - 1]; c.Qx[s] = c.Qx[s - 1]; c.Qy[s] = c.Qy[s - 1];
+    c.Qz[s] = c.Qz[s - 1]; c.q2[s] = c.q2[s - 1]; c.tau[s] = c.tau[s - 1];
+  }
+}
+template <class R>
+void remove_strand(Chain<R>& c, int i) {  // close strand slot i
+  for (int s = i; s < c.Z - 1; ++s) {
+    c.N[s] = c.N[s + 1]; c.Qx[s] = c.Qx[s + 1]; c.Qy[s] = c.Qy[s + 1];
+    c.Qz[s] = c.Qz[s + 1]; c.q2[s] = c.q2[s + 1];
+  }
+}
+template <class R>
+void remove_tau(Chain<R>& c, int i) {  // close entanglement slot i
+  for (int s = i; s < c.Z - 2; ++s) c.tau[s] = c.tau[s + 1];
+}
+
+static inline float q2f(float x, float y, float z) { return m_q2(x, y, z); }
+static inline double q2f(double x, double y, double z) { return x * x + y * y + z * z; }
+
+// Apply a picked event (immediate form of ensemble_kernel.cu:312-501).
+// g[3]: normals for a new strand; trate: lifetime rate of a new entanglement;
+// newn: Kuhn steps of the new strand for a CD creation.
+template <class R>
+void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
+  const int Z = c.Z;
+  auto setQ = [&](int i, R x, R y, R z) {
+    c.Qx[i] = x; c.Qy[i] = y; c.Qz[i] = z; c.q2[i] = q2f(x, y, z);
+  };
+  switch (ev) {
+    case CDD: {  // merge strands j, j+1 (ensemble_kernel.cu:312-323)
+      const int n = c.N[j] + c.N[j + 1];
+      R x = c.Qx[j] + c.Qx[j + 1], y = c.Qy[j] + c.Qy[j + 1], z = c.Qz[j] + c.Qz[j + 1];
+      if (j == Z - 2 || j == 0) { x = 0; y = 0; z = 0; }
+      remove_strand(c, j + 1);  // strands > j+1 move down one slot
+      remove_tau(c, j);         // entanglement j disappears
+      c.N[j] = n; setQ(j, x, y, z);
+      c.Z = Z - 1;
+      break;
+    }
+    case SDP: c.N[j] += 1; c.N[j + 1] -= 1; break;
+    case SDM: c.N[j] -= 1; c.N[j + 1] += 1; break;
+    case CDC_MID: {  // split strand j (ensemble_kernel.cu:378-411)
+      const int N1 = c.N[j];
+      if (j == 0) {
+        const int nn = N1 - newn;
+        const R sg = (R)std::sqrt((R)nn / (R)3);
+        insert_at(c, 0);
+        c.N[0] = newn; setQ(0, 0, 0, 0);
+        c.N[1] = nn; setQ(1, g[0] * sg, g[1] * sg, g[2] * sg);
+        c.tau[0] = trate;
+      } else {
+        const R sg = (R)std::sqrt((R)(newn * (N1 - newn)) / (R)(3 * N1));
+        const R ra = (R)newn / (R)N1;
+        const R x1 = c.Qx[j], y1 = c.Qy[j], z1 = c.Qz[j];
+        R x, y, z;
+        if constexpr (sizeof(R) == 4) {
+          x = std::fmaf(x1, ra, g[0] * sg); y = std::fmaf(y1, ra, g[1] * sg); z = std::fmaf(z1, ra, g[2] * sg);
+        } else {
+          x = g[0] * sg + x1 * ra; y = g[1] * sg + y1 * ra; z = g[2] * sg + z1 * ra;
+        }
+        insert_at(c, j);
+        c.N[j] = newn; setQ(j, x, y, z);
+        c.N[j + 1] = N1 - newn; setQ(j + 1, x1 - x, y1 - y, z1 - z);
+        c.tau[j] = trate;
+      }
+      c.Z = Z + 1;
+      break;
+    }
+    case CDC_TAIL: {  // split the tail strand (ensemble_kernel.cu:422-443)
+      const int Nt = c.N[Z - 1];
+      const R sg = (Z == 1) ? (R)0 : (R)std::sqrt((R)newn / (R)3);
+      c.N[Z] = Nt - newn; setQ(Z, 0, 0, 0);
+      c.N[Z - 1] = newn; setQ(Z - 1, g[0] * sg, g[1] * sg, g[2] * sg);
+      c.tau[Z - 1] = trate;
+      c.Z = Z + 1;
+      break;
+    }
+    case SDC_HEAD: {  // ensemble_kernel.cu:459-468
+      const int n0 = c.N[0] - 1;
+      const R sg = (Z == 1) ? (R)0 : (R)std::sqrt((R)n0 / (R)3);
+      insert_at(c, 0);
+      c.N[0] = 1; setQ(0, 0, 0, 0);
+      c.N[1] = n0; setQ(1, g[0] * sg, g[1] * sg, g[2] * sg);
+      c.tau[0] = trate;
+      c.Z = Z + 1;
+      break;
+    }
+    case SDC_TAIL: {  // ensemble_kernel.cu:469-479
+      const int nt = c.N[Z - 1] - 1;
+      const R sg = (Z == 1) ? (R)0 : (R)std::sqrt((R)nt / (R)3);
+      c.N[Z] = 1; setQ(Z, 0, 0, 0);
+      c.N[Z - 1] = nt; setQ(Z - 1, g[0] * sg, g[1] * sg, g[2] * sg);
+      c.tau[Z - 1] = trate;
+      c.Z = Z + 1;
+      break;
+    }
+    case SDD_HEAD: {  // ensemble_kernel.cu:492-494
+      const int n = c.N[1] + 1;
+      remove_strand(c, 0);
+      remove_tau(c, 0);
+      c.N[0] = n; setQ(0, 0, 0, 0);
+      c.Z = Z - 1;
+      break;
+    }
+    case SDD_TAIL: {  // ensemble_kernel.cu:495-498
+      c.N[Z - 2] = c.N[Z - 2] + 1; setQ(Z - 2, 0, 0, 0);
+      c.Z = Z - 1;
+      break;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ FP32 mirror step
+struct Ends { float w[5]; };  // CD creation at tail, SD creation head, tail, SD destruction head, tail
+
+static inline Ends end_rates_f(const Ensemble& E, const Chain<float>& c) {
+  Ends e{};
+  const Tables& T = E.tab;
+  const int Z = c.Z;
+  const int Nh = c.N[0], Nt = c.N[Z - 1];
+  e.w[0] = E.P.cd_flag ? T.CDC[Nt] : 0.0f;
+  if (Z == 1) {
+    const float w1 = (float)(1.0 / (E.P.beta * (double)c.nk));
+    e.w[1] = w1; e.w[2] = w1; e.w[3] = 0; e.w[4] = 0;
+  } else {
+    if (Nh == 1) { e.w[1] = 0; e.w[3] = (Z == 2) ? T.SDD2[c.N[1]] : T.SDDN[c.N[1]]; }
+    else { e.w[1] = T.SDC[Nh]; e.w[3] = 0; }
+    if (Nt == 1) { e.w[2] = 0; e.w[4] = (Z == 2) ? T.SDD2[c.N[Z - 2]] : T.SDDN[c.N[Z - 2]]; }
+    else { e.w[2] = T.SDC[Nt]; e.w[4] = 0; }
+  }
+  return e;
+}
+
+static inline int fexp(float x) {  // floor(log2 x) for normal positive x, -200 otherwise
+  const uint32_t b = as_u(x);
+  const int e = (int)((b >> 23) & 0xff);
+  if (e == 0) return -200;
+  return e - 127;
+}
+
+static inline float pow2f(int s) {  // 2^s, s in [-126, 127]
+  return f_as((uint32_t)(s + 127) << 23);
+}
+
+// One kMC event of a chain in FP32-mirror arithmetic.  Returns false when the
+// chain stalls (the event is then not applied).
+bool step_mirror(const Ensemble& E, Chain<float>& c, uint32_t ci) {
+  const int Z = c.Z;
+  const int cd = E.P.cd_flag;
+  const int npair = Z - 1;
+  // all components (the reference recomputes every pair each step,
+  // ensemble_kernel.cu:114-186)
+  static thread_local std::vector<float> comp;
+  comp.resize((size_t)4 * (npair > 0 ? npair : 1));
+  int emax = -200;
+  bool bad_nan = false, bad_inf = false;
+  for (int j = 0; j < npair; ++j) {
+    float* o = &comp[(size_t)4 * j];
+    pair_rates_f(E.tab, cd, c.N[j], c.q2[j], c.N[j + 1], c.q2[j + 1], c.tau[j], o);
+    for (int q = 0; q < 4; ++q) {
+      if (o[q] != o[q]) bad_nan = true;
+      else if (o[q] == INFINITY) bad_inf = true;
+      else emax = std::max(emax, fexp(o[q]));
+    }
+  }
+  const Ends en = end_rates_f(E, c);
+  for (int q = 0; q < 5; ++q) emax = std::max(emax, fexp(en.w[q]));
+  if (bad_nan) { c.stall = 2; return false; }
+  if (bad_inf) { c.stall = 3; return false; }
+  // Fixed-point scale 2^S of the rate components.  Every component must stay
+  // below 2^(LIMIT_E+1); equilibrium only ever lowers S, flow also raises it
+  // again (up to s0) once 2^16 of headroom is free.
+  const bool flow = (E.kap[0] != 0 || E.kap[1] != 0 || E.kap[2] != 0 || E.kap[3] != 0 ||
+                     E.kap[4] != 0 || E.kap[5] != 0 || E.kap[6] != 0 || E.kap[7] != 0 ||
+                     E.kap[8] != 0);
+  if (emax + c.S > LIMIT_E) c.S = LIMIT_E - emax;
+  else if (flow && c.S < E.s0 && emax + c.S < LIMIT_E - 16) c.S = std::min(E.s0, LIMIT_E - emax);
+  const float sf = pow2f(c.S);
+  static thread_local std::vector<uint64_t> qc;
+  qc.resize((size_t)4 * (npair > 0 ? npair : 1));
+  uint64_t pair_total = 0;
+  for (int j = 0; j < npair; ++j)
+    for (int q = 0; q < 4; ++q) {
+      const uint64_t v = (uint64_t)std::llrint(comp[(size_t)4 * j + q] * sf);
+      qc[(size_t)4 * j + q] = v;
+      pair_total += v;
+    }
+  uint64_t qe[5], ends_total = 0;
+  for (int q = 0; q < 5; ++q) { qe[q] = (uint64_t)std::llrint(en.w[q] * sf); ends_total += qe[q]; }
+  const uint64_t total = pair_total + ends_total;
+  // dt = 1/sum W (ensemble_kernel.cu:262-272)
+  const float sumw = (float)(int64_t)total * pow2f(-c.S);
+  const float dt = 1.0f / sumw;
+  if (dt == 0.0f) { c.stall = 1; return false; }
+  if (!(dt < 2.0e9f)) { c.stall = 3; return false; }
+  const int64_t dtt = (int64_t)std::llrint(dt * 4294967296.0f);
+  // pick (ensemble_kernel.cu:274-288): pr uniform in [0,total)
+  const U4 r = rng_step(E, P_EVENT, c.step, ci);
+  const uint64_t u64 = ((uint64_t)r.y << 32) | r.x;
+  uint64_t pr = (uint64_t)(((unsigned __int128)total * u64) >> 64);
+  int ev = -1, j = -1;
+  uint64_t rem = 0, wsel = 0;
+  if (pr < pair_total) {
+    j = 0;
+    while (pr >= qc[(size_t)4 * j] + qc[(size_t)4 * j + 1] + qc[(size_t)4 * j + 2] + qc[(size_t)4 * j + 3]) {
+      pr -= qc[(size_t)4 * j] + qc[(size_t)4 * j + 1] + qc[(size_t)4 * j + 2] + qc[(size_t)4 * j + 3];
+      ++j;
+    }
+    const uint64_t* q4 = &qc[(size_t)4 * j];
+    if (pr < q4[0]) ev = CDD;
+    else if ((pr -= q4[0]) < q4[1]) ev = SDP;
+    else if ((pr -= q4[1]) < q4[2]) ev = SDM;
+    else { pr -= q4[2]; ev = CDC_MID; rem = pr; wsel = q4[3]; }
+  } else {
+    pr -= pair_total;
+    if (pr < qe[0]) { ev = CDC_TAIL; rem = pr; wsel = qe[0]; }
+    else if ((pr -= qe[0]) < qe[1]) ev = SDC_HEAD;
+    else if ((pr -= qe[1]) < qe[2]) ev = SDC_TAIL;
+    else if ((pr -= qe[2]) < qe[3]) ev = SDD_HEAD;
+    else ev = SDD_TAIL;
+  }
+  c.T += dtt;
+  const bool create = (ev == CDC_MID || ev == CDC_TAIL || ev == SDC_HEAD || ev == SDC_TAIL);
+  uint32_t code = (uint32_t)ev << 24 | (uint32_t)(j < 0 ? 0 : j);
+  if (create && Z >= E.z_max) {
+    code |= (uint32_t)NULL_FLAG << 24;  // refused at capacity (ensemble_kernel.cu:380,423,451)
+  } else if (create) {
+    int newn = 0;
+    if (ev == CDC_MID || ev == CDC_TAIL) {
+      const int N1 = (ev == CDC_MID) ? c.N[j] : c.N[Z - 1];
+      const double x = std::floor(0.5 + (double)rem * (double)(N1 - 2) / (double)wsel);
+      newn = (int)x + 1;
+      if (newn < 1) newn = 1;
+      if (newn > N1 - 1) newn = N1 - 1;
+    }
+    const U4 gr = rng_step(E, P_CREATE, c.step, ci);
+    float g[3], g3;
+    m_gauss2(gr.x, gr.y, &g[0], &g[1]);
+    m_gauss2(gr.z, gr.w, &g[2], &g3);
+    const PCD& pp = partner_pcd(E, r.w);
+    const float u = u01(r.z);
+    const float trate = cd ? ((ev == CDC_MID || ev == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
+    apply_event<float>(c, ev, j, newn, g, trate);
+    code |= (uint32_t)newn << 8;
+  } else {
+    apply_event<float>(c, ev, j, 0, nullptr, 0.0f);
+  }
+  c.hash = hash_step(c.hash, code);
+  c.step++;
+  c.dt_prev = dt;
+  return true;
+}
+
+// ------------------------------------------------------------------ FP64 step
+bool step_fp64(const Ensemble& E, Chain<double>& c, uint32_t ci) {
+  const int Z = c.Z;
+  const int cd = E.P.cd_flag;
+  const int npair = Z - 1;
+  static thread_local std::vector<double> comp;
+  comp.resize((size_t)4 * (npair > 0 ? npair : 1));
+  double pair_total = 0;
+  for (int j = 0; j < npair; ++j) {
+    pair_rates_d(E.P.beta, cd, E.prefact_d, c.N[j], c.q2[j], c.N[j + 1], c.q2[j + 1], c.tau[j],
+                 &comp[(size_t)4 * j]);
+    pair_total += comp[(size_t)4 * j] + comp[(size_t)4 * j + 1] + comp[(size_t)4 * j + 2] + comp[(size_t)4 * j + 3];
+  }
+  double w[5] = {0, 0, 0, 0, 0};
+  const double be = E.P.beta;
+  const int Nh = c.N[0], Nt = c.N[Z - 1];
+  w[0] = cd ? E.prefact_d * (Nt - 1.0) : 0.0;
+  if (Z == 1) { w[1] = w[2] = 1.0 / (be * c.nk); }
+  else {
+    if (Nh == 1) w[3] = 1.0 / (0.75 + ((Z == 2) ? c.N[1] + 0.25 : 0.5 * c.N[1]));
+    else w[1] = 2.0 / (be * (Nh + 0.5));
+    if (Nt == 1) w[4] = 1.0 / (0.75 + ((Z == 2) ? c.N[Z - 2] + 0.25 : 0.5 * c.N[Z - 2]));
+    else w[2] = 2.0 / (be * (Nt + 0.5));
+  }
+  const double sumw = pair_total + w[0] + w[1] + w[2] + w[3] + w[4];
+  const double dt = 1.0 / sumw;
+  if (!(sumw == sumw)) { c.stall = 2; return false; }
+  if (dt == 0.0) { c.stall = 1; return false; }
+  if (std::isinf(dt)) { c.stall = 3; return false; }
+  const U4 r = rng_step(E, P_EVENT, c.step, ci);
+  const uint64_t u64 = ((uint64_t)r.y << 32) | r.x;
+  double pr = sumw * ((double)(u64 >> 11) * (1.0 / 9007199254740992.0));
+  int ev = -1, j = 0;
+  double rem = 0, wsel = 1;
+  while (j < npair - 1) {
+    const double t = comp[(size_t)4 * j] + comp[(size_t)4 * j + 1] + comp[(size_t)4 * j + 2] + comp[(size_t)4 * j + 3];
+    if (pr < t) break;
+    pr -= t;
+    ++j;
+  }
+  if (npair > 0) {
+    const double* q4 = &comp[(size_t)4 * j];
+    const double t = q4[0] + q4[1] + q4[2] + q4[3];
+    if (pr < t) {
+      if (pr < q4[0]) ev = CDD;
+      else if ((pr -= q4[0]) < q4[1]) ev = SDP;
+      else if ((pr -= q4[1]) < q4[2]) ev = SDM;
+      else { pr -= q4[2]; ev = CDC_MID; rem = pr; wsel = q4[3]; }
+    } else pr -= t;
+  }
+  if (ev < 0) {
+    j = -1;
+    if (pr < w[0]) { ev = CDC_TAIL; rem = pr; wsel = w[0]; }
+    else if ((pr -= w[0]) < w[1]) ev = SDC_HEAD;
+    else if ((pr -= w[1]) < w[2]) ev = SDC_TAIL;
+    else if ((pr -= w[2]) < w[3]) ev = SDD_HEAD;
+    else if ((pr -= w[3]) < w[4]) ev = SDD_TAIL;
+    else ev = -2;  // roundoff past the last rate: null event
+  }
+  c.Td += dt;
+  if (ev >= 0) {
+    const bool create = (ev == CDC_MID || ev == CDC_TAIL || ev == SDC_HEAD || ev == SDC_TAIL);
+    if (create && Z >= E.z_max) {
+    } else if (create) {
+      int newn = 0;
+      if (ev == CDC_MID || ev == CDC_TAIL) {
+        const int N1 = (ev == CDC_MID) ? c.N[j] : c.N[Z - 1];
+        newn = (int)std::floor(0.5 + rem * (N1 - 2) / wsel) + 1;
+        newn = std::max(1, std::min(N1 - 1, newn));
+      }
+      const U4 gr = rng_step(E, P_CREATE, c.step, ci);
+      const double u1a = ((gr.x >> 8) + 1u) * (1.0 / 16777216.0), u2a = (gr.y >> 8) * (1.0 / 16777216.0);
+      const double u1b = ((gr.z >> 8) + 1u) * (1.0 / 16777216.0), u2b = (gr.w >> 8) * (1.0 / 16777216.0);
+      const double ra = std::sqrt(-2.0 * std::log(u1a)), rb = std::sqrt(-2.0 * std::log(u1b));
+      const double g[3] = {ra * std::cos(2 * M_PI * u2a), ra * std::sin(2 * M_PI * u2a), rb * std::cos(2 * M_PI * u2b)};
+      const PCD& pp = partner_pcd(E, r.w);
+      const double u = ((r.z >> 8) + 1u) * (1.0 / 16777216.0);
+      const double trate = cd ? ((ev == CDC_MID || ev == CDC_TAIL) ? rate_f_dt_d(pp, u) : rate_f_t_d(pp, u)) : 0.0;
+      apply_event<double>(c, ev, j, newn, g, trate);
+    } else {
+      apply_event<double>(c, ev, j, 0, nullptr, 0.0);
+    }
+  }
+  c.step++;
+  c.dt_prev = dt;
+  return true;
+}
+
+// flow deformation Q += dt kappa Q (ensemble_kernel.cu:105-110)
+void deform_f(const Ensemble& E, Chain<float>& c) {
+  const float dt = c.dt_prev;
+  float a[9];
+  for (int q = 0; q < 9; ++q) a[q] = dt * E.kap[q];
+  for (int i = 0; i < c.Z; ++i) {
+    const float x = c.Qx[i], y = c.Qy[i], z = c.Qz[i];
+    const float nx = std::fmaf(a[2], z, std::fmaf(a[1], y, std::fmaf(a[0], x, x)));
+    const float ny = std::fmaf(a[5], z, std::fmaf(a[4], y, std::fmaf(a[3], x, y)));
+    const float nz = std::fmaf(a[8], z, std::fmaf(a[7], y, std::fmaf(a[6], x, z)));
+    c.Qx[i] = nx; c.Qy[i] = ny; c.Qz[i] = nz; c.q2[i] = m_q2(nx, ny, nz);
+  }
+}
+void deform_d(const Ensemble& E, Chain<double>& c) {
+  const double dt = c.dt_prev;
+  for (int i = 0; i < c.Z; ++i) {
+    const double x = c.Qx[i], y = c.Qy[i], z = c.Qz[i];
+    const double* k = nullptr; (void)k;
+    c.Qx[i] = x + dt * E.kap[0] * x + dt * E.kap[1] * y + dt * E.kap[2] * z;
+    c.Qy[i] = y + dt * E.kap[3] * x + dt * E.kap[4] * y + dt * E.kap[5] * z;
+    c.Qz[i] = z + dt * E.kap[6] * x + dt * E.kap[7] * y + dt * E.kap[8] * z;
+    c.q2[i] = c.Qx[i] * c.Qx[i] + c.Qy[i] * c.Qy[i] + c.Qz[i] * c.Qz[i];
+  }
+}
+
+static bool is_flow(const Ensemble& E) {
+  for (int q = 0; q < 9; ++q) if (E.kap[q] != 0.0f) return true;
+  return false;
+}
+
+// Run one chain until its time reaches t_end (or step_limit events).  Per
+// iteration (common/ensemble_kernel.cu:114-207, eq_ensemble_kernel.cu:260-331):
+// deform by the previous dt (flow), take due stress samples (equilibrium),
+// stop if time >= t_end or stalled, else do one event.
+template <class R>
+int64_t run_chain(const Ensemble& E, Chain<R>& c, uint32_t ci, double t_end, int64_t step_limit) {
+  const bool flow = is_flow(E);
+  const int64_t tend_ticks = (int64_t)std::llrint(t_end * TICKS);
+  const bool corr = E.P.corr_type >= 0 && !flow;
+  int64_t done = 0;
+  for (;;) {
+    if (flow && c.dt_prev != (R)0) {
+      if constexpr (sizeof(R) == 4) deform_f(E, c); else deform_d(E, c);
+    }
+    if (corr) {
+      for (;;) {
+        if (c.k_next >= E.P.corr_nsamples) break;
+        bool due;
+        if constexpr (sizeof(R) == 4) due = c.T > c.k_next * E.dt_sample_ticks;
+        else due = c.Td > (double)c.k_next * E.P.corr_dt;
+        if (!due) break;
+        double v[3];
+        stress_sample(c, v);
+        corr_add(E, c, v, 0);
+        c.k_next++;
+      }
+    }
+    bool reached;
+    if constexpr (sizeof(R) == 4) reached = c.T >= tend_ticks;
+    else reached = c.Td >= t_end;
+    if (c.stall || reached || (step_limit >= 0 && (int64_t)c.step >= step_limit)) {
+      c.dt_prev = 0;
+      break;
+    }
+    bool ok;
+    if constexpr (sizeof(R) == 4) ok = step_mirror(E, c, ci); else ok = step_fp64(E, c, ci);
+    if (!ok) { c.dt_prev = 0; break; }
+    ++done;
+  }
+  return done;
+}
+
+}  // namespace
+
+// ====================================================================== C API
+extern "C" {
+
+void* orc_create(const orc_params* p) {
+  Ensemble* E = new Ensemble();
+  E->P = *p;
+  E->poly = p->nk_chain != nullptr;
+  E->z_max = p->z_max > 0 ? p->z_max : p->nk;
+  E->s0 = p->s0 > 0 ? p->s0 : 40;
+  for (int q = 0; q < 9; ++q) E->kap[q] = p->kappa[q];
+  E->nk_chain.assign(p->n_chains, p->nk);
+  if (E->poly) for (int i = 0; i < p->n_chains; ++i) E->nk_chain[i] = p->nk_chain[i];
+  E->P.nk_chain = nullptr;
+  const float be_f = (float)p->beta;
+  E->P.beta = (double)be_f;
+  int nkmax = 0;
+  for (int v : E->nk_chain) nkmax = std::max(nkmax, v);
+  if (E->poly) {
+    // CD creation prefactor = <normdt>/beta over the partner law
+    // (role of ensemble.cu:137-146)
+    E->pcd_by_nk.assign(nkmax + 1, PCD{});
+    std::vector<char> seen(nkmax + 1, 0);
+    for (int v : E->nk_chain) if (!seen[v]) { seen[v] = 1; E->pcd_by_nk[v] = make_pcd(E->P.beta, v); }
+    double s = 0;
+    for (int v : E->nk_chain) s += E->pcd_by_nk[v].normdt;
+    E->prefact = (float)((s / p->n_chains) / E->P.beta);
+    E->pcd = make_pcd(E->P.beta, p->nk);
+  } else {
+    E->pcd = make_pcd(E->P.beta, p->nk);
+    E->prefact = (float)(E->pcd.normdt / E->P.beta);
+  }
+  E->prefact_d = E->prefact;
+  E->tab = make_tables(nkmax, E->P.beta, E->prefact);
+  E->dt_sample_ticks = (int64_t)std::llrint(p->corr_dt * TICKS);
+  if (p->mode == 0) E->cf.resize(p->n_chains); else E->cd.resize(p->n_chains);
+  for (int i = 0; i < p->n_chains; ++i) {
+    if (p->mode == 0) E->cf[i].nk = E->nk_chain[i]; else E->cd[i].nk = E->nk_chain[i];
+  }
+  return E;
+}
+
+void orc_destroy(void* h) { delete (Ensemble*)h; }
+
+int orc_init_equilibrium(void* h, int nthreads) {
+  Ensemble* E = (Ensemble*)h;
+  const int n = E->P.n_chains;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int i = 0; i < n; ++i) {
+    if (E->P.mode == 0) init_chain(*E, E->cf[i], (uint32_t)i);
+    else init_chain(*E, E->cd[i], (uint32_t)i);
+  }
+  if (E->P.mode == 0) {
+    // initial fixed-point scale: min(s0, 47 - max exponent of all rates)
+    for (int i = 0; i < n; ++i) {
+      Chain<float>& c = E->cf[i];
+      int emax = -200;
+      for (int j = 0; j < c.Z - 1; ++j) {
+        float o[4];
+        pair_rates_f(E->tab, E->P.cd_flag, c.N[j], c.q2[j], c.N[j + 1], c.q2[j + 1], c.tau[j], o);
+        for (int q = 0; q < 4; ++q) emax = std::max(emax, fexp(o[q]));
+      }
+      const Ends en = end_rates_f(*E, c);
+      for (int q = 0; q < 5; ++q) emax = std::max(emax, fexp(en.w[q]));
+      c.S = std::min(E->s0, LIMIT_E - emax);
+    }
+  }
+  return 0;
+}
+
+// Load chain state in the reference layout: per chain z_max float4 {Qx,Qy,Qz,N}
+// and z_max float tau rates (chain.h:37-53).  Optional extended scalars.
+int orc_set_state(void* h, const int32_t* Z, const float* QN, const float* tau, const int64_t* T,
+                  const uint64_t* step, const float* dt_prev, const int32_t* stall, const int32_t* S) {
+  Ensemble* E = (Ensemble*)h;
+  if (E->P.mode != 0) return -3;
+  const int cap = E->z_max;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    Chain<float>& c = E->cf[i];
+    c.Z = Z[i];
+    c.N.assign(cap + 1, 0);
+    c.Qx.assign(cap + 1, 0); c.Qy.assign(cap + 1, 0); c.Qz.assign(cap + 1, 0);
+    c.q2.assign(cap + 1, 0); c.tau.assign(cap + 1, 0);
+    for (int s = 0; s < c.Z; ++s) {
+      const float* q = &QN[((size_t)i * cap + s) * 4];
+      c.Qx[s] = q[0]; c.Qy[s] = q[1]; c.Qz[s] = q[2]; c.N[s] = (int32_t)q[3];
+      c.q2[s] = m_q2(q[0], q[1], q[2]);
+      c.tau[s] = tau[(size_t)i * cap + s];
+    }
+    c.T = T ? T[i] : 0;
+    c.step = step ? step[i] : 0;
+    c.dt_prev = dt_prev ? dt_prev[i] : 0.f;
+    c.stall = stall ? stall[i] : 0;
+    c.S = S ? S[i] : E->s0;
+    c.hash = 0xCBF29CE484222325ull;
+    c.k_next = 0;
+    corr_alloc(*E, c);
+  }
+  return 0;
+}
+
+int orc_get_state(void* h, int32_t* Z, float* QN, float* tau, int64_t* T, uint64_t* step,
+                  float* dt_prev, int32_t* stall, int32_t* S, uint64_t* hash) {
+  Ensemble* E = (Ensemble*)h;
+  const int cap = E->z_max;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    if (E->P.mode == 0) {
+      const Chain<float>& c = E->cf[i];
+      if (Z) Z[i] = c.Z;
+      if (QN) for (int s = 0; s < cap; ++s) {
+        float* q = &QN[((size_t)i * cap + s) * 4];
+        if (s < c.Z) { q[0] = c.Qx[s]; q[1] = c.Qy[s]; q[2] = c.Qz[s]; q[3] = (float)c.N[s]; }
+        else { q[0] = q[1] = q[2] = q[3] = 0.f; }
+      }
+      if (tau) for (int s = 0; s < cap; ++s) tau[(size_t)i * cap + s] = (s < c.Z - 1) ? c.tau[s] : 0.f;
+      if (T) T[i] = c.T;
+      if (step) step[i] = c.step;
+      if (dt_prev) dt_prev[i] = c.dt_prev;
+      if (stall) stall[i] = c.stall;
+      if (S) S[i] = c.S;
+      if (hash) hash[i] = c.hash;
+    } else {
+      const Chain<double>& c = E->cd[i];
+      if (Z) Z[i] = c.Z;
+      if (QN) for (int s = 0; s < cap; ++s) {
+        float* q = &QN[((size_t)i * cap + s) * 4];
+        if (s < c.Z) { q[0] = (float)c.Qx[s]; q[1] = (float)c.Qy[s]; q[2] = (float)c.Qz[s]; q[3] = (float)c.N[s]; }
+        else { q[0] = q[1] = q[2] = q[3] = 0.f; }
+      }
+      if (tau) for (int s = 0; s < cap; ++s) tau[(size_t)i * cap + s] = (s < c.Z - 1) ? (float)c.tau[s] : 0.f;
+      if (T) T[i] = (int64_t)std::llrint(c.Td * TICKS);
+      if (step) step[i] = c.step;
+      if (dt_prev) dt_prev[i] = (float)c.dt_prev;
+      if (stall) stall[i] = c.stall;
+      if (S) S[i] = 0;
+      if (hash) hash[i] = 0;
+    }
+  }
+  return 0;
+}
+
+// Advance every chain to time t_end (or step_limit events; -1 = none).
+// Returns the number of kMC events done.
+int64_t orc_run(void* h, double t_end, int64_t step_limit, int nthreads) {
+  Ensemble* E = (Ensemble*)h;
+  const int n = E->P.n_chains;
+  int64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : total) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int i = 0; i < n; ++i) {
+    if (E->P.mode == 0) total += run_chain(*E, E->cf[i], (uint32_t)i, t_end, step_limit);
+    else total += run_chain(*E, E->cd[i], (uint32_t)i, t_end, step_limit);
+  }
+  return total;
+}
+
+// Ensemble-average stress at the current state (flow output; stress_calc of
+// ensemble_kernel.cu:504-538 averaged as in ensemble_call_block.cu:452-505):
+// out = {xx, yy, zz, xy, yz, zx, Lpp, Z} over non-stalled, non-NaN chains.
+int orc_stress(void* h, double* out, int32_t* count) {
+  Ensemble* E = (Ensemble*)h;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int cnt = 0;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int Z, stall;
+    auto sum = [&](auto& c) {
+      Z = c.Z; stall = c.stall;
+      for (int j = 0; j < c.Z; ++j) {
+        const double x = c.Qx[j], y = c.Qy[j], z = c.Qz[j], n = c.N[j];
+        s[0] -= 3 * x * x / n; s[1] -= 3 * y * y / n; s[2] -= 3 * z * z / n;
+        s[3] -= 3 * x * y / n; s[4] -= 3 * y * z / n; s[5] -= 3 * x * z / n;
+        s[6] += std::sqrt(x * x + y * y + z * z);
+      }
+      s[7] = c.Z;
+    };
+    if (E->P.mode == 0) sum(E->cf[i]); else sum(E->cd[i]);
+    if (stall != 0 || s[0] != s[0]) continue;
+    for (int q = 0; q < 8; ++q) acc[q] += s[q];
+    ++cnt;
+  }
+  for (int q = 0; q < 8; ++q) out[q] = cnt ? acc[q] / cnt : 0.0;
+  if (count) *count = cnt;
+  return 0;
+}
+
+// Correlator output: gsum[k*p + j] = sum over chains of acc/count, count[k*p+j]
+// (count of chain 0).  G(t) = gsum/3/N_cha at lag j*m^k samples
+// (correlator.cu:146-187, ensemble.cu:318-321).
+int orc_gt(void* h, double* gsum, int64_t* count) {
+  Ensemble* E = (Ensemble*)h;
+  if (E->P.corr_type < 0) return -3;
+  const int L = E->P.corr_levels, p = E->P.corr_p;
+  for (int q = 0; q < L * p; ++q) { gsum[q] = 0; if (count) count[q] = 0; }
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    auto add = [&](auto& c) {
+      for (int k = 0; k < L; ++k)
+        for (int j = 0; j < p; ++j) {
+          const int64_t n = c.cnins[k] - j;
+          if (n <= 0) continue;
+          if (k > 0 && j < p / E->P.corr_m) continue;
+          gsum[k * p + j] += c.cacc[(size_t)k * p + j] / (double)n;
+          if (count && i == 0) count[k * p + j] = n;
+        }
+    };
+    if (E->P.mode == 0) add(E->cf[i]); else add(E->cd[i]);
+  }
+  return 0;
+}
+
+// p_cd constants: out[12] fp64 fit values, outf[9] device-form floats
+int orc_pcd(double beta, double nk, double* out, float* outf) {
+  const PCD p = make_pcd((double)(float)beta, nk);
+  const double v[12] = {p.alpha, p.tau_0, p.tau_max, p.tau_d, p.g, p.c1, p.cm1, p.rcm1c1, p.At, p.Adt, p.Bdt, p.normdt};
+  for (int q = 0; q < 12; ++q) out[q] = v[q];
+  if (outf) {
+    const float f[9] = {p.At_, p.Dt_, p.Ct_, p.Adt_, p.Bdt_, p.Cdt_, p.Ddt_, p.tau_d_inv, p.one_minus_g};
+    for (int q = 0; q < 9; ++q) outf[q] = f[q];
+  }
+  return 0;
+}
+
+void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  const U4 r = philox(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
+// element-wise math spec, for unit tests: which = 0 exp, 1 log, 2 gauss pair
+// from words (x as bits), 3 sin2pi, 4 cos2pi
+void orc_math(int which, const float* x, const uint32_t* w, float* y, int n) {
+  for (int i = 0; i < n; ++i) {
+    switch (which) {
+      case 0: y[i] = m_exp(x[i]); break;
+      case 1: y[i] = m_log(x[i]); break;
+      case 2: { float a, b; m_gauss2(w[2 * i], w[2 * i + 1], &a, &b); y[2 * i] = a; y[2 * i + 1] = b; break; }
+      case 3: { float s, c; m_sincos2pi(w[i] & 0xffffffu, &s, &c); y[i] = s; break; }
+      case 4: { float s, c; m_sincos2pi(w[i] & 0xffffffu, &s, &c); y[i] = c; break; }
+      default: y[i] = 0; break;
+    }
+  }
+}
+
+// lifetime samplers for tests: kind 0 f_t, 1 f_d*t; mode 0 float spec, 1 fp64
+void orc_tau_sample(double beta, double nk, int kind, int mode, const float* u, double* out, int n) {
+  const PCD p = make_pcd((double)(float)beta, nk);
+  for (int i = 0; i < n; ++i) {
+    if (mode == 0) out[i] = kind == 0 ? rate_f_t(p, u[i]) : rate_f_dt(p, u[i]);
+    else out[i] = kind == 0 ? rate_f_t_d(p, u[i]) : rate_f_dt_d(p, u[i]);
+  }
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+"""ORACLE — test infrastructure only.
+
+ctypes binding of ``oracle/liboracle.so`` (the CPU restatement of the
+reference DSM kMC path, see dsm_oracle.cpp) and of ``oracle/_ref/libdsmref.so``
+(the reference's own host initialiser and p_cd, compiled from the reference
+tree).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline /
+reference legs use this module, as the checker or the timed CPU restatement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REFLIB = HERE / "_ref" / "libdsmref.so"
+REFSRC = Path("/root/reference/common")
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("beta", C.c_double), ("nk", C.c_int32), ("n_chains", C.c_int32), ("z_max", C.c_int32),
+        ("cd_flag", C.c_int32), ("kappa", C.c_float * 9), ("mode", C.c_int32), ("stream", C.c_uint32),
+        ("seed", C.c_uint64), ("corr_type", C.c_int32), ("corr_p", C.c_int32), ("corr_m", C.c_int32),
+        ("corr_levels", C.c_int32), ("corr_dt", C.c_double), ("corr_nsamples", C.c_int64),
+        ("nk_chain", C.c_void_p), ("s0", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+
+def build(ref: bool = False) -> None:
+    """make liboracle.so (and _ref/libdsmref.so when the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
+    if ref and REFSRC.exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        vp = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(OrcParams)]
+        L.orc_create.restype = vp
+        L.orc_destroy.argtypes = [vp]
+        L.orc_init_equilibrium.argtypes = [vp, C.c_int]
+        L.orc_set_state.argtypes = [vp] + [vp] * 8
+        L.orc_get_state.argtypes = [vp] + [vp] * 9
+        L.orc_run.argtypes = [vp, C.c_double, C.c_int64, C.c_int]
+        L.orc_run.restype = C.c_int64
+        L.orc_stress.argtypes = [vp, vp, vp]
+        L.orc_gt.argtypes = [vp, vp, vp]
+        L.orc_pcd.argtypes = [C.c_double, C.c_double, vp, vp]
+        L.orc_philox.argtypes = [vp, vp, vp]
+        L.orc_math.argtypes = [C.c_int, vp, vp, vp, C.c_int]
+        L.orc_tau_sample.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, vp, vp, C.c_int]
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def corr_levels_for(t_end: float, dt: float, p: int, m: int) -> int:
+    """common/main_cuda.cu:70"""
+    import math
+    return max(1, int(math.ceil(math.log(t_end / dt / p) / math.log(m)) + 1))
+
+
+class Oracle:
+    """One ensemble on the CPU.  mode 0 = FP32 mirror of the GPU arithmetic,
+    mode 1 = FP64 literal transcription."""
+
+    def __init__(self, *, beta=1.0, nk, n_chains, z_max=0, cd_flag=1, kappa=(0.0,) * 9, mode=0, seed=1,
+                 stream=0, corr=False, corr_p=64, corr_m=8, corr_levels=0, sync_dt=1.0, t_end=0.0,
+                 nk_chain: Optional[np.ndarray] = None, s0=0, threads=0):
+        L = lib()
+        p = OrcParams()
+        p.beta = float(np.float32(beta))
+        p.nk = nk
+        p.n_chains = n_chains
+        p.z_max = z_max if z_max > 0 else nk
+        p.cd_flag = cd_flag
+        for i, k in enumerate(kappa):
+            p.kappa[i] = k
+        p.mode = mode
+        p.stream = stream
+        p.seed = seed
+        flow = any(k != 0 for k in kappa)
+        p.corr_type = 0 if (corr and not flow) else -1
+        p.corr_p, p.corr_m = corr_p, corr_m
+        p.corr_levels = corr_levels if corr_levels > 0 else (corr_levels_for(t_end, sync_dt, corr_p, corr_m) if corr else 1)
+        p.corr_dt = sync_dt
+        import math
+        p.corr_nsamples = int(math.ceil(t_end / sync_dt)) if corr else 0
+        self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
+        p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
+        p.s0 = s0
+        self.p = p
+        self.n = n_chains
+        self.cap = p.z_max
+        self.threads = threads if threads > 0 else L.orc_num_threads()
+        self._h = L.orc_create(C.byref(p))
+
+    def close(self):
+        if self._h:
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_equilibrium(self):
+        lib().orc_init_equilibrium(self._h, self.threads)
+
+    def set_state(self, Z, QN, tau, T=None, step=None, dt_prev=None, stall=None, S=None):
+        a = lambda x, t: None if x is None else np.ascontiguousarray(x, dtype=t)
+        Z, QN, tau = a(Z, np.int32), a(QN, np.float32), a(tau, np.float32)
+        T, step, dt_prev, stall, S = a(T, np.int64), a(step, np.uint64), a(dt_prev, np.float32), a(stall, np.int32), a(S, np.int32)
+        rc = lib().orc_set_state(self._h, _p(Z), _p(QN), _p(tau), _p(T), _p(step), _p(dt_prev), _p(stall), _p(S))
+        assert rc == 0
+
+    def get_state(self) -> dict:
+        n, cap = self.n, self.cap
+        d = {"Z": np.zeros(n, np.int32), "QN": np.zeros((n, cap, 4), np.float32), "tau": np.zeros((n, cap), np.float32),
+             "T": np.zeros(n, np.int64), "step": np.zeros(n, np.uint64), "dt_prev": np.zeros(n, np.float32),
+             "stall": np.zeros(n, np.int32), "S": np.zeros(n, np.int32), "hash": np.zeros(n, np.uint64)}
+        lib().orc_get_state(self._h, _p(d["Z"]), _p(d["QN"]), _p(d["tau"]), _p(d["T"]), _p(d["step"]),
+                            _p(d["dt_prev"]), _p(d["stall"]), _p(d["S"]), _p(d["hash"]))
+        return d
+
+    def run(self, t_end: float, step_limit: int = -1) -> int:
+        return int(lib().orc_run(self._h, float(t_end), int(step_limit), self.threads))
+
+    def stress(self):
+        out = np.zeros(8, np.float64)
+        cnt = np.zeros(1, np.int32)
+        lib().orc_stress(self._h, _p(out), _p(cnt))
+        return out, int(cnt[0])
+
+    def gt_raw(self):
+        L, p = self.p.corr_levels, self.p.corr_p
+        g = np.zeros(L * p, np.float64)
+        c = np.zeros(L * p, np.int64)
+        lib().orc_gt(self._h, _p(g), _p(c))
+        return g.reshape(L, p), c.reshape(L, p)
+
+
+def pcd(beta: float, nk: float):
+    out = np.zeros(12, np.float64)
+    outf = np.zeros(9, np.float32)
+    lib().orc_pcd(float(beta), float(nk), _p(out), _p(outf))
+    return out, outf
+
+
+def philox(ctr, key):
+    c = np.asarray(ctr, np.uint32)
+    k = np.asarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().orc_philox(_p(c), _p(k), _p(o))
+    return o
+
+
+def math_f(which: int, x=None, w=None, n=None):
+    x = None if x is None else np.ascontiguousarray(x, np.float32)
+    w = None if w is None else np.ascontiguousarray(w, np.uint32)
+    n = n if n is not None else (len(x) if x is not None else len(w))
+    y = np.zeros(2 * n if which == 2 else n, np.float32)
+    lib().orc_math(which, _p(x), _p(w), _p(y), n)
+    return y
+
+
+def tau_samples(beta, nk, kind, mode, u):
+    u = np.ascontiguousarray(u, np.float32)
+    out = np.zeros(len(u), np.float64)
+    lib().orc_tau_sample(float(beta), float(nk), kind, mode, _p(u), _p(out), len(u))
+    return out
+
+
+# ---------------------------------------------------------------- compiled reference
+_ref = None
+
+
+def ref_lib() -> Optional[C.CDLL]:
+    """The reference's own host code (only where the reference tree was available)."""
+    global _ref
+    if _ref is None:
+        if not REFLIB.exists():
+            if REFSRC.exists():
+                build(ref=True)
+            else:
+                return None
+        R = C.CDLL(str(REFLIB))
+        R.ref_pcd.argtypes = [C.c_float, C.c_float, C.c_void_p]
+        R.ref_chain_init.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        R.ref_tau_samples.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _ref = R
+    return _ref

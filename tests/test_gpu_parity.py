@@ -1,0 +1,130 @@
+"""GPU (sm_103a, through the C ABI) against the oracle: integer state, event
+sequence, Q and lifetimes must agree bit for bit under the shared Philox
+streams; stress and G(t) within the stated tolerances."""
+import numpy as np
+import pytest
+
+from helpers import assert_bitexact, gpu_state, pair
+
+pytestmark = pytest.mark.gpu
+
+
+def test_init_bitexact(dsm_mod, oracle_mod):
+    g, o = pair(dsm_mod, oracle_mod, nk=25, n=1024, seed=1)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "S", "T", "step"), what="init")
+
+
+@pytest.mark.parametrize("nk,n,steps", [(25, 1024, 3000), (200, 128, 4000), (3, 64, 500), (1, 16, 200)])
+def test_fixed_steps_bitexact(dsm_mod, oracle_mod, nk, n, steps):
+    g, o = pair(dsm_mod, oracle_mod, nk=nk, n=n, seed=7)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    ev = g.advance(1.0e9, step_limit=steps)
+    evo = o.run(1.0e9, step_limit=steps)
+    assert ev == evo == n * steps
+    assert_bitexact(gpu_state(g), o.get_state(), what=f"nk={nk}")
+
+
+def test_time_windows_bitexact(dsm_mod, oracle_mod):
+    """Chains advanced in several windows on the GPU equal one oracle run."""
+    g, o = pair(dsm_mod, oracle_mod, nk=25, n=512, seed=3)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    tot = 0
+    for t in (5.0, 17.5, 40.0, 100.0):
+        tot += g.advance(t)
+    assert tot == o.run(100.0)
+    assert_bitexact(gpu_state(g), o.get_state(), what="windows")
+
+
+@pytest.mark.parametrize("beta,cd", [(0.5, 1), (2.0, 1), (1.0, 0)])
+def test_beta_cd_variants_bitexact(dsm_mod, oracle_mod, beta, cd):
+    g, o = pair(dsm_mod, oracle_mod, nk=40, n=256, seed=11, beta=beta, cd=cd)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(60.0)
+    o.run(60.0)
+    assert_bitexact(gpu_state(g), o.get_state(), what=f"beta={beta} cd={cd}")
+
+
+def test_capacity_refusal_bitexact(dsm_mod, oracle_mod):
+    """Creation refused at Z == z_max (null events, ensemble_kernel.cu:380,423,451)."""
+    g, o = pair(dsm_mod, oracle_mod, nk=30, n=256, seed=5, z_max=14)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(1.0e9, step_limit=3000)
+    o.run(1.0e9, step_limit=3000)
+    st = gpu_state(g)
+    assert st["Z"].max() == 14
+    assert_bitexact(st, o.get_state(), what="z_max=14")
+
+
+def test_flow_bitexact(dsm_mod, oracle_mod):
+    kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    g, o = pair(dsm_mod, oracle_mod, nk=50, n=256, seed=2, kappa=kap)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    for t in (10.0, 20.0, 30.0):
+        g.advance(t)
+        o.run(t)
+        assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash", "S", "stall", "dt_prev"),
+                        what=f"flow t={t}")
+        sg, cg = g.stress()
+        so, co = o.stress()
+        assert cg == co
+        # per-chain FP32 sums vs FP64: 1e-4 relative to the stress scale
+        scale = np.abs(so[:6]).max() + 1e-6
+        assert np.all(np.abs(sg[:6] - so[:6]) <= 1e-4 * scale + 1e-6), (sg, so)
+        assert abs(sg[6] - so[6]) <= 1e-5 * abs(so[6]) and sg[7] == pytest.approx(so[7], rel=1e-6)
+
+
+def test_polydisperse_bitexact(dsm_mod, oracle_mod):
+    rng = np.random.default_rng(7)
+    nkc = rng.integers(10, 120, size=300).astype(np.int32)
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=300, seed=9, nk_chain=nkc)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(30.0)
+    o.run(30.0)
+    st = gpu_state(g)
+    assert np.all(st["QN"][:, :, 3].sum(axis=1) == nkc)
+    assert_bitexact(st, o.get_state(), what="polydisperse")
+
+
+def test_correlator_against_oracle(dsm_mod, oracle_mod):
+    """G(t) sums: GPU FP32-compensated level 0 / FP64 long lags vs FP64 oracle."""
+    g, o = pair(dsm_mod, oracle_mod, nk=25, n=512, seed=1, corr=True, sync_dt=1.0, t_end=400.0,
+                corr_p=16, corr_m=2)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    for t in (100.0, 250.0, 400.0):
+        g.advance(t)
+    o.run(400.0)
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash"), what="corr run")
+    gs, gc = g.gt_raw()
+    os_, oc = o.gt_raw()
+    assert np.array_equal(gc, oc)
+    mask = oc > 0
+    rel = np.abs(gs[mask] - os_[mask]) / np.abs(os_[mask]).max()
+    assert rel.max() < 1e-5, rel.max()
+
+
+def test_set_get_roundtrip(dsm_mod, oracle_mod, tmp_path):
+    g, o = pair(dsm_mod, oracle_mod, nk=25, n=64, seed=4)
+    g.init_equilibrium()
+    g.advance(20.0)
+    heads, qn, tau = g.get_chains()
+    p = tmp_path / "conf.bin"
+    g.save(str(p))
+    g2 = dsm_mod.Ensemble(nk=25, n_chains=64, seed=4)
+    g2.load(str(p))
+    h2, q2, t2 = g2.get_chains()
+    assert np.array_equal(heads["Z"], h2["Z"]) and np.array_equal(qn, q2) and np.array_equal(tau, t2)
+    # continue both from the loaded conformations: oracle fed the same state
+    o.set_state(h2["Z"], q2, t2, T=g2.get_ext()["T"])
+    g2.advance(40.0)
+    o.run(40.0)
+    assert_bitexact(gpu_state(g2), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash", "S"),
+                    what="loaded")
