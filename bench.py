@@ -37,7 +37,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "kMC events/s on 1 GB300 (N_K=200); serve p50/p99 vs plain at G(t) err<=1%"
 UNIT = "events/s"
-N_CHAINS, NK, BETA = 65536, 200, 1.0
+NK, BETA = 200, 1.0
+N_CHAINS = 65536
 T_END_RUN, SAMPLE_DT, CORR_P, CORR_M = 1.0e7, 1.0, 64, 8
 
 
@@ -101,24 +102,23 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU legs
-def cpu_sample(target_s: float, threads: int = 0):
+def cpu_sample(target_s: float, threads: int = 0, n: int = 256):
     """Time the oracle (FP32 mirror, OpenMP over chains) on a bounded sample of the
     workload: n chains of N_K=200 from the equilibrium state, advanced by a window
     sized to ~target_s of CPU time after a short calibration."""
     from oracle import oracle as orc
 
     orc.build()
-    n = 256
     o = orc.Oracle(nk=NK, n_chains=n, seed=1, corr=True, sync_dt=SAMPLE_DT, t_end=T_END_RUN, corr_p=CORR_P,
                    corr_m=CORR_M, threads=threads)
     o.init_equilibrium()
     t0 = time.perf_counter()
-    ev = o.run(10.0)
+    ev = o.run(2.0)
     dt = time.perf_counter() - t0
     rate = ev / max(dt, 1e-6)
-    window = max(10.0, min(2000.0, target_s * rate / (n * 42.6)))
+    window = max(2.0, min(2000.0, target_s * rate / (n * 42.6)))
     t0 = time.perf_counter()
-    ev = o.run(10.0 + window)
+    ev = o.run(2.0 + window)
     dt = time.perf_counter() - t0
     return {"value": ev / dt, "unit": UNIT, "cores": o.threads, "kind": "port",
             "sample": f"{n} chains x {window:.0f} tau_K of the N_K=200 workload (oracle FP32 mirror, "
@@ -129,11 +129,13 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    per_step = max(3.0, 150.0 / max(1, args.steps + args.warmup))
-    base, o = cpu_sample(min(per_step, 20.0))
-    rates, t_cur = [], 2000.0 + 10.0
+    # whole run ~90 s of CPU time: a short calibration, then K+W steps of ~equal size
+    per_step = max(2.0, 80.0 / max(1, args.steps + args.warmup))
+    base, o = cpu_sample(3.0)
     n = o.n
-    window = max(5.0, per_step * base["value"] / (n * 42.6))
+    t_cur = 2.0 + float(base["sample"].split(" x ")[1].split(" ")[0])
+    rates = []
+    window = max(1.0, per_step * base["value"] / (n * 42.6))
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         ev = o.run(t_cur + window)
@@ -319,7 +321,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--chains", type=int, default=65536, help="chains per GPU (65536 = headline workload)")
     args = ap.parse_args()
+    global N_CHAINS
+    N_CHAINS = args.chains
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

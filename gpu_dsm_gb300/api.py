@@ -66,7 +66,9 @@ HEAD_DTYPE = np.dtype([("Z", np.int32), ("time", np.float32), ("dummy", np.float
 
 
 def lib_path() -> Path:
-    return _PKG / "libgpudsm.so"
+    """libgpudsm.so next to this module; GPU_DSM_LIB overrides the path."""
+    env = os.environ.get("GPU_DSM_LIB")
+    return Path(env) if env else _PKG / "libgpudsm.so"
 
 
 def load_library() -> C.CDLL:

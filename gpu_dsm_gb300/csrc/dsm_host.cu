@@ -67,20 +67,21 @@ static double pow075(double x) { return std::sqrt(x) * std::sqrt(std::sqrt(x)); 
 
 void dsm::make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off) {
   const size_t n = (size_t)nmax + 2;
-  off.SIGP = 0; off.SIGM = n; off.PWP = 2 * n; off.PWM = 3 * n; off.SDC = 4 * n; off.SDD2 = 5 * n;
-  off.SDDN = 6 * n; off.CDC = 7 * n; off.INV3N = 8 * n; off.FRIC = 9 * n;
   const size_t nf = 8 * n + 8;
-  buf.assign(9 * n + nf, 0.f);
+  off.NT = 0; off.NE = 4 * n; off.FRIC = 8 * n; off.INV3N = 8 * n + nf;
+  buf.assign(off.INV3N + n + 4, 0.f);
   for (size_t N = 1; N < n; ++N) {
     const double d = (double)N;
-    buf[off.SIGP + N] = (float)(0.75 / (d * (d + 1.0)));
-    buf[off.SIGM + N] = N >= 2 ? (float)(0.75 / (d * (d - 1.0))) : 0.f;
-    buf[off.PWP + N] = (float)pow075(d / (d + 1.0));
-    buf[off.PWM + N] = N >= 2 ? (float)pow075(d / (d - 1.0)) : 0.f;
-    buf[off.SDC + N] = (float)(2.0 / (beta_f * (d + 0.5)));
-    buf[off.SDD2 + N] = (float)(1.0 / (0.75 + (d + 0.25)));
-    buf[off.SDDN + N] = (float)(1.0 / (0.75 + 0.5 * d));
-    buf[off.CDC + N] = (float)((double)prefact * (d - 1.0));
+    float* nt = &buf[off.NT + 4 * N];
+    nt[0] = (float)(0.75 / (d * (d + 1.0)));
+    nt[1] = N >= 2 ? (float)(0.75 / (d * (d - 1.0))) : 0.f;
+    nt[2] = (float)pow075(d / (d + 1.0));
+    nt[3] = N >= 2 ? (float)pow075(d / (d - 1.0)) : 0.f;
+    float* ne = &buf[off.NE + 4 * N];
+    ne[0] = (float)(2.0 / (beta_f * (d + 0.5)));
+    ne[1] = (float)(1.0 / (0.75 + (d + 0.25)));
+    ne[2] = (float)(1.0 / (0.75 + 0.5 * d));
+    ne[3] = (float)((double)prefact * (d - 1.0));
     buf[off.INV3N + N] = (float)(3.0 / d);
   }
   for (size_t i = 1; i < nf; ++i) buf[off.FRIC + i] = (float)(4.0 / (double)i);
@@ -241,10 +242,8 @@ int dsm::sim_setup(dsm_sim* s) {
   E.t_end_ticks = 0; E.step_limit = INT64_MAX; E.watchdog_events = INT64_MAX;
   E.pcd = s->pcd.dev;
   E.pcd_by_nk = s->d_pcd_by_nk; E.nk_chain = s->d_nk_chain;
-  E.SIGP = s->d_tables + to.SIGP; E.SIGM = s->d_tables + to.SIGM; E.PWP = s->d_tables + to.PWP;
-  E.PWM = s->d_tables + to.PWM; E.FRIC = s->d_tables + to.FRIC; E.SDC = s->d_tables + to.SDC;
-  E.SDD2 = s->d_tables + to.SDD2; E.SDDN = s->d_tables + to.SDDN; E.CDC = s->d_tables + to.CDC;
-  E.INV3N = s->d_tables + to.INV3N;
+  E.NT = (const float4*)(s->d_tables + to.NT); E.NE = (const float4*)(s->d_tables + to.NE);
+  E.FRIC = s->d_tables + to.FRIC; E.INV3N = s->d_tables + to.INV3N;
   E.QN = s->d_QN; E.tau = s->d_tau; E.cs = s->d_cs;
   E.corr_shift = s->d_cshift; E.corr_acc = s->d_cacc; E.corr_avg = s->d_cavg; E.corr_cnt = s->d_ccnt;
   E.out_stress = s->d_stress; E.counters = s->d_counters;
@@ -417,8 +416,20 @@ extern "C" int dsm_set_ext(dsm_sim* s, const int64_t* T, const uint64_t* steps, 
 int dsm::sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit) {
   EnsDev& E = s->h;
   E.t_end_ticks = (int64_t)std::llrint(t_end * TICKS);
+  s->t_window = t_end;
   E.step_limit = step_limit < 0 ? INT64_MAX : step_limit;
-  E.watchdog_events = s->watchdog_events > 0 ? s->watchdog_events : INT64_MAX;
+  // Per-chain event cap of one launch: a chain whose dt collapses (rates blowing
+  // up) stops with stall code 5 instead of keeping the GPU busy.  The cap is
+  // 100x the expected events of the window (<sum W> ~ 0.25 N_K per tau_K), at
+  // least 2^24.
+  double expect = 0.0;
+  {
+    int64_t tmin = INT64_MAX;
+    (void)tmin;
+    expect = 0.25 * (double)s->nkmax * std::max(0.0, t_end - s->t_done) * 100.0;
+  }
+  const double wd = std::max(16777216.0, std::min(expect, 9.0e18));
+  E.watchdog_events = s->watchdog_events > 0 ? s->watchdog_events : (int64_t)wd;
   CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
   CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
   CK(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st));
@@ -440,6 +451,7 @@ int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
   CK(cudaGetLastError());
   if (events) *events = cnt[0];
   s->events_total += cnt[0];
+  s->t_done = std::max(s->t_done, s->t_window);
   s->last_events = cnt[0];
   CK(cudaEventElapsedTime(&s->last_kernel_ms, s->ev0, s->ev1));
   if (status & 1) return DSM_ABORTED;

@@ -16,7 +16,7 @@ struct HostPcd {  // p_cd fit (common/pcd_tau.h:26-66) in double + device form
   PcdDev dev;
 };
 
-struct TableOffsets { size_t SIGP, SIGM, PWP, PWM, SDC, SDD2, SDDN, CDC, INV3N, FRIC; };
+struct TableOffsets { size_t NT, NE, FRIC, INV3N; };  // float offsets into one buffer
 
 HostPcd make_pcd(double beta, double nk);
 void make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off);
@@ -37,6 +37,7 @@ struct dsm_sim {
   size_t bytes = 0;
   int sm_count = 0, blocks_per_sm = 0, grid = 0;
   int64_t watchdog_events = 0;
+  double t_done = 0.0, t_window = 0.0;  // lowest time all chains reached / target of the window
   unsigned long long events_total = 0, last_events = 0;
   float last_kernel_ms = 0.f;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -56,8 +56,15 @@ struct EnsDev {
   PcdDev pcd;                // monodisperse partner law
   const PcdDev* pcd_by_nk;   // polydisperse: partner law by N_K
   const int32_t* nk_chain;   // polydisperse: N_K of every chain
-  // per-N tables
-  const float *SIGP, *SIGM, *PWP, *PWM, *FRIC, *SDC, *SDD2, *SDDN, *CDC, *INV3N;
+  // per-N tables: NT[N] = {0.75/(N(N+1)), 0.75/(N(N-1)), (N/(N+1))^0.75, (N/(N-1))^0.75}
+  // (sliding-rate factors, ensemble_kernel.cu:153-178); NE[N] = {2/(beta(N+1/2)),
+  // 1/(1+N), 1/(3/4+N/2), prefact*(N-1)} (chain-end and CD creation rates,
+  // ensemble_kernel.cu:219-260,378); FRIC[i] = 4/i (friction 2/(f1+f2) with
+  // i = 2(f1+f2)); INV3N[N] = 3/N
+  const float4* NT;
+  const float4* NE;
+  const float* FRIC;
+  const float* INV3N;
   // state (reference layout: float4 {Qx,Qy,Qz,N} x cap per chain; tau rate x cap)
   float4* QN;
   float* tau;

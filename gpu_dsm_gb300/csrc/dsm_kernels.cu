@@ -2,20 +2,23 @@
 //
 // Design (one GB300, one process):
 //   * Each chain is simulated by ONE WARP that keeps the whole chain in shared
-//     memory (SoA slot: Q+Q^2 float4, N int, tau rate float, quantised pair
-//     rate uint64) inside a persistent loop.  Warps pull chains from an atomic
-//     work counter, load them with coalesced float4 loads, run them to the end
-//     of the launch window and write them back: HBM is touched only at window
-//     boundaries (and by the long-lag correlator levels).
+//     memory (slot: {Qx,Qy,Qz,Q^2} float4, N int, tau rate float, quantised
+//     rate uint64 per strand) inside a persistent loop.  Warps pull chains from
+//     an atomic work counter, load them with coalesced float4 loads, run them to
+//     the end of the launch window and write them back: HBM is touched only at
+//     window boundaries and by the long-lag correlator levels.
 //   * The event pick is exact integer arithmetic: every rate component is
-//     quantised to int64 fixed point (scale 2^S per chain), each lane sums a
-//     contiguous odd-width chunk of pair totals (bank-conflict free), a warp
-//     inclusive scan + ballot finds the lane, the lane walks its chunk.  The
-//     result does not depend on summation order, so the oracle reproduces it.
+//     quantised to int64 fixed point (scale 2^S per chain).  The quantised pair
+//     totals and the five chain-end rates form one array of Z-1+5 elements in
+//     the reference's pick order; each lane sums a contiguous odd-width chunk
+//     (bank-conflict free), one warp inclusive scan + ballot finds the lane, the
+//     lane walks its chunk.  Integer sums do not depend on order, so a CPU
+//     restatement reproduces the pick bit for bit.
 //   * Equilibrium: only the <=3 pair rates touched by an event are recomputed
-//     (the reference recomputes all of them every step, ensemble_kernel.cu
-//     strent_kernel).  Flow: all strands are deformed and all rates
-//     recomputed every step, as in the reference.
+//     (in parallel, one lane each), the chain-end rates only when a strand next
+//     to an end changes.  The reference recomputes every pair every step
+//     (ensemble_kernel.cu strent_kernel).  Flow: all strands are deformed and all
+//     rates recomputed every step, as in the reference.
 //   * Insert/remove of strands is a warp-cooperative memmove in shared memory
 //     (the reference defers it to the next step, ensemble_kernel.cu:64-102).
 //   * Randomness: Philox4x32-10; lane l computes the event words of step
@@ -30,6 +33,11 @@
 namespace dsm {
 
 #define FULL_MASK 0xffffffffu
+#define NEND 5
+// minimum resident blocks of 4 warps per SM the step kernel is compiled for
+#ifndef DSM_MINB
+#define DSM_MINB 4
+#endif
 
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ unsigned long long warp_incl_scan_u64(unsigned long long v, int lane) {
@@ -57,7 +65,7 @@ __device__ __forceinline__ unsigned long long quant(float x, float sf) {
   return (unsigned long long)__float2ll_rn(__fmul_rn(x, sf));
 }
 
-// Philox words of one event / one creation (counter layout shared with the oracle)
+// Philox words (counter layout shared with the oracle)
 __device__ __forceinline__ U4 rng_at(const EnsDev& E, uint32_t purpose, uint64_t ctr, uint32_t hi24,
                                      uint32_t chain) {
   return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain, E.stream, E.seed_lo, E.seed_hi);
@@ -76,45 +84,28 @@ __device__ __forceinline__ PcdDev partner_pcd(const EnsDev& E, uint32_t w) {
   return E.pcd_by_nk[__ldg(&E.nk_chain[idx])];
 }
 
-// Components {CD destruction, shift N1+1, shift N1-1, CD creation} of the pair
-// (strand j, strand j+1): ensemble_kernel.cu:149-181,304-414.
-__device__ __forceinline__ void pair_comp(const EnsDev& E, int N1, float q1, int N2, float q2,
-                                          float taurate, float o[4]) {
+// Shift components of the pair (strand j, strand j+1), ensemble_kernel.cu:149-179:
+// wp moves a Kuhn step from strand j+1 into strand j, wm the reverse.
+// a = NT[N1], b = NT[N2].
+__device__ __forceinline__ float shift_plus(const EnsDev& E, int N1, float q1, int N2, float q2, const float4& a,
+                                            const float4& b) {
   const bool z1 = (q1 == 0.0f), z2 = (q2 == 0.0f);
-  float wp = 0.0f, wm = 0.0f;
-  if (N2 > 1) {
-    const int i = (z1 ? 4 * N1 + 1 : 2 * N1) + (z2 ? 4 * N2 - 1 : 2 * N2);
-    const float t2 = __fmul_rn(q2, __ldg(&E.SIGM[N2]));
-    const float arg = __fmaf_rn(q1, __ldg(&E.SIGP[N1]), -t2);
-    const float pw = __fmul_rn(z1 ? 1.0f : __ldg(&E.PWP[N1]), z2 ? 1.0f : __ldg(&E.PWM[N2]));
-    wp = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
-  }
-  if (N1 > 1) {
-    const int i = (z1 ? 4 * N1 - 1 : 2 * N1) + (z2 ? 4 * N2 + 1 : 2 * N2);
-    const float t1 = __fmul_rn(q1, __ldg(&E.SIGM[N1]));
-    const float arg = __fmaf_rn(q2, __ldg(&E.SIGP[N2]), -t1);
-    const float pw = __fmul_rn(z1 ? 1.0f : __ldg(&E.PWM[N1]), z2 ? 1.0f : __ldg(&E.PWP[N2]));
-    wm = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
-  }
-  o[0] = E.cd_flag ? taurate : 0.0f;
-  o[1] = wp;
-  o[2] = wm;
-  o[3] = E.cd_flag ? __ldg(&E.CDC[N1]) : 0.0f;
+  const int i = (z1 ? 4 * N1 + 1 : 2 * N1) + (z2 ? 4 * N2 - 1 : 2 * N2);
+  const float t2 = __fmul_rn(q2, b.y);
+  const float arg = __fmaf_rn(q1, a.x, -t2);
+  const float pw = __fmul_rn(z1 ? 1.0f : a.z, z2 ? 1.0f : b.w);
+  const float w = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
+  return (N2 > 1) ? w : 0.0f;
 }
-
-// Chain-end rate q (0 CD creation at the tail, 1 SD creation head, 2 SD
-// creation tail, 3 SD destruction head, 4 SD destruction tail):
-// ensemble_kernel.cu:219-260.
-__device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const int* sN, float wz1) {
-  const int Nh = sN[0], Nt = sN[Z - 1];
-  switch (q) {
-    case 0: return E.cd_flag ? __ldg(&E.CDC[Nt]) : 0.0f;
-    case 1: return Z == 1 ? wz1 : (Nh == 1 ? 0.0f : __ldg(&E.SDC[Nh]));
-    case 2: return Z == 1 ? wz1 : (Nt == 1 ? 0.0f : __ldg(&E.SDC[Nt]));
-    case 3: return (Z == 1 || Nh != 1) ? 0.0f : (Z == 2 ? __ldg(&E.SDD2[sN[1]]) : __ldg(&E.SDDN[sN[1]]));
-    case 4: return (Z == 1 || Nt != 1) ? 0.0f : (Z == 2 ? __ldg(&E.SDD2[sN[Z - 2]]) : __ldg(&E.SDDN[sN[Z - 2]]));
-    default: return 0.0f;
-  }
+__device__ __forceinline__ float shift_minus(const EnsDev& E, int N1, float q1, int N2, float q2, const float4& a,
+                                             const float4& b) {
+  const bool z1 = (q1 == 0.0f), z2 = (q2 == 0.0f);
+  const int i = (z1 ? 4 * N1 - 1 : 2 * N1) + (z2 ? 4 * N2 + 1 : 2 * N2);
+  const float t1 = __fmul_rn(q1, a.y);
+  const float arg = __fmaf_rn(q2, b.x, -t1);
+  const float pw = __fmul_rn(z1 ? 1.0f : a.w, z2 ? 1.0f : b.z);
+  const float w = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
+  return (N1 > 1) ? w : 0.0f;
 }
 
 // status flags of a component: bit0 NaN, bit1 inf
@@ -123,11 +114,20 @@ __device__ __forceinline__ int comp_bad(float x) {
 }
 
 // ------------------------------------------------------------------ SMEM slot
+struct Corr0 {  // correlator level-0 counters of the resident chain
+  int ins, navg;
+  long long nins;
+  float a0, a1, a2;
+  int pad_;
+  long long k_next, t_next;
+};
+
 struct Slot {
   float4* Q;                // {Qx, Qy, Qz, Q^2} per strand
-  unsigned long long* R;    // quantised pair totals
+  unsigned long long* R;    // quantised pair totals, then the 5 chain-end rates
   int* N;                   // Kuhn steps per strand
   float* T;                 // CD lifetime rates per entanglement
+  Corr0* k0;                // correlator level-0 counters
   float* Csh;               // correlator level-0 shift register [p][3]
   float2* Cacc;             // correlator level-0 compensated sums [p]
 };
@@ -135,8 +135,9 @@ struct Slot {
 __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax) {
-  const size_t n = (size_t)slot_cap + 1;
-  size_t b = n * 16 + n * 8 + n * 4 + n * 4;
+  const size_t n = (size_t)slot_cap + 1, nr = (size_t)slot_cap + NEND + 1;
+  size_t b = n * 16 + nr * 8 + n * 4 + n * 4;
+  b = align_up(b, 16) + sizeof(Corr0);
   b = align_up(b, 8) + (size_t)pmax * 12;
   b = align_up(b, 8) + (size_t)pmax * 8;
   return align_up(b, 16);
@@ -144,12 +145,14 @@ __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax) {
 
 __device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int pmax) {
   Slot s;
-  const size_t n = (size_t)slot_cap + 1;
+  const size_t n = (size_t)slot_cap + 1, nr = (size_t)slot_cap + NEND + 1;
   s.Q = (float4*)base;
   s.R = (unsigned long long*)(base + n * 16);
-  s.N = (int*)(base + n * 24);
-  s.T = (float*)(base + n * 28);
-  size_t off = align_up(n * 32, 8);
+  s.N = (int*)(base + n * 16 + nr * 8);
+  s.T = (float*)(base + n * 20 + nr * 8);
+  size_t off = align_up(n * 24 + nr * 8, 16);
+  s.k0 = (Corr0*)(base + off);
+  off = align_up(off + sizeof(Corr0), 8);
   s.Csh = (float*)(base + off);
   off = align_up(off + (size_t)pmax * 12, 8);
   s.Cacc = (float2*)(base + off);
@@ -182,15 +185,41 @@ __device__ __forceinline__ void move_down(T* a, int lo, int hi, int lane) {  // 
   }
 }
 
-// recompute quantised pair totals of pairs [p0, p0+cnt) (cnt <= 32) in
-// parallel; returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 overflow
-__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt,
-                                            int lane) {
+// float components {CD destruction, shift +1, shift -1, CD creation} of pair p
+// (ensemble_kernel.cu:149-181,304-414)
+__device__ __forceinline__ void pair_floats(const EnsDev& E, const Slot& sl, int p, float o[4]) {
+  const int N1 = sl.N[p], N2 = sl.N[p + 1];
+  const float q1 = sl.Q[p].w, q2 = sl.Q[p + 1].w;
+  const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
+  o[0] = E.cd_flag ? sl.T[p] : 0.0f;
+  o[1] = shift_plus(E, N1, q1, N2, q2, a, b);
+  o[2] = shift_minus(E, N1, q1, N2, q2, a, b);
+  o[3] = E.cd_flag ? __ldg(&E.NE[N1]).w : 0.0f;
+}
+
+// Chain-end component q (0 CD creation at the tail, 1 SD creation head, 2 SD
+// creation tail, 3 SD destruction head, 4 SD destruction tail),
+// ensemble_kernel.cu:219-260; branch-free over the five lanes.
+__device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const int* sN, float wz1) {
+  const bool tail = (q == 0) || (q == 2) || (q == 4);
+  const int Ne = tail ? sN[Z - 1] : sN[0];
+  const int Nn = (Z >= 2) ? (tail ? sN[Z - 2] : sN[1]) : 1;
+  const float4 e1 = __ldg(&E.NE[Ne]);
+  const float4 e2 = __ldg(&E.NE[Nn]);
+  const float cdc = E.cd_flag ? e1.w : 0.0f;
+  const float sdc = (Z == 1) ? wz1 : ((Ne == 1) ? 0.0f : e1.x);
+  const float sdd = (Z == 1 || Ne != 1) ? 0.0f : ((Z == 2) ? e2.y : e2.z);
+  return (q == 0) ? cdc : ((q <= 2) ? sdc : sdd);
+}
+
+// recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 32), one lane each;
+// returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 scale overflow
+__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, int lane) {
   int flags = 0;
   const int p = p0 + lane;
   if (lane < cnt && p >= 0 && p < Z - 1) {
     float o[4];
-    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
+    pair_floats(E, sl, p, o);
     const float sf = pow2f(S);
     unsigned long long tot = 0;
 #pragma unroll
@@ -205,37 +234,49 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
   return __reduce_or_sync(FULL_MASK, flags);
 }
 
-// full pass over all pairs: float components -> max exponent & flags, then
-// quantise with the scale chosen by the rule shared with the oracle.
-// Returns the new S; *flags gets NaN/inf bits.
+// Full pass over all pairs and the chain ends: quantise with the current scale,
+// track the max exponent; apply the scale rule shared with the oracle (lower on
+// overflow; flow raises again once 2^16 of headroom is free) and requantise if S
+// changes.  Returns the new S; *flags_out gets NaN/inf bits (S kept then).
 template <bool FLOW>
-__device__ int full_pairs(const EnsDev& E, Slot& sl, int Z, int S, float eval, int lane, int* flags_out) {
+__device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, int lane, int* flags_out) {
   const int np = Z - 1;
   int emax = -200, flags = 0;
+  const float sf = pow2f(S);
   for (int p = lane; p < np; p += 32) {
     float o[4];
-    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
+    pair_floats(E, sl, p, o);
+    unsigned long long tot = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int b = comp_bad(o[q]);
       flags |= b;
       if (!b) emax = max(emax, fexp(o[q]));
+      tot += quant(o[q], sf);
     }
+    sl.R[p] = tot;
   }
-  // chain-end components are part of the same scale decision
-  emax = max(emax, (lane < 5) ? fexp(eval) : -200);
+  float ev = 0.0f;
+  if (lane < NEND) {
+    ev = end_comp(E, lane, Z, sl.N, wz1);
+    emax = max(emax, fexp(ev));
+    sl.R[np + lane] = quant(ev, sf);
+  }
   emax = warp_max_i(emax);
   flags = __reduce_or_sync(FULL_MASK, flags);
   int Snew = S;
-  if (flags != 0) {
-    // the chain stalls before any event: keep the scale (oracle order)
-  } else if (emax + S > LIMIT_E) Snew = LIMIT_E - emax;
-  else if (FLOW && S < E.s0 && emax + S < LIMIT_E - S_HYST) Snew = min(E.s0, LIMIT_E - emax);
-  const float sf = pow2f(Snew);
-  for (int p = lane; p < np; p += 32) {
-    float o[4];
-    pair_comp(E, sl.N[p], sl.Q[p].w, sl.N[p + 1], sl.Q[p + 1].w, sl.T[p], o);
-    sl.R[p] = quant(o[0], sf) + quant(o[1], sf) + quant(o[2], sf) + quant(o[3], sf);
+  if (flags == 0) {
+    if (emax + S > LIMIT_E) Snew = LIMIT_E - emax;
+    else if (FLOW && S < E.s0 && emax + S < LIMIT_E - S_HYST) Snew = min(E.s0, LIMIT_E - emax);
+  }
+  if (Snew != S) {
+    const float sf2 = pow2f(Snew);
+    for (int p = lane; p < np; p += 32) {
+      float o[4];
+      pair_floats(E, sl, p, o);
+      sl.R[p] = quant(o[0], sf2) + quant(o[1], sf2) + quant(o[2], sf2) + quant(o[3], sf2);
+    }
+    if (lane < NEND) sl.R[np + lane] = quant(ev, sf2);
   }
   __syncwarp();
   *flags_out = flags;
@@ -243,9 +284,9 @@ __device__ int full_pairs(const EnsDev& E, Slot& sl, int Z, int S, float eval, i
 }
 
 // ------------------------------------------------------------------ correlator
-// Level >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
+// Levels >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
 // push the block average w into level 1 and cascade while blocks complete.
-__device__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, int lane) {
+__device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, int lane) {
   const int L = E.corr_levels, p = E.corr_p, m = E.corr_m, dmin = p / m;
   for (int k = 1; k < L; ++k) {
     const size_t lk = (size_t)c * L + k;
@@ -283,60 +324,168 @@ __device__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, flo
   }
 }
 
-struct Corr0 {  // level-0 counters kept in registers during a residency
-  int ins, navg;
-  long long nins;
-  float a0, a1, a2;
-};
-
-// shear-stress sample (eq_ensemble_kernel.cu:282-294) into correlator level 0
-__device__ void corr_sample(const EnsDev& E, Slot& sl, int Z, int c, Corr0& k0, int lane) {
-  float sxy = 0.f, syz = 0.f, sxz = 0.f;
-  for (int s = lane; s < Z; s += 32) {
-    const float4 q = sl.Q[s];
-    const float w = __ldg(&E.INV3N[sl.N[s]]);
-    sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
-    syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
-    sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
-  }
-  sxy = warp_sum_f(sxy); syz = warp_sum_f(syz); sxz = warp_sum_f(sxz);
+// Take every stress sample due at chain time T (eq_ensemble_kernel.cu:281-331):
+// shear stresses (xy, yz, xz) of the current state into correlator level 0.
+__device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int c, long long T, int lane) {
+  Corr0& k0 = *sl.k0;
   const int p = E.corr_p, m = E.corr_m;
-  __syncwarp();
-  if (lane == 0) { sl.Csh[k0.ins * 3 + 0] = sxy; sl.Csh[k0.ins * 3 + 1] = syz; sl.Csh[k0.ins * 3 + 2] = sxz; }
-  __syncwarp();
-  const long long n0 = k0.nins + 1;
-  for (int j = lane; j < p; j += 32) {
-    if ((long long)j >= n0) break;
-    int i2 = k0.ins - j;
-    if (i2 < 0) i2 += p;
-    const float pv = __fmaf_rn(sxz, sl.Csh[i2 * 3 + 2], __fmaf_rn(syz, sl.Csh[i2 * 3 + 1], __fmul_rn(sxy, sl.Csh[i2 * 3 + 0])));
-    // Kahan-compensated FP32 accumulation
-    float2 a = sl.Cacc[j];
-    const float y = __fsub_rn(pv, a.y);
-    const float t = __fadd_rn(a.x, y);
-    a.y = __fsub_rn(__fsub_rn(t, a.x), y);
-    a.x = t;
-    sl.Cacc[j] = a;
+  while (k0.k_next < E.nsamples && T > k0.t_next) {
+    float sxy = 0.f, syz = 0.f, sxz = 0.f;
+    for (int s = lane; s < Z; s += 32) {
+      const float4 q = sl.Q[s];
+      const float w = __ldg(&E.INV3N[sl.N[s]]);
+      sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
+      syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
+      sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
+    }
+    sxy = warp_sum_f(sxy); syz = warp_sum_f(syz); sxz = warp_sum_f(sxz);
+    const int ins = k0.ins;
+    const long long n0 = k0.nins + 1;
+    __syncwarp();
+    if (lane == 0) { sl.Csh[ins * 3 + 0] = sxy; sl.Csh[ins * 3 + 1] = syz; sl.Csh[ins * 3 + 2] = sxz; }
+    __syncwarp();
+    for (int j = lane; j < p; j += 32) {
+      if ((long long)j >= n0) break;
+      int i2 = ins - j;
+      if (i2 < 0) i2 += p;
+      const float pv = __fmaf_rn(sxz, sl.Csh[i2 * 3 + 2], __fmaf_rn(syz, sl.Csh[i2 * 3 + 1], __fmul_rn(sxy, sl.Csh[i2 * 3 + 0])));
+      // Kahan-compensated FP32 accumulation
+      float2 a = sl.Cacc[j];
+      const float y = __fsub_rn(pv, a.y);
+      const float t = __fadd_rn(a.x, y);
+      a.y = __fsub_rn(__fsub_rn(t, a.x), y);
+      a.x = t;
+      sl.Cacc[j] = a;
+    }
+    const float a0 = __fadd_rn(k0.a0, sxy), a1 = __fadd_rn(k0.a1, syz), a2 = __fadd_rn(k0.a2, sxz);
+    const int navg = k0.navg + 1;
+    __syncwarp();
+    if (lane == 0) {
+      k0.ins = (ins + 1 == p) ? 0 : ins + 1;
+      k0.nins = n0;
+      if (navg == m) { k0.a0 = k0.a1 = k0.a2 = 0.f; k0.navg = 0; }
+      else { k0.a0 = a0; k0.a1 = a1; k0.a2 = a2; k0.navg = navg; }
+      k0.k_next += 1;
+      k0.t_next += E.dt_sample_ticks;
+    }
+    __syncwarp();
+    if (navg == m && E.corr_levels > 1) {
+      const float rm = (float)m;
+      corr_push_levels(E, c, __fdiv_rn(a0, rm), __fdiv_rn(a1, rm), __fdiv_rn(a2, rm), lane);
+    }
   }
-  k0.ins = (k0.ins + 1 == p) ? 0 : k0.ins + 1;
-  k0.nins = n0;
-  k0.a0 = __fadd_rn(k0.a0, sxy); k0.a1 = __fadd_rn(k0.a1, syz); k0.a2 = __fadd_rn(k0.a2, sxz);
-  if (++k0.navg == m) {
-    const float rm = (float)m;
-    const float w0 = __fdiv_rn(k0.a0, rm), w1 = __fdiv_rn(k0.a1, rm), w2 = __fdiv_rn(k0.a2, rm);
-    k0.a0 = k0.a1 = k0.a2 = 0.f;
-    k0.navg = 0;
-    if (E.corr_levels > 1) corr_push_levels(E, c, w0, w1, w2, lane);
+}
+
+// ------------------------------------------------------------------ creation events
+// Apply a creation (CD inside strand j / CD at the tail / SD at head or tail):
+// returns newn and the pairs to recompute (up0, upn).
+__device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int j, int Z, int c, uint64_t step,
+                                         unsigned long long rem, unsigned long long wsel, uint32_t w2, uint32_t w3,
+                                         int lane, int* up0_out, int* upn_out) {
+  int newn = 0;
+  if (evn == CDC_MID || evn == CDC_TAIL) {
+    const int N1 = (evn == CDC_MID) ? sl.N[j] : sl.N[Z - 1];
+    const double x = floor(__dadd_rn(0.5, __ddiv_rn(__dmul_rn(__ull2double_rn(rem), (double)(N1 - 2)),
+                                                  __ull2double_rn(wsel))));
+    newn = (int)x + 1;
+    newn = max(1, min(N1 - 1, newn));
+  }
+  const U4 gr = rng_at(E, P_CREATE, step, (uint32_t)(step >> 32), (uint32_t)c);
+  float g0, g1, g2, g3;
+  m_gauss2(gr.x, gr.y, &g0, &g1);
+  m_gauss2(gr.z, gr.w, &g2, &g3);
+  const PcdDev pp = partner_pcd(E, w3);
+  const float u = u01(w2);
+  const float trate = E.cd_flag ? ((evn == CDC_MID || evn == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
+  if (evn == CDC_MID && j > 0) {
+    const int N1 = sl.N[j];
+    const float4 q1 = sl.Q[j];
+    __syncwarp();
+    move_up(sl.Q, j, Z, lane); move_up(sl.N, j, Z, lane);
+    move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane);
+    if (lane == 0) {
+      const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
+      const float ra = __fdiv_rn((float)newn, (float)N1);
+      const float x = __fmaf_rn(q1.x, ra, __fmul_rn(g0, sg));
+      const float y = __fmaf_rn(q1.y, ra, __fmul_rn(g1, sg));
+      const float z = __fmaf_rn(q1.z, ra, __fmul_rn(g2, sg));
+      sl.N[j] = newn; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+      const float x2 = __fsub_rn(q1.x, x), y2 = __fsub_rn(q1.y, y), z2 = __fsub_rn(q1.z, z);
+      sl.N[j + 1] = N1 - newn; sl.Q[j + 1] = make_float4(x2, y2, z2, m_q2(x2, y2, z2));
+      sl.T[j] = trate;
+    }
+    *up0_out = j - 1; *upn_out = 3;
+  } else if ((evn == CDC_MID && j == 0) || evn == SDC_HEAD) {
+    const int N0 = sl.N[0];
+    const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
+    const int nd = (evn == SDC_HEAD) ? 1 : newn;
+    __syncwarp();
+    move_up(sl.Q, 0, Z, lane); move_up(sl.N, 0, Z, lane);
+    move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane);
+    if (lane == 0) {
+      const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+      const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+      sl.N[0] = nd; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+      sl.N[1] = nn; sl.Q[1] = make_float4(x, y, z, m_q2(x, y, z));
+      sl.T[0] = trate;
+    }
+    *up0_out = 0; *upn_out = 2;
+  } else {  // CDC_TAIL, SDC_TAIL
+    const int Nt = sl.N[Z - 1];
+    const int nn = (evn == SDC_TAIL) ? Nt - 1 : newn;
+    const int nd = (evn == SDC_TAIL) ? 1 : Nt - newn;
+    __syncwarp();
+    if (lane == 0) {
+      const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+      const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+      sl.N[Z] = nd; sl.Q[Z] = make_float4(0.f, 0.f, 0.f, 0.f);
+      sl.N[Z - 1] = nn; sl.Q[Z - 1] = make_float4(x, y, z, m_q2(x, y, z));
+      sl.T[Z - 1] = trate;
+    }
+    *up0_out = Z - 2; *upn_out = 2;
+  }
+  __syncwarp();
+  return newn;
+}
+
+// Apply a destruction (CD of pair j, SD at head or tail): sets the pairs to
+// recompute (up0, upn).
+__device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, int lane, int* up0_out, int* upn_out) {
+  if (evn == CDD) {  // ensemble_kernel.cu:312-323
+    const int n = sl.N[j] + sl.N[j + 1];
+    const float4 a = sl.Q[j], b = sl.Q[j + 1];
+    const bool endp = (j == Z - 2) || (j == 0);
+    __syncwarp();
+    move_down(sl.Q, j + 2, Z, lane); move_down(sl.N, j + 2, Z, lane);
+    move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane);
+    if (lane == 0) {
+      const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
+      const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
+      const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
+      sl.N[j] = n; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+    }
+    *up0_out = j - 1; *upn_out = 2;
+  } else if (evn == SDD_HEAD) {  // ensemble_kernel.cu:492-494
+    const int n = sl.N[1] + 1;
+    __syncwarp();
+    move_down(sl.Q, 1, Z, lane); move_down(sl.N, 1, Z, lane);
+    move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane);
+    if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    *up0_out = 0; *upn_out = 1;
+  } else {  // SDD_TAIL, ensemble_kernel.cu:495-498
+    __syncwarp();
+    if (lane == 0) { sl.N[Z - 2] += 1; sl.Q[Z - 2] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    *up0_out = Z - 3; *upn_out = 1;
   }
   __syncwarp();
 }
 
 // ------------------------------------------------------------------ step kernel
 template <bool FLOW, bool CORR>
-__global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, int n_ens,
-                                              const long long* __restrict__ prefix, long long total,
-                                              unsigned int* work, int slot_cap, int pmax,
-                                              const volatile int* abort_flag, int* status) {
+__global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict__ ens, int n_ens,
+                                                 const long long* __restrict__ prefix, long long total,
+                                                 unsigned int* work, int slot_cap, int pmax,
+                                                 const volatile int* abort_flag, int* status) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -360,10 +509,9 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
     // ---- load chain into the slot
     ChainState st = E.cs[c];
     int Z = st.Z, S = st.S, stall = st.stall;
-    int64_t T = st.T;
+    long long T = st.T;
     uint64_t step = st.step, hash = st.hash;
     float dt_prev = st.dt_prev;
-    int64_t k_next = st.k_next;
     const uint64_t step0 = step;
     const float4* gq = E.QN + (size_t)c * cap;
     const float* gt = E.tau + (size_t)c * cap;
@@ -374,8 +522,16 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
       sl.T[s] = gt[s];
     }
     const float wz1 = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(E.beta_d, (double)st.nk)));
-    Corr0 k0{0, 0, 0, 0.f, 0.f, 0.f};
-    int64_t t_next_sample = 0;
+    if (CORR && lane == 0) {
+      const size_t l0 = (size_t)c * E.corr_levels;
+      const int4 cn = E.corr_cnt[l0];
+      Corr0& k0 = *sl.k0;
+      k0.ins = cn.x; k0.navg = cn.y;
+      k0.nins = ((long long)(unsigned)cn.w) << 32 | (unsigned)cn.z;
+      k0.a0 = E.corr_avg[l0 * 3 + 0]; k0.a1 = E.corr_avg[l0 * 3 + 1]; k0.a2 = E.corr_avg[l0 * 3 + 2];
+      k0.k_next = st.k_next;
+      k0.t_next = st.k_next * E.dt_sample_ticks;
+    }
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
@@ -385,25 +541,19 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
         sl.Csh[j * 3 + 2] = E.corr_shift[l0 * p * 3 + j * 3 + 2];
         sl.Cacc[j] = make_float2(0.f, 0.f);
       }
-      const int4 cn = E.corr_cnt[l0];
-      k0.ins = cn.x; k0.navg = cn.y;
-      k0.nins = ((long long)(unsigned)cn.w) << 32 | (unsigned)cn.z;
-      k0.a0 = E.corr_avg[l0 * 3 + 0]; k0.a1 = E.corr_avg[l0 * 3 + 1]; k0.a2 = E.corr_avg[l0 * 3 + 2];
-      t_next_sample = k_next * E.dt_sample_ticks;
     }
     __syncwarp();
 
-    int pend = 0;  // bit0 NaN, bit1 inf, bit2 scale overflow (from incremental updates)
+    // bit0 NaN, bit1 inf, bit2 scale overflow (pending from incremental updates)
+    int pend = 0;
     const int S_stored = S;
     if (!FLOW) {
-      // equilibrium keeps quantised pair totals in the slot; recompute them
-      // (the overflow rule can only lower the scale; it is kept only if an
-      // event follows, as in the oracle where the rule runs inside a step)
-      const float ev = (lane < 5) ? end_comp(E, lane, Z, sl.N, wz1) : 0.f;
-      int fl;
-      S = full_pairs<false>(E, sl, Z, S, ev, lane, &fl);
-      pend = fl;
+      // equilibrium keeps quantised rates in the slot; the overflow rule can
+      // only lower the scale, and is kept only if an event follows (the oracle
+      // applies it inside a step)
+      S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
     }
+    bool ends_dirty = false;
 
     uint64_t rbase = ~0ull;
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
@@ -425,13 +575,7 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
         __syncwarp();
       }
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
-      if (CORR) {
-        while (k_next < E.nsamples && T > t_next_sample) {
-          corr_sample(E, sl, Z, c, k0, lane);
-          ++k_next;
-          t_next_sample += E.dt_sample_ticks;
-        }
-      }
+      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples(E, sl, Z, c, T, lane);
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207)
       if (stall != 0 || T >= E.t_end_ticks || (int64_t)step >= E.step_limit) {
         dt_prev = 0.0f;
@@ -447,43 +591,41 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
         dt_prev = 0.0f;
         break;
       }
-      // (4) chain-end rates, lanes 0..4
-      const float ev = (lane < 5) ? end_comp(E, lane, Z, sl.N, wz1) : 0.f;
+      const int np = Z - 1;
+      // (4) rates: flow recomputes everything; equilibrium refreshes the chain
+      // ends when a strand next to an end changed
       if (FLOW) {
-        int fl;
-        S = full_pairs<true>(E, sl, Z, S, ev, lane, &fl);
-        pend = fl;
-      } else {
-        const int over = (lane < 5 && fexp(ev) + S > LIMIT_E) ? 4 : 0;
-        pend |= __reduce_or_sync(FULL_MASK, over);
-        if (pend & 4) {
-          int fl;
-          S = full_pairs<false>(E, sl, Z, S, ev, lane, &fl);
-          pend = fl;
+        S = full_rates<true>(E, sl, Z, S, wz1, lane, &pend);
+      } else if (ends_dirty) {
+        int over = 0;
+        if (lane < NEND) {
+          const float ev = end_comp(E, lane, Z, sl.N, wz1);
+          over = (fexp(ev) + S > LIMIT_E) ? 4 : 0;
+          sl.R[np + lane] = quant(ev, pow2f(S));
         }
+        pend |= __reduce_or_sync(FULL_MASK, over);
+        if (pend & 4) S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
+        ends_dirty = false;
+        __syncwarp();
       }
       if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
       if (pend & 2) { stall = ST_INF; dt_prev = 0.0f; break; }
       const float sf = pow2f(S);
-      const unsigned long long qe = (lane < 5) ? quant(ev, sf) : 0ull;
-      // (5) sums: contiguous odd-width chunk per lane + warp scan
-      const int np = Z - 1;
-      const int cw = ((np + 31) >> 5) | 1;
+      // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
+      const int ne = np + NEND;
+      const int cw = ((ne + 31) >> 5) | 1;
       const int j0 = lane * cw;
-      const int j1 = min(j0 + cw, np);
+      const int j1 = min(j0 + cw, ne);
       unsigned long long part = 0;
-      for (int j = j0; j < j1; ++j) part += sl.R[j];
+      for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
       const unsigned long long incl = warp_incl_scan_u64(part, lane);
-      const unsigned long long einc = warp_incl_scan_u64(qe, lane);
-      const unsigned long long pair_total = __shfl_sync(FULL_MASK, incl, 31);
-      const unsigned long long ends_total = __shfl_sync(FULL_MASK, einc, 4);
-      const unsigned long long tot = pair_total + ends_total;
+      const unsigned long long tot = __shfl_sync(FULL_MASK, incl, 31);
       // (6) dt = 1/sum W (ensemble_kernel.cu:262-272)
       const float sumw = __fmul_rn(__ll2float_rn((long long)tot), pow2f(-S));
       const float dt = __fdiv_rn(1.0f, sumw);
       if (dt == 0.0f) { stall = ST_DT_ZERO; dt_prev = 0.0f; break; }
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
-      const int64_t dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
+      const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
       // (7) Philox words of this event (one evaluation per 32 events)
       if ((step & ~31ull) != rbase) {
         rbase = step & ~31ull;
@@ -494,149 +636,65 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
       const int src = (int)(step & 31ull);
       const uint32_t w0 = __shfl_sync(FULL_MASK, r0, src);
       const uint32_t w1 = __shfl_sync(FULL_MASK, r1, src);
-      const uint32_t w2 = __shfl_sync(FULL_MASK, r2, src);
-      const uint32_t w3 = __shfl_sync(FULL_MASK, r3, src);
       // (8) pick (ensemble_kernel.cu:274-501): pr uniform in [0, tot)
-      const unsigned long long u64 = ((unsigned long long)w1 << 32) | w0;
-      const unsigned long long pr = __umul64hi(tot, u64);
+      const unsigned long long pr = __umul64hi(tot, ((unsigned long long)w1 << 32) | w0);
+      const int L = __ffs(__ballot_sync(FULL_MASK, incl > pr)) - 1;
+      int jj = 0;
+      unsigned long long r = 0;
+      if (lane == L) {
+        r = pr - (incl - part);
+        jj = j0;
+        while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
+      }
+      jj = __shfl_sync(FULL_MASK, jj, L);
+      r = __shfl_sync(FULL_MASK, r, L);
       int evn, j = -1;
       unsigned long long rem = 0, wsel = 0;
-      if (pr < pair_total) {
-        const unsigned mask = __ballot_sync(FULL_MASK, incl > pr);
-        const int L = __ffs(mask) - 1;
-        int jj = 0;
-        unsigned long long r = 0;
-        if (lane == L) {
-          r = pr - (incl - part);
-          jj = j0;
-          while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
-        }
-        j = __shfl_sync(FULL_MASK, jj, L);
-        r = __shfl_sync(FULL_MASK, r, L);
-        float o[4];
-        pair_comp(E, sl.N[j], sl.Q[j].w, sl.N[j + 1], sl.Q[j + 1].w, sl.T[j], o);
-        const unsigned long long q0 = quant(o[0], sf), q1 = quant(o[1], sf), q2 = quant(o[2], sf),
-                                 q3 = quant(o[3], sf);
+      if (jj < np) {
+        // inside pair j: CD destruction, shift +1, shift -1, CD creation
+        j = jj;
+        const unsigned long long q0 = E.cd_flag ? quant(sl.T[j], sf) : 0ull;
+        const unsigned long long q3 = E.cd_flag ? quant(__ldg(&E.NE[sl.N[j]]).w, sf) : 0ull;
+        const unsigned long long lim = sl.R[j] - q3;
         if (r < q0) evn = CDD;
-        else if ((r -= q0) < q1) evn = SDP;
-        else if ((r -= q1) < q2) evn = SDM;
-        else { r -= q2; evn = CDC_MID; rem = r; wsel = q3; }
+        else if (r >= lim) { evn = CDC_MID; rem = r - lim; wsel = q3; }
+        else {
+          const int N1 = sl.N[j], N2 = sl.N[j + 1];
+          const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
+          const unsigned long long q1 = quant(shift_plus(E, N1, sl.Q[j].w, N2, sl.Q[j + 1].w, a, b), sf);
+          evn = (r - q0 < q1) ? SDP : SDM;
+        }
       } else {
-        const unsigned long long r = pr - pair_total;
-        const unsigned mask = __ballot_sync(FULL_MASK, lane < 5 && einc > r);
-        const int L = __ffs(mask) - 1;
-        const unsigned long long lo = __shfl_sync(FULL_MASK, einc - qe, L);
-        wsel = __shfl_sync(FULL_MASK, qe, L);
-        rem = r - lo;
-        evn = (L == 0) ? CDC_TAIL : (L == 1) ? SDC_HEAD : (L == 2) ? SDC_TAIL : (L == 3) ? SDD_HEAD : SDD_TAIL;
+        const int q = jj - np;
+        rem = r;
+        wsel = sl.R[jj];
+        evn = (q == 0) ? CDC_TAIL : (q == 1) ? SDC_HEAD : (q == 2) ? SDC_TAIL : (q == 3) ? SDD_HEAD : SDD_TAIL;
       }
       T += dtt;
       // (9) apply
-      const bool create = (evn == CDC_MID || evn == CDC_TAIL || evn == SDC_HEAD || evn == SDC_TAIL);
       uint32_t code = ((uint32_t)evn << 24) | (uint32_t)(j < 0 ? 0 : j);
-      int up0 = 0, upn = 0;  // pairs to recompute [up0, up0+upn)
-      if (create && Z >= cap) {
-        code |= (uint32_t)NULL_FLAG << 24;  // refused at capacity (ensemble_kernel.cu:380,423,451)
-      } else if (create) {
-        int newn = 0;
-        if (evn == CDC_MID || evn == CDC_TAIL) {
-          const int N1 = (evn == CDC_MID) ? sl.N[j] : sl.N[Z - 1];
-          const double x = floor(__dadd_rn(0.5, __ddiv_rn(__dmul_rn(__ull2double_rn(rem), (double)(N1 - 2)),
-                                                        __ull2double_rn(wsel))));
-          newn = (int)x + 1;
-          newn = max(1, min(N1 - 1, newn));
-        }
-        const U4 gr = rng_at(E, P_CREATE, step, (uint32_t)(step >> 32), (uint32_t)c);
-        float g0, g1, g2, g3;
-        m_gauss2(gr.x, gr.y, &g0, &g1);
-        m_gauss2(gr.z, gr.w, &g2, &g3);
-        const PcdDev pp = partner_pcd(E, w3);
-        const float u = u01(w2);
-        const float trate = E.cd_flag ? ((evn == CDC_MID || evn == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
-        if (evn == CDC_MID && j > 0) {
-          const int N1 = sl.N[j];
-          const float4 q1 = sl.Q[j];
-          __syncwarp();
-          move_up(sl.Q, j, Z, lane); move_up(sl.N, j, Z, lane);
-          move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane);
-          if (lane == 0) {
-            const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
-            const float ra = __fdiv_rn((float)newn, (float)N1);
-            const float x = __fmaf_rn(q1.x, ra, __fmul_rn(g0, sg));
-            const float y = __fmaf_rn(q1.y, ra, __fmul_rn(g1, sg));
-            const float z = __fmaf_rn(q1.z, ra, __fmul_rn(g2, sg));
-            sl.N[j] = newn; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
-            const float x2 = __fsub_rn(q1.x, x), y2 = __fsub_rn(q1.y, y), z2 = __fsub_rn(q1.z, z);
-            sl.N[j + 1] = N1 - newn; sl.Q[j + 1] = make_float4(x2, y2, z2, m_q2(x2, y2, z2));
-            sl.T[j] = trate;
-          }
-          up0 = j - 1; upn = 3;
-        } else if ((evn == CDC_MID && j == 0) || evn == SDC_HEAD) {
-          const int N0 = sl.N[0];
-          const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
-          const int nd = (evn == SDC_HEAD) ? 1 : newn;
-          __syncwarp();
-          move_up(sl.Q, 0, Z, lane); move_up(sl.N, 0, Z, lane);
-          move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane);
-          if (lane == 0) {
-            const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
-            const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
-            sl.N[0] = nd; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-            sl.N[1] = nn; sl.Q[1] = make_float4(x, y, z, m_q2(x, y, z));
-            sl.T[0] = trate;
-          }
-          up0 = 0; upn = 2;
-        } else {  // CDC_TAIL, SDC_TAIL
-          const int Nt = sl.N[Z - 1];
-          const int nn = (evn == SDC_TAIL) ? Nt - 1 : newn;
-          const int nd = (evn == SDC_TAIL) ? 1 : Nt - newn;
-          __syncwarp();
-          if (lane == 0) {
-            const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
-            const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
-            sl.N[Z] = nd; sl.Q[Z] = make_float4(0.f, 0.f, 0.f, 0.f);
-            sl.N[Z - 1] = nn; sl.Q[Z - 1] = make_float4(x, y, z, m_q2(x, y, z));
-            sl.T[Z - 1] = trate;
-          }
-          up0 = Z - 2; upn = 2;
-        }
-        Z += 1;
-        code |= (uint32_t)newn << 8;
-      } else if (evn == SDP || evn == SDM) {
+      int up0 = 0, upn = 0;
+      if (evn == SDP || evn == SDM) {
         __syncwarp();
         if (lane == 0) {
           const int d = (evn == SDP) ? 1 : -1;
           sl.N[j] += d; sl.N[j + 1] -= d;
         }
         up0 = j - 1; upn = 3;
-      } else if (evn == CDD) {
-        const int n = sl.N[j] + sl.N[j + 1];
-        const float4 a = sl.Q[j], b = sl.Q[j + 1];
-        const bool endp = (j == Z - 2) || (j == 0);
-        __syncwarp();
-        move_down(sl.Q, j + 2, Z, lane); move_down(sl.N, j + 2, Z, lane);
-        move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane);
-        if (lane == 0) {
-          const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
-          const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
-          const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
-          sl.N[j] = n; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
-        }
+        ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
+      } else if (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) {
+        apply_destroy(sl, evn, j, Z, lane, &up0, &upn);
         Z -= 1;
-        up0 = j - 1; upn = 2;
-      } else if (evn == SDD_HEAD) {
-        const int n = sl.N[1] + 1;
-        __syncwarp();
-        move_down(sl.Q, 1, Z, lane); move_down(sl.N, 1, Z, lane);
-        move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane);
-        if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
-        Z -= 1;
-        up0 = 0; upn = 1;
-      } else {  // SDD_TAIL
-        __syncwarp();
-        if (lane == 0) { sl.N[Z - 2] += 1; sl.Q[Z - 2] = make_float4(0.f, 0.f, 0.f, 0.f); }
-        Z -= 1;
-        up0 = Z - 2; upn = 1;
+        ends_dirty = true;
+      } else if (Z >= cap) {
+        code |= (uint32_t)NULL_FLAG << 24;  // creation refused at capacity (ensemble_kernel.cu:380,423,451)
+      } else {
+        const uint32_t w2 = __shfl_sync(FULL_MASK, r2, src);
+        const uint32_t w3 = __shfl_sync(FULL_MASK, r3, src);
+        const int newn = apply_create(E, sl, evn, j, Z, c, step, rem, wsel, w2, w3, lane, &up0, &upn);
+        Z += 1;
+        ends_dirty = true;
+        code |= (uint32_t)newn << 8;
       }
       __syncwarp();
       if (!FLOW && upn > 0) pend |= update_pairs(E, sl, Z, S, up0, upn, lane);
@@ -670,6 +728,7 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
       }
     }
     // ---- correlator level 0 back to HBM (compensated FP32 sums -> FP64)
+    long long k_next = st.k_next;
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
@@ -680,6 +739,8 @@ __global__ void __launch_bounds__(128) k_step(const EnsDev* __restrict__ ens, in
         const float2 a = sl.Cacc[j];
         E.corr_acc[l0 * p + j] += (double)a.x - (double)a.y;
       }
+      const Corr0& k0 = *sl.k0;
+      k_next = k0.k_next;
       if (lane == 0) {
         E.corr_cnt[l0] = make_int4(k0.ins, k0.navg, (int)(unsigned)(k0.nins & 0xffffffffll),
                                    (int)(unsigned)(k0.nins >> 32));
@@ -805,12 +866,15 @@ __global__ void __launch_bounds__(128) k_init(const EnsDev* __restrict__ ensp, i
   // initial fixed-point scale: min(s0, 47 - max exponent of all rate components)
   int emax = -200;
   for (int p = lane; p < Z - 1; p += 32) {
-    float o[4];
-    pair_comp(E, sN[p], gq2[p], sN[p + 1], gq2[p + 1], gt[p], o);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) emax = max(emax, fexp(o[q]));
+    const int N1 = sN[p], N2 = sN[p + 1];
+    const float q1 = gq2[p], q2 = gq2[p + 1];
+    const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
+    emax = max(emax, fexp(E.cd_flag ? gt[p] : 0.0f));
+    emax = max(emax, fexp(shift_plus(E, N1, q1, N2, q2, a, b)));
+    emax = max(emax, fexp(shift_minus(E, N1, q1, N2, q2, a, b)));
+    emax = max(emax, fexp(E.cd_flag ? __ldg(&E.NE[N1]).w : 0.0f));
   }
-  if (lane < 5) {
+  if (lane < NEND) {
     const float wz1 = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(E.beta_d, (double)nk)));
     emax = max(emax, fexp(end_comp(E, lane, Z, sN, wz1)));
   }
@@ -887,14 +951,21 @@ template <bool FLOW, bool CORR>
 static void* step_fn() { return (void*)k_step<FLOW, CORR>; }
 
 static void* pick_step(bool flow, bool corr) {
-  if (flow) return corr ? step_fn<true, true>() : step_fn<true, false>();
+  if (flow) return step_fn<true, false>();
   return corr ? step_fn<false, true>() : step_fn<false, false>();
+}
+
+static cudaError_t prep_step(void* fn, size_t sm) {
+  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (err != cudaSuccess) return err;
+  // the slots are the working set: ask for the largest shared-memory carveout
+  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg) {
   const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
   void* fn = pick_step(flow, corr);
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (prep_step(fn, sm) != cudaSuccess) return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, cfg.warps_per_block * 32, sm) != cudaSuccess) return 0;
   return nb;
@@ -905,7 +976,7 @@ cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefi
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st) {
   const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
   void* fn = pick_step(flow, corr);
-  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t err = prep_step(fn, sm);
   if (err != cudaSuccess) return err;
   void* args[] = {(void*)&d_ens, (void*)&n_ens, (void*)&d_prefix, (void*)&total, (void*)&d_work,
                   (void*)&cfg.slot_cap, (void*)&cfg.pmax, (void*)&abort_flag, (void*)&d_status};
@@ -922,7 +993,6 @@ cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, 
   return cudaGetLastError();
 }
 
-// launchers that need the device copy of the ensemble
 cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
                                  cudaStream_t st) {
   k_gt_reduce<<<levels * p, 256, 0, st>>>(d_ens, d_gsum, d_count);

@@ -45,15 +45,15 @@ __device__ __forceinline__ float u01(uint32_t w) {
   return __fmul_rn((float)((w >> 8) + 1u), 5.9604644775390625e-08f);
 }
 
+// exp(x); argument clamped to [-87.3365, 88.7228], NaN propagates; 2^k applied
+// as two exact power-of-two factors.
 __device__ __forceinline__ float m_exp(float x) {
-  if (x != x) return x;
-  if (x > 88.7228390f) return __int_as_float(0x7f800000);
-  if (x < -87.3365448f) return 0.0f;
+  const float xc = fminf(fmaxf(x, -87.3365448f), 88.7228390f);
   const float MAGIC = 12582912.0f;
-  const float t = __fmaf_rn(x, 1.44269504088896341f, MAGIC);
+  const float t = __fmaf_rn(xc, 1.44269504088896341f, MAGIC);
   const float kf = __fsub_rn(t, MAGIC);
   const int k = __float_as_int(t) - __float_as_int(MAGIC);
-  float r = __fmaf_rn(kf, -0.693145751953125f, x);
+  float r = __fmaf_rn(kf, -0.693145751953125f, xc);
   r = __fmaf_rn(kf, -1.428606765330187e-06f, r);
   float p = 1.98412698e-4f;
   p = __fmaf_rn(p, r, 1.38888889e-3f);
@@ -63,8 +63,9 @@ __device__ __forceinline__ float m_exp(float x) {
   p = __fmaf_rn(p, r, 0.5f);
   p = __fmaf_rn(p, r, 1.0f);
   p = __fmaf_rn(p, r, 1.0f);
-  if (k > 127) return __fmul_rn(__fmul_rn(p, __int_as_float((k - 1 + 127) << 23)), 2.0f);
-  return __fmul_rn(p, __int_as_float((k + 127) << 23));
+  const int k1 = k >> 1, k2 = k - k1;
+  const float res = __fmul_rn(__fmul_rn(p, __int_as_float((k1 + 127) << 23)), __int_as_float((k2 + 127) << 23));
+  return (x != x) ? x : res;
 }
 
 __device__ __forceinline__ float m_log(float x) {

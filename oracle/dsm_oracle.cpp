@@ -1067,6 +1067,19 @@ void orc_tau_sample(double beta, double nk, int kind, int mode, const float* u, 
   }
 }
 
+// Multi-tau correlator alone on a series of n 3-vectors (unit test of the
+// correlator semantics of eq_ensemble_kernel.cu:133-227).
+int orc_corr_series(int p, int m, int levels, int64_t n, const double* series, double* acc, int64_t* nins) {
+  Ensemble E;
+  E.P.corr_type = 0; E.P.corr_p = p; E.P.corr_m = m; E.P.corr_levels = levels;
+  Chain<double> c;
+  corr_alloc(E, c);
+  for (int64_t t = 0; t < n; ++t) corr_add(E, c, &series[3 * t], 0);
+  for (int q = 0; q < levels * p; ++q) acc[q] = c.cacc[q];
+  for (int k = 0; k < levels; ++k) nins[k] = c.cnins[k];
+  return 0;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

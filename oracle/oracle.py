@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
         L.orc_math.argtypes = [C.c_int, vp, vp, vp, C.c_int]
         L.orc_tau_sample.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, vp, vp, C.c_int]
         L.orc_num_threads.restype = C.c_int
+        L.orc_corr_series.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -210,3 +211,12 @@ def ref_lib() -> Optional[C.CDLL]:
         R.ref_tau_samples.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref = R
     return _ref
+
+
+def corr_series(series: np.ndarray, p: int, m: int, levels: int):
+    """Run the oracle's multi-tau correlator on one series of 3-vectors."""
+    x = np.ascontiguousarray(series, np.float64)
+    acc = np.zeros(levels * p, np.float64)
+    nins = np.zeros(levels, np.int64)
+    lib().orc_corr_series(p, m, levels, len(x), _p(x), _p(acc), _p(nins))
+    return acc.reshape(levels, p), nins

@@ -59,15 +59,16 @@ static inline float u01(uint32_t w) {
 }
 
 // ---------------------------------------------------------------- exp / log
+// exp(x); the argument is clamped to [-87.3365, 88.7228] (results between
+// ~FLT_MIN and ~FLT_MAX), NaN propagates.  Scaling by 2^k uses two exact
+// power-of-two factors 2^(k>>1) * 2^(k-(k>>1)).
 static inline float m_exp(float x) {
-  if (x != x) return x;
-  if (x > 88.7228390f) return INFINITY;
-  if (x < -87.3365448f) return 0.0f;
+  const float xc = std::fmin(std::fmax(x, -87.3365448f), 88.7228390f);
   const float MAGIC = 12582912.0f;  // 1.5 * 2^23
-  const float t = std::fmaf(x, 1.44269504088896341f, MAGIC);
+  const float t = std::fmaf(xc, 1.44269504088896341f, MAGIC);
   const float kf = t - MAGIC;
   const int32_t k = (int32_t)as_u(t) - (int32_t)as_u(MAGIC);
-  float r = std::fmaf(kf, -0.693145751953125f, x);
+  float r = std::fmaf(kf, -0.693145751953125f, xc);
   r = std::fmaf(kf, -1.428606765330187e-06f, r);
   float p = 1.98412698e-4f;
   p = std::fmaf(p, r, 1.38888889e-3f);
@@ -77,8 +78,9 @@ static inline float m_exp(float x) {
   p = std::fmaf(p, r, 0.5f);
   p = std::fmaf(p, r, 1.0f);
   p = std::fmaf(p, r, 1.0f);
-  if (k > 127) return (p * f_as((uint32_t)(k - 1 + 127) << 23)) * 2.0f;
-  return p * f_as((uint32_t)(k + 127) << 23);
+  const int32_t k1 = k >> 1, k2 = k - k1;
+  const float res = (p * f_as((uint32_t)(k1 + 127) << 23)) * f_as((uint32_t)(k2 + 127) << 23);
+  return (x != x) ? x : res;
 }
 
 // natural log for finite x > 0

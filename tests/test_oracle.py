@@ -202,3 +202,24 @@ def test_flow_shear_stress_sign(oracle_mod):
     s1, c = o.stress()
     assert c == 2048
     assert s1[3] < s0[3] - 0.05  # sxy = -3<QxQy/N> becomes negative for kappa_xy > 0
+
+
+@pytest.mark.parametrize("p,m,levels,n", [(16, 2, 6, 1000), (64, 8, 3, 5000)])
+def test_correlator_matches_bruteforce(oracle_mod, p, m, levels, n):
+    """Multi-tau correlator (eq_ensemble_kernel.cu:133-227): level k holds block
+    averages of m^k consecutive samples; lag j of level k (j >= p/m for k > 0)
+    accumulates sum_i y_k(i) . y_k(i-j) over the last p values.  Checked
+    against the O(n^2) definition on a random series."""
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((n, 3)).cumsum(axis=0) * 0.1
+    acc, nins = oracle_mod.corr_series(x, p, m, levels)
+    dmin = p // m
+    for k in range(levels):
+        nb = n // m ** k
+        y = x[: nb * m ** k].reshape(nb, m ** k, 3).mean(axis=1)
+        assert nins[k] == nb
+        for j in range(0 if k == 0 else dmin, p):
+            if j >= nb:
+                continue
+            brute = np.sum(y[j:] * y[: nb - j])
+            assert acc[k, j] == pytest.approx(brute, rel=1e-9, abs=1e-9), (k, j)
