@@ -140,6 +140,52 @@ int dsm_save_file(dsm_sim* sim, const char* path);
 int dsm_load_file(dsm_sim* sim, const char* path);
 
 /* ---------------------------------------------------------------------
+ * Allocation-free time step.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc/cudaFree around a step (a serving loop
+ * or host framework that owns every byte of device memory through its own
+ * allocator or budget, or a loop that cannot take the device-wide
+ * synchronisation those calls imply).  The caller passes device buffers for
+ * the chains; tables, descriptor and counters live in one static device array
+ * of DSM_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  Limits: nk <= DSM_NOALLOC_MAX_NK (larger is rejected with
+ * DSM_ERR_INVALID), z_max <= 4096, monodisperse, no G(t) correlator.  The first
+ * call on a device looks up the array's device address (make it before any
+ * stream capture).  All calls share the array and it keeps the last call's
+ * contents: calls that overlap on the GPU race and must be serialised.
+ * --------------------------------------------------------------------- */
+#define DSM_NOALLOC_SCRATCH_BYTES (160 * 1024)
+#define DSM_NOALLOC_MAX_NK 2048
+
+/* Per-chain scalars in the device layout (64 bytes): strands, stall code,
+ * fixed-point scale of the rates, pending flow dt, time in 2^-32 tau_K ticks,
+ * events done (Philox counter), event-sequence hash, next stress-sample
+ * index, Kuhn steps.  dsm_get_ext / dsm_get_chains report the same values. */
+typedef struct dsm_chain_state {
+  int32_t Z;
+  int32_t stall_flag;
+  int32_t scale;
+  float dt_prev;
+  int64_t time_ticks;
+  uint64_t steps;
+  uint64_t hash;
+  int64_t next_sample;
+  int32_t nk;
+  int32_t pad_[3];
+} dsm_chain_state;
+
+/* Advance n_chains chains held in caller-owned device memory (d_QN: n*z_max
+ * float4 {Qx,Qy,Qz,N}; d_tau: n*z_max rates; d_state: n dsm_chain_state) to
+ * time t_end or step_limit events, on `stream` (a cudaStream_t, NULL = legacy
+ * default stream).  Flow ensembles (kappa != 0) also need d_stress_out
+ * (n*8 floats: xx yy zz xy yz zx Lpp Z of every chain at the end).  Results
+ * are identical to dsm_advance on the same inputs.  If events is non-NULL the
+ * call waits for the kernel and stores the number of kMC events done. */
+int dsm_advance_noalloc(const dsm_params* params, dsm_float4* d_QN, float* d_tau, dsm_chain_state* d_state,
+                        float* d_stress_out, double t_end, int64_t step_limit, void* stream, uint64_t* events);
+/* Message of the last failed dsm_advance_noalloc of the calling thread */
+const char* dsm_noalloc_last_error(void);
+
+/* ---------------------------------------------------------------------
  * Reference driver entry point (common/main_cuda.cu:34), same signature and
  * return convention (0 ok, -1 aborted): reads input.dat from the working
  * directory, writes tau[_id].dat / G[_id].dat, honours -s/-l/-distr.
