@@ -11,8 +11,9 @@ from .api import (  # noqa: F401
     DSMError,
     Ensemble,
     StressPlus,
+    advance_batch,
     lib_path,
     load_library,
 )
 
-__all__ = ["DSMError", "Ensemble", "StressPlus", "lib_path", "load_library"]
+__all__ = ["DSMError", "Ensemble", "StressPlus", "advance_batch", "lib_path", "load_library"]

@@ -99,6 +99,8 @@ def load_library() -> C.CDLL:
     lib.dsm_corr_shape.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
     lib.dsm_last_window.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(u64), C.POINTER(i32), C.POINTER(i32)]
     lib.dsm_last_window.restype = C.c_int
+    lib.dsm_advance_batch.argtypes = [vp, i32, vp, vp, vp]
+    lib.dsm_advance_batch.restype = C.c_int
     lib.dsm_save_file.argtypes = [vp, C.c_char_p]
     lib.dsm_load_file.argtypes = [vp, C.c_char_p]
     for fn in ("dsm_init_equilibrium", "dsm_set_chains", "dsm_get_chains", "dsm_get_ext", "dsm_set_ext",
@@ -267,3 +269,18 @@ class Ensemble:
 
     def load(self, path: str) -> None:
         self._check(self._lib.dsm_load_file(self._h, os.fsencode(path)))
+
+
+def advance_batch(ensembles, t_end, step_limit=None):
+    """Advance several Ensemble objects (same GPU) in one persistent launch per kind.
+    Returns the kMC events of each ensemble."""
+    lib = load_library()
+    n = len(ensembles)
+    hs = (C.c_void_p * n)(*[e._h.value for e in ensembles])
+    te = np.ascontiguousarray(np.broadcast_to(np.asarray(t_end, np.float64), (n,)))
+    sl = None if step_limit is None else np.ascontiguousarray(np.broadcast_to(np.asarray(step_limit, np.int64), (n,)))
+    ev = np.zeros(n, np.uint64)
+    rc = lib.dsm_advance_batch(C.cast(hs, C.c_void_p), n, _ptr(te), _ptr(sl), _ptr(ev))
+    if rc != DSM_OK:
+        raise DSMError(rc, lib.dsm_last_error(ensembles[0]._h).decode())
+    return ev

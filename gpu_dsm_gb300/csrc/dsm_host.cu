@@ -586,3 +586,97 @@ extern "C" int dsm_last_window(const dsm_sim* s, float* kernel_ms, uint64_t* eve
   if (blocks_per_sm) *blocks_per_sm = s->blocks_per_sm;
   return DSM_OK;
 }
+
+// ------------------------------------------------------------------ batched windows
+// Advance several ensembles in one persistent launch per kind (equilibrium /
+// equilibrium+G(t) / flow): the work items of all ensembles of a kind form one
+// index space (prefix sums of chain counts) that the warps pull from, so short
+// and long ensembles share the GPU without a launch per ensemble.  The
+// shared-memory slot is sized for the largest z_max of the kind.
+extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end, const int64_t* step_limit,
+                                 uint64_t* events) {
+  if (!sims || n < 1 || !t_end) return DSM_ERR_INVALID;
+  dsm_sim* s = sims[0];
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  for (int i = 0; i < n; ++i) {
+    if (!sims[i] || !sims[i]->ready) return DSM_ERR_INVALID;
+    if (sims[i]->P.device != s->P.device) return fail(s, DSM_ERR_INVALID, "batch spans devices");
+    if (!(t_end[i] >= 0.0) || t_end[i] * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
+    for (int k = 0; k < i; ++k)
+      if (sims[k] == sims[i]) return fail(s, DSM_ERR_INVALID, "ensemble listed twice in a batch");
+  }
+  CK(cudaSetDevice(s->P.device));
+  struct Group {
+    std::vector<int> idx;
+    bool flow, corr;
+  };
+  std::vector<Group> groups;
+  for (int i = 0; i < n; ++i) {
+    const bool fl = sims[i]->flow, co = sims[i]->corr;
+    Group* g = nullptr;
+    for (auto& x : groups) if (x.flow == fl && x.corr == co) g = &x;
+    if (!g) { groups.push_back(Group{{}, fl, co}); g = &groups.back(); }
+    g->idx.push_back(i);
+  }
+  // windows of every ensemble (same bookkeeping as dsm_advance)
+  for (int i = 0; i < n; ++i) {
+    dsm_sim* q = sims[i];
+    EnsDev& E = q->h;
+    const double te = t_end[i];
+    const int64_t sl = step_limit ? step_limit[i] : -1;
+    E.t_end_ticks = (int64_t)std::llrint(te * TICKS);
+    q->t_window = te;
+    E.step_limit = sl < 0 ? INT64_MAX : sl;
+    const double expect = 0.25 * (double)q->nkmax * std::max(0.0, te - q->t_done) * 100.0;
+    const double wd = std::max(16777216.0, std::min(expect, 9.0e18));
+    E.watchdog_events = q->watchdog_events > 0 ? q->watchdog_events : (int64_t)wd;
+    CK(cudaMemcpyAsync(q->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemsetAsync(q->d_counters, 0, 4 * sizeof(unsigned long long), s->st));
+  }
+  std::vector<void*> tmp;
+  int rc = DSM_OK;
+  for (auto& g : groups) {
+    const int k = (int)g.idx.size();
+    std::vector<EnsDev> hE(k);
+    std::vector<long long> pre(k + 1, 0);
+    LaunchCfg cfg{4, 0, 0};
+    for (int q = 0; q < k; ++q) {
+      dsm_sim* x = sims[g.idx[q]];
+      hE[q] = x->h;
+      pre[q + 1] = pre[q] + x->P.n_chains;
+      cfg.slot_cap = std::max(cfg.slot_cap, x->cap);
+      if (g.corr) cfg.pmax = std::max(cfg.pmax, x->cp);
+    }
+    EnsDev* dE = nullptr;
+    long long* dP = nullptr;
+    unsigned int* dW = nullptr;
+    CK(cudaMallocAsync((void**)&dE, sizeof(EnsDev) * k, s->st));
+    tmp.push_back(dE);
+    CK(cudaMallocAsync((void**)&dP, sizeof(long long) * (k + 1) + 16, s->st));
+    tmp.push_back(dP);
+    dW = (unsigned int*)(dP + k + 1);
+    CK(cudaMemcpyAsync(dE, hE.data(), sizeof(EnsDev) * k, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(dP, pre.data(), sizeof(long long) * (k + 1), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemsetAsync(dW, 0, 16, s->st));
+    const int bps = step_max_blocks_per_sm(g.flow, g.corr, cfg);
+    if (bps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory"); break; }
+    const long long want = (pre[k] + cfg.warps_per_block - 1) / cfg.warps_per_block;
+    const int grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
+    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, cfg, nullptr, (int*)(dW + 1), grid, s->st));
+  }
+  for (int i = 0; i < n && rc == DSM_OK; ++i)
+    if (sims[i]->flow) CK(launch_stress_reduce_dev(sims[i]->d_ens, sims[i]->d_red, s->st));
+  for (void* p : tmp) cudaFreeAsync(p, s->st);
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaGetLastError());
+  if (rc != DSM_OK) return rc;
+  for (int i = 0; i < n; ++i) {
+    unsigned long long cnt[4];
+    CK(cudaMemcpy(cnt, sims[i]->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    if (events) events[i] = cnt[0];
+    sims[i]->events_total += cnt[0];
+    sims[i]->last_events = cnt[0];
+    sims[i]->t_done = std::max(sims[i]->t_done, sims[i]->t_window);
+  }
+  return DSM_OK;
+}

@@ -125,6 +125,7 @@ struct Corr0 {  // correlator level-0 counters of the resident chain
 struct Slot {
   float4* Q;                // {Qx, Qy, Qz, Q^2} per strand
   unsigned long long* R;    // quantised pair totals, then the 5 chain-end rates
+  unsigned long long* P;    // quantised shift +1 component per pair
   int* N;                   // Kuhn steps per strand
   float* T;                 // CD lifetime rates per entanglement
   Corr0* k0;                // correlator level-0 counters
@@ -136,7 +137,7 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 
 __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax) {
   const size_t n = (size_t)slot_cap + 1, nr = (size_t)slot_cap + NEND + 1;
-  size_t b = n * 16 + nr * 8 + n * 4 + n * 4;
+  size_t b = n * 16 + nr * 8 + n * 8 + n * 4 + n * 4;
   b = align_up(b, 16) + sizeof(Corr0);
   b = align_up(b, 8) + (size_t)pmax * 12;
   b = align_up(b, 8) + (size_t)pmax * 8;
@@ -148,9 +149,10 @@ __device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int
   const size_t n = (size_t)slot_cap + 1, nr = (size_t)slot_cap + NEND + 1;
   s.Q = (float4*)base;
   s.R = (unsigned long long*)(base + n * 16);
-  s.N = (int*)(base + n * 16 + nr * 8);
-  s.T = (float*)(base + n * 20 + nr * 8);
-  size_t off = align_up(n * 24 + nr * 8, 16);
+  s.P = (unsigned long long*)(base + n * 16 + nr * 8);
+  s.N = (int*)(base + n * 24 + nr * 8);
+  s.T = (float*)(base + n * 28 + nr * 8);
+  size_t off = align_up(n * 32 + nr * 8, 16);
   s.k0 = (Corr0*)(base + off);
   off = align_up(off + sizeof(Corr0), 8);
   s.Csh = (float*)(base + off);
@@ -213,23 +215,31 @@ __device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const i
 }
 
 // recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 32), one lane each;
-// returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 scale overflow
-__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, int lane) {
+// returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 scale overflow; *delta
+// gets new - old of the lane's pair total (0 for idle lanes)
+__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, int lane,
+                                            unsigned long long* delta) {
   int flags = 0;
   const int p = p0 + lane;
+  unsigned long long d = 0;
   if (lane < cnt && p >= 0 && p < Z - 1) {
     float o[4];
     pair_floats(E, sl, p, o);
     const float sf = pow2f(S);
-    unsigned long long tot = 0;
+    unsigned long long tot = 0, qp = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       flags |= comp_bad(o[q]);
       if (fexp(o[q]) + S > LIMIT_E) flags |= 4;
-      tot += quant(o[q], sf);
+      const unsigned long long v = quant(o[q], sf);
+      tot += v;
+      if (q == 1) qp = v;
     }
+    d = tot - sl.R[p];
     sl.R[p] = tot;
+    sl.P[p] = qp;
   }
+  *delta = d;
   __syncwarp();
   return __reduce_or_sync(FULL_MASK, flags);
 }
@@ -255,6 +265,7 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
       tot += quant(o[q], sf);
     }
     sl.R[p] = tot;
+    sl.P[p] = quant(o[1], sf);
   }
   float ev = 0.0f;
   if (lane < NEND) {
@@ -274,7 +285,9 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
     for (int p = lane; p < np; p += 32) {
       float o[4];
       pair_floats(E, sl, p, o);
-      sl.R[p] = quant(o[0], sf2) + quant(o[1], sf2) + quant(o[2], sf2) + quant(o[3], sf2);
+      const unsigned long long qp = quant(o[1], sf2);
+      sl.R[p] = quant(o[0], sf2) + qp + quant(o[2], sf2) + quant(o[3], sf2);
+      sl.P[p] = qp;
     }
     if (lane < NEND) sl.R[np + lane] = quant(ev, sf2);
   }
@@ -402,7 +415,7 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
     const float4 q1 = sl.Q[j];
     __syncwarp();
     move_up(sl.Q, j, Z, lane); move_up(sl.N, j, Z, lane);
-    move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane);
+    move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane); move_up(sl.P, j, Z - 1, lane);
     if (lane == 0) {
       const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
       const float ra = __fdiv_rn((float)newn, (float)N1);
@@ -421,7 +434,7 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
     const int nd = (evn == SDC_HEAD) ? 1 : newn;
     __syncwarp();
     move_up(sl.Q, 0, Z, lane); move_up(sl.N, 0, Z, lane);
-    move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane);
+    move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane); move_up(sl.P, 0, Z - 1, lane);
     if (lane == 0) {
       const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
       const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
@@ -457,7 +470,7 @@ __device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, int 
     const bool endp = (j == Z - 2) || (j == 0);
     __syncwarp();
     move_down(sl.Q, j + 2, Z, lane); move_down(sl.N, j + 2, Z, lane);
-    move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane);
+    move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane); move_down(sl.P, j + 1, Z - 1, lane);
     if (lane == 0) {
       const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
       const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
@@ -469,7 +482,7 @@ __device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, int 
     const int n = sl.N[1] + 1;
     __syncwarp();
     move_down(sl.Q, 1, Z, lane); move_down(sl.N, 1, Z, lane);
-    move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane);
+    move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane); move_down(sl.P, 1, Z - 1, lane);
     if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
     *up0_out = 0; *upn_out = 1;
   } else {  // SDD_TAIL, ensemble_kernel.cu:495-498
@@ -507,12 +520,16 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     const int cap = E.cap;
 
     // ---- load chain into the slot
-    ChainState st = E.cs[c];
+    const ChainState st = E.cs[c];
     int Z = st.Z, S = st.S, stall = st.stall;
     long long T = st.T;
     uint64_t step = st.step, hash = st.hash;
     float dt_prev = st.dt_prev;
-    const uint64_t step0 = step;
+    const long long k_next0 = st.k_next;
+    // stop at step_lim; if the watchdog cap is the tighter one, stopping there is a stall
+    const bool wd_tighter = (E.watchdog_events < E.step_limit - (long long)step);
+    const long long step_lim = wd_tighter ? (long long)step + E.watchdog_events : E.step_limit;
+    const long long t_end = E.t_end_ticks;
     const float4* gq = E.QN + (size_t)c * cap;
     const float* gt = E.tau + (size_t)c * cap;
     for (int s = lane; s < Z; s += 32) {
@@ -554,8 +571,14 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
     }
     bool ends_dirty = false;
+    // per-lane exclusive/inclusive prefix of the element array and its total;
+    // rebuilt by a chunk sum + warp scan only after structural events, end or
+    // scale changes and in flow; sliding events patch them with the deltas of
+    // the <=3 recomputed pairs
+    bool rescan = true;
+    unsigned long long incl = 0, excl = 0, tot = 0;
+    int cw = 1, j0 = 0;
 
-    uint64_t rbase = ~0ull;
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
     long long done = 0;
 
@@ -577,16 +600,12 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
       if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples(E, sl, Z, c, T, lane);
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207)
-      if (stall != 0 || T >= E.t_end_ticks || (int64_t)step >= E.step_limit) {
+      if (stall != 0 || T >= t_end || (long long)step >= step_lim) {
+        if (stall == 0 && T < t_end && wd_tighter) stall = ST_WATCHDOG;
         dt_prev = 0.0f;
         break;
       }
-      if ((long long)(step - step0) >= E.watchdog_events) {
-        stall = ST_WATCHDOG;
-        dt_prev = 0.0f;
-        break;
-      }
-      if (abort_flag != nullptr && ((step - step0) & 4095u) == 4095u && *abort_flag != 0) {
+      if (abort_flag != nullptr && (done & 4095) == 4095 && *abort_flag != 0) {
         if (lane == 0) atomicOr(status, 1);
         dt_prev = 0.0f;
         break;
@@ -596,6 +615,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // ends when a strand next to an end changed
       if (FLOW) {
         S = full_rates<true>(E, sl, Z, S, wz1, lane, &pend);
+        rescan = true;
       } else if (ends_dirty) {
         int over = 0;
         if (lane < NEND) {
@@ -606,20 +626,28 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         pend |= __reduce_or_sync(FULL_MASK, over);
         if (pend & 4) S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
         ends_dirty = false;
+        rescan = true;
         __syncwarp();
+      } else if (pend & 4) {
+        S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
+        rescan = true;
       }
       if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
       if (pend & 2) { stall = ST_INF; dt_prev = 0.0f; break; }
       const float sf = pow2f(S);
       // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
-      const int ne = np + NEND;
-      const int cw = ((ne + 31) >> 5) | 1;
-      const int j0 = lane * cw;
-      const int j1 = min(j0 + cw, ne);
-      unsigned long long part = 0;
-      for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
-      const unsigned long long incl = warp_incl_scan_u64(part, lane);
-      const unsigned long long tot = __shfl_sync(FULL_MASK, incl, 31);
+      if (rescan) {
+        const int ne = np + NEND;
+        cw = ((ne + 31) >> 5) | 1;
+        j0 = lane * cw;
+        const int j1 = min(j0 + cw, ne);
+        unsigned long long part = 0;
+        for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
+        incl = warp_incl_scan_u64(part, lane);
+        excl = incl - part;
+        tot = __shfl_sync(FULL_MASK, incl, 31);
+        rescan = false;
+      }
       // (6) dt = 1/sum W (ensemble_kernel.cu:262-272)
       const float sumw = __fmul_rn(__ll2float_rn((long long)tot), pow2f(-S));
       const float dt = __fdiv_rn(1.0f, sumw);
@@ -627,9 +655,8 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
       // (7) Philox words of this event (one evaluation per 32 events)
-      if ((step & ~31ull) != rbase) {
-        rbase = step & ~31ull;
-        const uint64_t ctr = rbase + (uint64_t)lane;
+      if ((step & 31ull) == 0 || done == 0) {
+        const uint64_t ctr = (step & ~31ull) + (uint64_t)lane;
         const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
         r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
       }
@@ -642,7 +669,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       int jj = 0;
       unsigned long long r = 0;
       if (lane == L) {
-        r = pr - (incl - part);
+        r = pr - excl;
         jj = j0;
         while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
       }
@@ -658,12 +685,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         const unsigned long long lim = sl.R[j] - q3;
         if (r < q0) evn = CDD;
         else if (r >= lim) { evn = CDC_MID; rem = r - lim; wsel = q3; }
-        else {
-          const int N1 = sl.N[j], N2 = sl.N[j + 1];
-          const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
-          const unsigned long long q1 = quant(shift_plus(E, N1, sl.Q[j].w, N2, sl.Q[j + 1].w, a, b), sf);
-          evn = (r - q0 < q1) ? SDP : SDM;
-        }
+        else evn = (r - q0 < sl.P[j]) ? SDP : SDM;
       } else {
         const int q = jj - np;
         rem = r;
@@ -674,6 +696,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (9) apply
       uint32_t code = ((uint32_t)evn << 24) | (uint32_t)(j < 0 ? 0 : j);
       int up0 = 0, upn = 0;
+      bool slide = false;
       if (evn == SDP || evn == SDM) {
         __syncwarp();
         if (lane == 0) {
@@ -682,6 +705,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         }
         up0 = j - 1; upn = 3;
         ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
+        slide = !ends_dirty;
       } else if (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) {
         apply_destroy(sl, evn, j, Z, lane, &up0, &upn);
         Z -= 1;
@@ -697,7 +721,25 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         code |= (uint32_t)newn << 8;
       }
       __syncwarp();
-      if (!FLOW && upn > 0) pend |= update_pairs(E, sl, Z, S, up0, upn, lane);
+      if (!FLOW && upn > 0) {
+        unsigned long long dl;
+        pend |= update_pairs(E, sl, Z, S, up0, upn, lane, &dl);
+        if (slide) {
+          // patch the prefix sums with the deltas of pairs up0..up0+2
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const unsigned long long d = __shfl_sync(FULL_MASK, dl, k);
+            const int own = (up0 + k) / cw;  // idle or out-of-range pairs carry d == 0
+            if (lane >= own) incl += d;
+            if (lane > own) excl += d;
+            tot += d;
+          }
+        } else {
+          rescan = true;
+        }
+      } else if (upn > 0 || ends_dirty) {
+        rescan = true;
+      }
       hash = (hash ^ (uint64_t)code) * 0x100000001B3ull;
       ++step;
       ++done;
@@ -728,7 +770,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       }
     }
     // ---- correlator level 0 back to HBM (compensated FP32 sums -> FP64)
-    long long k_next = st.k_next;
+    long long k_next = k_next0;
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
@@ -756,9 +798,9 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       wt[s] = (s < Z - 1) ? sl.T[s] : 0.0f;
     }
     if (lane == 0) {
-      st.Z = Z; st.S = (done > 0) ? S : S_stored; st.stall = stall; st.T = T; st.step = step; st.hash = hash;
-      st.dt_prev = dt_prev; st.k_next = k_next;
-      E.cs[c] = st;
+      ChainState* cs = &E.cs[c];
+      cs->Z = Z; cs->S = (done > 0) ? S : S_stored; cs->stall = stall; cs->dt_prev = dt_prev;
+      cs->T = T; cs->step = step; cs->hash = hash; cs->k_next = k_next;
       atomicAdd(&E.counters[0], (unsigned long long)done);
       atomicAdd(&E.counters[1], 1ull);
     }

@@ -114,6 +114,15 @@ int dsm_set_ext(dsm_sim* sim, const int64_t* time_ticks, const uint64_t* steps, 
 int dsm_advance(dsm_sim* sim, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
                 uint64_t* events);
 
+/* Advance n ensembles (same device) to their own t_end[i] / step_limit[i]
+ * (step_limit may be NULL) in one persistent launch per kind (equilibrium,
+ * equilibrium with G(t), flow).  No counterpart in the reference, which runs
+ * one ensemble per process; used for multi-condition runs (several flow
+ * rates) and by the serving loop.  events[i] (may be NULL) receives the kMC
+ * events of ensemble i.  Results equal per-ensemble dsm_advance calls. */
+int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end, const int64_t* step_limit,
+                      uint64_t* events);
+
 /* Ensemble-average stress of the current state over non-stalled chains
  * (flow output).  Replaces calc_stress / calc_stress_call_block
  * (common/ensemble.cu:210-221, common/ensemble_call_block.cu:452-505). */
