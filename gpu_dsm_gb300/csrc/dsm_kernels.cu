@@ -214,34 +214,45 @@ __device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const i
   return (q == 0) ? cdc : ((q <= 2) ? sdc : sdd);
 }
 
-// recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 32), one lane each;
-// returns warp-uniform flags: bit0 NaN, bit1 inf, bit2 scale overflow; *delta
-// gets new - old of the lane's pair total (0 for idle lanes)
+// Recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 16) with two lanes
+// per pair: the even lane evaluates the shift +1 component, the odd lane the
+// shift -1 component.  Returns 4 when a component is NaN, inf or beyond the
+// fixed-point range (the caller then runs the full pass, which decides between a
+// stall and a lower scale, as the oracle does); *delta gets new - old of the
+// pair total on the even lane (0 elsewhere).
 __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, int lane,
                                             unsigned long long* delta) {
-  int flags = 0;
-  const int p = p0 + lane;
+  const int p = p0 + (lane >> 1);
+  const bool act = (lane < 2 * cnt) && p >= 0 && p < Z - 1;
+  float w = 0.0f;
+  int N1 = 1;
+  if (act) {
+    N1 = sl.N[p];
+    const int N2 = sl.N[p + 1];
+    const float q1 = sl.Q[p].w, q2 = sl.Q[p + 1].w;
+    const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
+    w = (lane & 1) ? shift_minus(E, N1, q1, N2, q2, a, b) : shift_plus(E, N1, q1, N2, q2, a, b);
+  }
+  const float wm = __shfl_xor_sync(FULL_MASK, w, 1);
   unsigned long long d = 0;
-  if (lane < cnt && p >= 0 && p < Z - 1) {
-    float o[4];
-    pair_floats(E, sl, p, o);
+  bool bad = false;
+  if (act && !(lane & 1)) {
     const float sf = pow2f(S);
-    unsigned long long tot = 0, qp = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      flags |= comp_bad(o[q]);
-      if (fexp(o[q]) + S > LIMIT_E) flags |= 4;
-      const unsigned long long v = quant(o[q], sf);
-      tot += v;
-      if (q == 1) qp = v;
-    }
+    const float o0 = E.cd_flag ? sl.T[p] : 0.0f;
+    const float o3 = E.cd_flag ? __ldg(&E.NE[N1]).w : 0.0f;
+    const float y0 = __fmul_rn(o0, sf), y1 = __fmul_rn(w, sf), y2 = __fmul_rn(wm, sf), y3 = __fmul_rn(o3, sf);
+    const float lim = 281474976710656.0f;  // 2^(LIMIT_E+1)
+    bad = !(y0 < lim) || !(y1 < lim) || !(y2 < lim) || !(y3 < lim);
+    const unsigned long long v1 = (unsigned long long)__float2ll_rn(y1);
+    const unsigned long long tot = (unsigned long long)__float2ll_rn(y0) + v1 +
+                                   (unsigned long long)__float2ll_rn(y2) + (unsigned long long)__float2ll_rn(y3);
     d = tot - sl.R[p];
     sl.R[p] = tot;
-    sl.P[p] = qp;
+    sl.P[p] = v1;
   }
   *delta = d;
   __syncwarp();
-  return __reduce_or_sync(FULL_MASK, flags);
+  return __any_sync(FULL_MASK, bad) ? 4 : 0;
 }
 
 // Full pass over all pairs and the chain ends: quantise with the current scale,
@@ -725,11 +736,14 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         unsigned long long dl;
         pend |= update_pairs(E, sl, Z, S, up0, upn, lane, &dl);
         if (slide) {
-          // patch the prefix sums with the deltas of pairs up0..up0+2
+          // patch the prefix sums with the deltas of pairs j-1, j, j+1 (even
+          // lanes 0, 2, 4); pair j lies in lane L's chunk, its neighbours in L's
+          // or the adjacent chunk (out-of-range pairs carry d == 0)
+          const int jL = L * cw;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
-            const unsigned long long d = __shfl_sync(FULL_MASK, dl, k);
-            const int own = (up0 + k) / cw;  // idle or out-of-range pairs carry d == 0
+            const unsigned long long d = __shfl_sync(FULL_MASK, dl, 2 * k);
+            const int own = (k == 0) ? ((j == jL) ? L - 1 : L) : (k == 1) ? L : ((j + 1 == jL + cw) ? L + 1 : L);
             if (lane >= own) incl += d;
             if (lane > own) excl += d;
             tot += d;
