@@ -191,7 +191,8 @@ def run_gpu(args):
     torch.cuda.set_device(local)
 
     ens = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT, t_end=T_END_RUN,
-                       seed=1, stream=rank, device=local, corr_p=CORR_P, corr_m=CORR_M)
+                       seed=1, stream=rank, device=local, corr_p=CORR_P, corr_m=CORR_M,
+                       lanes_per_chain=args.lanes)
     ens.init_equilibrium()
     t = 0.0
     for _ in range(args.warmup):
@@ -322,6 +323,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--chains", type=int, default=65536, help="chains per GPU (65536 = headline workload)")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per chain (16 or 32; 0 = library default)")
     args = ap.parse_args()
     global N_CHAINS
     N_CHAINS = args.chains

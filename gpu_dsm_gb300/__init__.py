@@ -10,10 +10,13 @@ simulator raises.
 from .api import (  # noqa: F401
     DSMError,
     Ensemble,
+    Server,
     StressPlus,
     advance_batch,
     lib_path,
     load_library,
+    make_params,
+    pcd,
 )
 
-__all__ = ["DSMError", "Ensemble", "StressPlus", "advance_batch", "lib_path", "load_library"]
+__all__ = ["DSMError", "Ensemble", "Server", "StressPlus", "advance_batch", "lib_path", "load_library", "make_params", "pcd"]

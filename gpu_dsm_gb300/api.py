@@ -48,6 +48,8 @@ class DsmParams(C.Structure):
         ("nk_chain", C.c_void_p),
         ("warps_per_block", C.c_int32),
         ("s0", C.c_int32),
+        ("lanes_per_chain", C.c_int32),
+        ("pad_", C.c_int32),
     ]
 
 
@@ -60,6 +62,11 @@ class StressPlus(C.Structure):
 
     def as_array(self) -> np.ndarray:
         return np.array([getattr(self, n) for n, _ in self._fields_], dtype=np.float64)
+
+
+class ServeTotals(C.Structure):
+    _fields_ = [("events", C.c_uint64), ("busy_s", C.c_double), ("ticks", C.c_uint64), ("completed", C.c_uint64),
+                ("peak_bytes", C.c_uint64), ("peak_active", C.c_int32), ("pad_", C.c_int32)]
 
 
 HEAD_DTYPE = np.dtype([("Z", np.int32), ("time", np.float32), ("dummy", np.float32), ("stall_flag", np.int32)])
@@ -103,9 +110,22 @@ def load_library() -> C.CDLL:
     lib.dsm_advance_batch.restype = C.c_int
     lib.dsm_save_file.argtypes = [vp, C.c_char_p]
     lib.dsm_load_file.argtypes = [vp, C.c_char_p]
+    lib.dsm_pcd.argtypes = [C.c_double, i32, vp]
+    lib.dsm_pcd.restype = C.c_int
+    lib.dsm_serve_open.argtypes = [i32, u64, i32, C.c_double, C.POINTER(vp)]
+    lib.dsm_serve_submit.argtypes = [vp, C.POINTER(DsmParams), C.POINTER(u64)]
+    lib.dsm_serve_status.argtypes = [vp, u64, C.POINTER(i32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(u64)]
+    lib.dsm_serve_wait_all.argtypes = [vp, C.c_double]
+    lib.dsm_serve_result_gt.argtypes = [vp, u64, vp, vp, C.POINTER(i32)]
+    lib.dsm_serve_result_stress.argtypes = [vp, u64, vp, vp, C.POINTER(i32)]
+    lib.dsm_serve_stats.argtypes = [vp, C.POINTER(ServeTotals)]
+    lib.dsm_serve_close.argtypes = [vp]
+    lib.dsm_serve_close.restype = None
     for fn in ("dsm_init_equilibrium", "dsm_set_chains", "dsm_get_chains", "dsm_get_ext", "dsm_set_ext",
                "dsm_advance", "dsm_stress", "dsm_gt", "dsm_gt_raw", "dsm_corr_shape", "dsm_save_file",
-               "dsm_load_file"):
+               "dsm_load_file", "dsm_serve_open", "dsm_serve_submit", "dsm_serve_status", "dsm_serve_wait_all",
+               "dsm_serve_result_gt", "dsm_serve_result_stress", "dsm_serve_stats"):
         getattr(lib, fn).restype = C.c_int
     _LIB = lib
     return lib
@@ -113,6 +133,45 @@ def load_library() -> C.CDLL:
 
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def pcd(beta: float, nk: int) -> dict:
+    """p_cd(beta, N_K) constants (common/pcd_tau.h:26-66): alpha, tau_0, tau_max, tau_d, g, normdt."""
+    out = np.zeros(6, np.float64)
+    rc = load_library().dsm_pcd(beta, nk, _ptr(out))
+    if rc != DSM_OK:
+        raise DSMError(rc, "dsm_pcd")
+    return dict(zip(("alpha", "tau_0", "tau_max", "tau_d", "g", "normdt"), out.tolist()))
+
+
+def make_params(*, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[float] = (0.0,) * 9,
+                cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
+                device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
+                stream: int = 0, warps_per_block: int = 0, s0: int = 0, lanes_per_chain: int = 0) -> DsmParams:
+    """dsm_params of a monodisperse ensemble (input.dat fields, common/main_cuda.cu:55-68)."""
+    p = DsmParams()
+    p.beta = beta
+    p.nk = nk
+    p.n_chains = n_chains
+    for i, k in enumerate(kappa):
+        p.kappa[i] = k
+    p.cd_flag = cd_flag
+    p.pd_flag = 0
+    p.eq_type = eq_type
+    p.sync_dt = sync_dt
+    p.t_end = t_end
+    p.seed = seed
+    p.device = device
+    p.z_max = z_max
+    p.corr_p = corr_p
+    p.corr_m = corr_m
+    p.corr_levels = corr_levels
+    p.stream = stream
+    p.nk_chain = None
+    p.warps_per_block = warps_per_block
+    p.s0 = s0
+    p.lanes_per_chain = lanes_per_chain
+    return p
 
 
 class Ensemble:
@@ -127,30 +186,15 @@ class Ensemble:
     def __init__(self, *, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[float] = (0.0,) * 9,
                  cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
                  device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
-                 stream: int = 0, nk_chain: Optional[np.ndarray] = None, warps_per_block: int = 0, s0: int = 0):
+                 stream: int = 0, nk_chain: Optional[np.ndarray] = None, warps_per_block: int = 0, s0: int = 0,
+                 lanes_per_chain: int = 0):
         self._lib = load_library()
-        p = DsmParams()
-        p.beta = beta
-        p.nk = nk
-        p.n_chains = n_chains
-        for i, k in enumerate(kappa):
-            p.kappa[i] = k
-        p.cd_flag = cd_flag
-        p.pd_flag = 0
-        p.eq_type = eq_type
-        p.sync_dt = sync_dt
-        p.t_end = t_end
-        p.seed = seed
-        p.device = device
-        p.z_max = z_max
-        p.corr_p = corr_p
-        p.corr_m = corr_m
-        p.corr_levels = corr_levels
-        p.stream = stream
         self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
+        p = make_params(beta=beta, nk=nk, n_chains=n_chains, kappa=kappa, cd_flag=cd_flag, eq_type=eq_type,
+                        sync_dt=sync_dt, t_end=t_end, seed=seed, device=device, z_max=z_max, corr_p=corr_p,
+                        corr_m=corr_m, corr_levels=corr_levels, stream=stream, warps_per_block=warps_per_block,
+                        s0=s0, lanes_per_chain=lanes_per_chain)
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
-        p.warps_per_block = warps_per_block
-        p.s0 = s0
         self.params = p
         self.n_chains = n_chains
         self.z_max = z_max if z_max > 0 else nk
@@ -284,3 +328,91 @@ def advance_batch(ensembles, t_end, step_limit=None):
     if rc != DSM_OK:
         raise DSMError(rc, lib.dsm_last_error(ensembles[0]._h).decode())
     return ev
+
+
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class Server:
+    """Continuous-batching serving loop on one GPU (dsm_serve_* of the C ABI).
+
+    Requests (keyword arguments of ``make_params``) are admitted while their
+    ensembles fit in ``hbm_budget`` bytes of device memory, stay resident and
+    are advanced together, one batched launch per kind and size class per
+    tick of about ``tick_s`` seconds.  ``max_active=1, tick_s=-1`` is the plain
+    form: one request at a time, each in as few launches as its outputs allow.
+    """
+
+    def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, tick_s: float = 0.0):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, tick_s, C.byref(h))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_open")
+        self._h = h
+        self.device = device
+
+    def submit(self, **kw) -> int:
+        kw.setdefault("device", self.device)
+        p = make_params(**kw)
+        rid = C.c_uint64()
+        rc = self._lib.dsm_serve_submit(self._h, C.byref(p), C.byref(rid))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_submit")
+        return rid.value
+
+    def status(self, rid: int) -> dict:
+        st, lat, q, ev = C.c_int32(), C.c_double(), C.c_double(), C.c_uint64()
+        rc = self._lib.dsm_serve_status(self._h, rid, C.byref(st), C.byref(lat), C.byref(q), C.byref(ev))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_status")
+        return {"state": st.value, "latency_s": lat.value, "queue_s": q.value, "events": ev.value}
+
+    def wait_all(self, timeout_s: float = 3600.0) -> None:
+        rc = self._lib.dsm_serve_wait_all(self._h, timeout_s)
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_wait_all")
+
+    def result_gt(self, rid: int):
+        n = C.c_int32(0)
+        self._lib.dsm_serve_result_gt(self._h, rid, None, None, C.byref(n))
+        t = np.zeros(max(n.value, 1), np.float32)
+        g = np.zeros(max(n.value, 1), np.float32)
+        rc = self._lib.dsm_serve_result_gt(self._h, rid, _ptr(t), _ptr(g), C.byref(n))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_result_gt")
+        return t[:n.value], g[:n.value]
+
+    def result_stress(self, rid: int):
+        n = C.c_int32(0)
+        self._lib.dsm_serve_result_stress(self._h, rid, None, None, C.byref(n))
+        t = np.zeros(max(n.value, 1), np.float64)
+        s = (StressPlus * max(n.value, 1))()
+        rc = self._lib.dsm_serve_result_stress(self._h, rid, _ptr(t), C.cast(s, C.c_void_p), C.byref(n))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_result_stress")
+        return t[:n.value], np.array([s[i].as_array() for i in range(n.value)], np.float32).reshape(n.value, -1)
+
+    def stats(self) -> dict:
+        t = ServeTotals()
+        rc = self._lib.dsm_serve_stats(self._h, C.byref(t))
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_stats")
+        return {n: getattr(t, n) for n, _ in ServeTotals._fields_ if n != "pad_"}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dsm_serve_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

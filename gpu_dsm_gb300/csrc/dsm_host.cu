@@ -61,6 +61,13 @@ HostPcd dsm::make_pcd(double Be, double Nk) {
   return p;
 }
 
+extern "C" int dsm_pcd(double beta, int32_t nk, double* out) {
+  if (!out || !(beta > 0.0) || nk < 1) return DSM_ERR_INVALID;
+  const HostPcd p = make_pcd(beta, (double)nk);
+  out[0] = p.alpha; out[1] = p.tau_0; out[2] = p.tau_max; out[3] = p.tau_d; out[4] = p.g; out[5] = p.normdt;
+  return DSM_OK;
+}
+
 // Per-N factors of the sliding rates (ensemble_kernel.cu:153-178,219-260)
 // in double, rounded to float.  x^0.75 = sqrt(x)*sqrt(sqrt(x)).
 static double pow075(double x) { return std::sqrt(x) * std::sqrt(std::sqrt(x)); }
@@ -254,13 +261,17 @@ int dsm::sim_setup(dsm_sim* s) {
   s->cfg.pmax = s->corr ? s->cp : 0;
   s->cfg.warps_per_block = P.warps_per_block > 0 ? P.warps_per_block : 4;
   if (s->cfg.warps_per_block > 4) s->cfg.warps_per_block = 4;  // __launch_bounds__(128)
-  const size_t smem = step_slot_bytes(s->cfg.slot_cap, s->cfg.pmax) * s->cfg.warps_per_block;
+  if (P.lanes_per_chain != 0 && P.lanes_per_chain != 16 && P.lanes_per_chain != 32)
+    return fail(s, DSM_ERR_INVALID, "lanes_per_chain must be 16 or 32");
+  s->cfg.lanes = P.lanes_per_chain > 0 ? P.lanes_per_chain : 32;
+  const size_t smem = step_block_smem(s->cfg);
   if (smem > (size_t)prop.sharedMemPerBlockOptin)
     return fail(s, DSM_ERR_INVALID, "chain capacity z_max=" + std::to_string(s->cap) + " does not fit one shared-memory slot");
   const int bps = step_max_blocks_per_sm(s->flow, s->corr, s->cfg);
   if (bps < 1) return fail(s, DSM_ERR_CUDA, "step kernel cannot be resident (occupancy 0)");
   s->blocks_per_sm = bps;
-  const long long want = ((long long)P.n_chains + s->cfg.warps_per_block - 1) / s->cfg.warps_per_block;
+  const int tiles = s->cfg.warps_per_block * 32 / s->cfg.lanes;
+  const long long want = ((long long)P.n_chains + tiles - 1) / tiles;
   s->grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
   s->ready = true;
   return DSM_OK;
@@ -606,16 +617,23 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
       if (sims[k] == sims[i]) return fail(s, DSM_ERR_INVALID, "ensemble listed twice in a batch");
   }
   CK(cudaSetDevice(s->P.device));
+  // one launch per kind and shared-memory size class (slot capacity rounded
+  // up to a power of two, correlator p, lanes per chain): ensembles of very
+  // different chain lengths then do not share the largest one's slot size
   struct Group {
     std::vector<int> idx;
     bool flow, corr;
+    int cap_class, cp, lanes;
   };
+  auto cap_class = [](int cap) { int c = 16; while (c < cap) c <<= 1; return c; };
   std::vector<Group> groups;
   for (int i = 0; i < n; ++i) {
     const bool fl = sims[i]->flow, co = sims[i]->corr;
+    const int cc = cap_class(sims[i]->cap), cp = co ? sims[i]->cp : 0, ln = sims[i]->cfg.lanes;
     Group* g = nullptr;
-    for (auto& x : groups) if (x.flow == fl && x.corr == co) g = &x;
-    if (!g) { groups.push_back(Group{{}, fl, co}); g = &groups.back(); }
+    for (auto& x : groups)
+      if (x.flow == fl && x.corr == co && x.cap_class == cc && x.cp == cp && x.lanes == ln) g = &x;
+    if (!g) { groups.push_back(Group{{}, fl, co, cc, cp, ln}); g = &groups.back(); }
     g->idx.push_back(i);
   }
   // windows of every ensemble (same bookkeeping as dsm_advance)
@@ -635,11 +653,21 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
   }
   std::vector<void*> tmp;
   int rc = DSM_OK;
+  // groups run concurrently, each on the stream of its first ensemble, after
+  // the descriptor copies on s->st; s->st then waits for all of them
+  cudaEvent_t ready = nullptr;
+  std::vector<cudaEvent_t> joins;
+  const bool fan = groups.size() > 1;
+  if (fan) {
+    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(ready, s->st));
+  }
   for (auto& g : groups) {
     const int k = (int)g.idx.size();
     std::vector<EnsDev> hE(k);
     std::vector<long long> pre(k + 1, 0);
-    LaunchCfg cfg{4, 0, 0};
+    LaunchCfg cfg{4, 0, 0, g.lanes};
+    cudaStream_t gs = fan ? sims[g.idx[0]]->st : s->st;
     for (int q = 0; q < k; ++q) {
       dsm_sim* x = sims[g.idx[q]];
       hE[q] = x->h;
@@ -660,10 +688,26 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     CK(cudaMemsetAsync(dW, 0, 16, s->st));
     const int bps = step_max_blocks_per_sm(g.flow, g.corr, cfg);
     if (bps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory"); break; }
-    const long long want = (pre[k] + cfg.warps_per_block - 1) / cfg.warps_per_block;
+    const int tiles = cfg.warps_per_block * 32 / cfg.lanes;
+    const long long want = (pre[k] + tiles - 1) / tiles;
     const int grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
-    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, cfg, nullptr, (int*)(dW + 1), grid, s->st));
+    if (fan) {
+      CK(cudaEventRecord(ready, s->st));
+      CK(cudaStreamWaitEvent(gs, ready, 0));
+    }
+    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, cfg, nullptr, (int*)(dW + 1), grid, gs));
+    if (fan) {
+      cudaEvent_t j = nullptr;
+      CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+      joins.push_back(j);
+      CK(cudaEventRecord(j, gs));
+    }
   }
+  for (cudaEvent_t j : joins) {
+    CK(cudaStreamWaitEvent(s->st, j, 0));
+    cudaEventDestroy(j);
+  }
+  if (ready) cudaEventDestroy(ready);
   for (int i = 0; i < n && rc == DSM_OK; ++i)
     if (sims[i]->flow) CK(launch_stress_reduce_dev(sims[i]->d_ens, sims[i]->d_red, s->st));
   for (void* p : tmp) cudaFreeAsync(p, s->st);

@@ -41,7 +41,7 @@ struct dsm_sim {
   unsigned long long events_total = 0, last_events = 0;
   float last_kernel_ms = 0.f;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  dsm::LaunchCfg cfg{4, 0, 0};
+  dsm::LaunchCfg cfg{4, 0, 0, 32};
   dsm::EnsDev h{};
   cudaStream_t st = nullptr;
   // device buffers

@@ -84,6 +84,7 @@ struct LaunchCfg {
   int warps_per_block;
   int slot_cap;        // strands per SMEM slot (max cap of the ensembles launched)
   int pmax;            // correlator points per level (max over ensembles)
+  int lanes = 32;      // lanes per chain: 32 (one chain per warp) or 16 (two per warp)
 };
 
 __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax);
@@ -94,6 +95,7 @@ cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefi
                         unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st);
 int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg);
+size_t step_block_smem(const LaunchCfg& cfg);
 cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
                                  cudaStream_t st);
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st);

@@ -39,6 +39,57 @@ namespace dsm {
 #define DSM_MINB 4
 #endif
 
+// ------------------------------------------------------------------ tiles
+// A chain is simulated by a tile of W lanes (W = 32: one chain per warp; W = 16:
+// two chains per warp).  All collectives of a chain run inside its tile.
+template <int W>
+struct Tile {
+  unsigned mask;  // lanes of this tile within the warp
+  int base;       // first warp lane of the tile
+  int lane;       // lane within the tile
+  __device__ __forceinline__ Tile() {
+    const int l = threadIdx.x & 31;
+    base = l & ~(W - 1);
+    lane = l & (W - 1);
+    mask = (W == 32) ? 0xffffffffu : (((1u << W) - 1u) << base);
+  }
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  template <class T>
+  __device__ __forceinline__ T shfl(T v, int src) const { return __shfl_sync(mask, v, src, W); }
+  template <class T>
+  __device__ __forceinline__ T shfl_up(T v, int d) const { return __shfl_up_sync(mask, v, d, W); }
+  template <class T>
+  __device__ __forceinline__ T shfl_xor(T v, int d) const { return __shfl_xor_sync(mask, v, d, W); }
+  // predicate bits of the tile's lanes, bit i = lane i of the tile
+  __device__ __forceinline__ unsigned ballot(bool p) const { return (__ballot_sync(mask, p) & mask) >> base; }
+  __device__ __forceinline__ bool any(bool p) const { return (__ballot_sync(mask, p) & mask) != 0u; }
+  __device__ __forceinline__ int or_(int v) const {
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v |= shfl_xor(v, o);
+    return v;
+  }
+  __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v = __fadd_rn(v, shfl_xor(v, o));
+    return v;
+  }
+  __device__ __forceinline__ int maxi(int v) const {
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v = max(v, shfl_xor(v, o));
+    return v;
+  }
+};
+
+template <int W>
+__device__ __forceinline__ unsigned long long tile_scan(const Tile<W>& t, unsigned long long v) {
+#pragma unroll
+  for (int o = 1; o < W; o <<= 1) {
+    const unsigned long long u = t.shfl_up(v, o);
+    if (t.lane >= o) v += u;
+  }
+  return v;
+}
+
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ unsigned long long warp_incl_scan_u64(unsigned long long v, int lane) {
 #pragma unroll
@@ -162,28 +213,28 @@ __device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int
 }
 
 // warp-cooperative moves inside the slot
-template <class T>
-__device__ __forceinline__ void move_up(T* a, int lo, int hi, int lane) {  // [lo,hi) -> [lo+1,hi+1)
-  for (int top = hi - 1; top >= lo; top -= 32) {
-    const int s = top - lane;
+template <class T, int W>
+__device__ __forceinline__ void move_up(T* a, int lo, int hi, const Tile<W>& t) {  // [lo,hi) -> [lo+1,hi+1)
+  for (int top = hi - 1; top >= lo; top -= W) {
+    const int s = top - t.lane;
     T v;
     const bool act = s >= lo;
     if (act) v = a[s];
-    __syncwarp();
+    t.sync();
     if (act) a[s + 1] = v;
-    __syncwarp();
+    t.sync();
   }
 }
-template <class T>
-__device__ __forceinline__ void move_down(T* a, int lo, int hi, int lane) {  // [lo,hi) -> [lo-1,hi-1)
-  for (int bot = lo; bot < hi; bot += 32) {
-    const int s = bot + lane;
+template <class T, int W>
+__device__ __forceinline__ void move_down(T* a, int lo, int hi, const Tile<W>& t) {  // [lo,hi) -> [lo-1,hi-1)
+  for (int bot = lo; bot < hi; bot += W) {
+    const int s = bot + t.lane;
     T v;
     const bool act = s < hi;
     if (act) v = a[s];
-    __syncwarp();
+    t.sync();
     if (act) a[s - 1] = v;
-    __syncwarp();
+    t.sync();
   }
 }
 
@@ -220,8 +271,10 @@ __device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const i
 // fixed-point range (the caller then runs the full pass, which decides between a
 // stall and a lower scale, as the oracle does); *delta gets new - old of the
 // pair total on the even lane (0 elsewhere).
-__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, int lane,
+template <int W>
+__device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, const Tile<W>& t,
                                             unsigned long long* delta) {
+  const int lane = t.lane;
   const int p = p0 + (lane >> 1);
   const bool act = (lane < 2 * cnt) && p >= 0 && p < Z - 1;
   float w = 0.0f;
@@ -233,7 +286,7 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
     const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
     w = (lane & 1) ? shift_minus(E, N1, q1, N2, q2, a, b) : shift_plus(E, N1, q1, N2, q2, a, b);
   }
-  const float wm = __shfl_xor_sync(FULL_MASK, w, 1);
+  const float wm = t.shfl_xor(w, 1);
   unsigned long long d = 0;
   bool bad = false;
   if (act && !(lane & 1)) {
@@ -251,20 +304,22 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
     sl.P[p] = v1;
   }
   *delta = d;
-  __syncwarp();
-  return __any_sync(FULL_MASK, bad) ? 4 : 0;
+  t.sync();
+  return t.any(bad) ? 4 : 0;
 }
 
 // Full pass over all pairs and the chain ends: quantise with the current scale,
 // track the max exponent; apply the scale rule shared with the oracle (lower on
 // overflow; flow raises again once 2^16 of headroom is free) and requantise if S
 // changes.  Returns the new S; *flags_out gets NaN/inf bits (S kept then).
-template <bool FLOW>
-__device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, int lane, int* flags_out) {
+template <bool FLOW, int W>
+__device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, const Tile<W> t,
+                                       int* flags_out) {
+  const int lane = t.lane;
   const int np = Z - 1;
   int emax = -200, flags = 0;
   const float sf = pow2f(S);
-  for (int p = lane; p < np; p += 32) {
+  for (int p = lane; p < np; p += W) {
     float o[4];
     pair_floats(E, sl, p, o);
     unsigned long long tot = 0;
@@ -284,8 +339,8 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
     emax = max(emax, fexp(ev));
     sl.R[np + lane] = quant(ev, sf);
   }
-  emax = warp_max_i(emax);
-  flags = __reduce_or_sync(FULL_MASK, flags);
+  emax = t.maxi(emax);
+  flags = t.or_(flags);
   int Snew = S;
   if (flags == 0) {
     if (emax + S > LIMIT_E) Snew = LIMIT_E - emax;
@@ -293,7 +348,7 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
   }
   if (Snew != S) {
     const float sf2 = pow2f(Snew);
-    for (int p = lane; p < np; p += 32) {
+    for (int p = lane; p < np; p += W) {
       float o[4];
       pair_floats(E, sl, p, o);
       const unsigned long long qp = quant(o[1], sf2);
@@ -302,7 +357,7 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
     }
     if (lane < NEND) sl.R[np + lane] = quant(ev, sf2);
   }
-  __syncwarp();
+  t.sync();
   *flags_out = flags;
   return Snew;
 }
@@ -310,7 +365,9 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
 // ------------------------------------------------------------------ correlator
 // Levels >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
 // push the block average w into level 1 and cascade while blocks complete.
-__device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, int lane) {
+template <int W>
+__device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, const Tile<W> t) {
+  const int lane = t.lane;
   const int L = E.corr_levels, p = E.corr_p, m = E.corr_m, dmin = p / m;
   for (int k = 1; k < L; ++k) {
     const size_t lk = (size_t)c * L + k;
@@ -322,10 +379,10 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
     const int ins = cnt.x;
     const long long nins = (((long long)(unsigned)cnt.w) << 32 | (unsigned)cnt.z) + 1;
     const float a0 = __fadd_rn(av[0], w0), a1 = __fadd_rn(av[1], w1), a2 = __fadd_rn(av[2], w2);
-    __syncwarp();
+    t.sync();
     if (lane == 0) { sh[ins * 3 + 0] = w0; sh[ins * 3 + 1] = w1; sh[ins * 3 + 2] = w2; }
-    __syncwarp();
-    for (int j = dmin + lane; j < p; j += 32) {
+    t.sync();
+    for (int j = dmin + lane; j < p; j += W) {
       if ((long long)j >= nins) break;
       int i2 = ins - j;
       if (i2 < 0) i2 += p;
@@ -334,14 +391,14 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
     }
     const int navg = cnt.y + 1;
     const bool up = (navg == m);
-    __syncwarp();
+    t.sync();
     if (lane == 0) {
       if (up) { av[0] = 0.f; av[1] = 0.f; av[2] = 0.f; }
       else { av[0] = a0; av[1] = a1; av[2] = a2; }
       *cntp = make_int4(ins + 1 == p ? 0 : ins + 1, up ? 0 : navg, (int)(unsigned)(nins & 0xffffffffll),
                         (int)(unsigned)(nins >> 32));
     }
-    __syncwarp();
+    t.sync();
     if (!up) break;
     const float rm = (float)m;
     w0 = __fdiv_rn(a0, rm); w1 = __fdiv_rn(a1, rm); w2 = __fdiv_rn(a2, rm);
@@ -350,25 +407,27 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
 
 // Take every stress sample due at chain time T (eq_ensemble_kernel.cu:281-331):
 // shear stresses (xy, yz, xz) of the current state into correlator level 0.
-__device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int c, long long T, int lane) {
+template <int W>
+__device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int c, long long T, const Tile<W> t) {
+  const int lane = t.lane;
   Corr0& k0 = *sl.k0;
   const int p = E.corr_p, m = E.corr_m;
   while (k0.k_next < E.nsamples && T > k0.t_next) {
     float sxy = 0.f, syz = 0.f, sxz = 0.f;
-    for (int s = lane; s < Z; s += 32) {
+    for (int s = lane; s < Z; s += W) {
       const float4 q = sl.Q[s];
       const float w = __ldg(&E.INV3N[sl.N[s]]);
       sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
       syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
       sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
     }
-    sxy = warp_sum_f(sxy); syz = warp_sum_f(syz); sxz = warp_sum_f(sxz);
+    sxy = t.sum(sxy); syz = t.sum(syz); sxz = t.sum(sxz);
     const int ins = k0.ins;
     const long long n0 = k0.nins + 1;
-    __syncwarp();
+    t.sync();
     if (lane == 0) { sl.Csh[ins * 3 + 0] = sxy; sl.Csh[ins * 3 + 1] = syz; sl.Csh[ins * 3 + 2] = sxz; }
-    __syncwarp();
-    for (int j = lane; j < p; j += 32) {
+    t.sync();
+    for (int j = lane; j < p; j += W) {
       if ((long long)j >= n0) break;
       int i2 = ins - j;
       if (i2 < 0) i2 += p;
@@ -383,7 +442,7 @@ __device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int 
     }
     const float a0 = __fadd_rn(k0.a0, sxy), a1 = __fadd_rn(k0.a1, syz), a2 = __fadd_rn(k0.a2, sxz);
     const int navg = k0.navg + 1;
-    __syncwarp();
+    t.sync();
     if (lane == 0) {
       k0.ins = (ins + 1 == p) ? 0 : ins + 1;
       k0.nins = n0;
@@ -392,10 +451,10 @@ __device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int 
       k0.k_next += 1;
       k0.t_next += E.dt_sample_ticks;
     }
-    __syncwarp();
+    t.sync();
     if (navg == m && E.corr_levels > 1) {
       const float rm = (float)m;
-      corr_push_levels(E, c, __fdiv_rn(a0, rm), __fdiv_rn(a1, rm), __fdiv_rn(a2, rm), lane);
+      corr_push_levels(E, c, __fdiv_rn(a0, rm), __fdiv_rn(a1, rm), __fdiv_rn(a2, rm), t);
     }
   }
 }
@@ -403,9 +462,11 @@ __device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int 
 // ------------------------------------------------------------------ creation events
 // Apply a creation (CD inside strand j / CD at the tail / SD at head or tail):
 // returns newn and the pairs to recompute (up0, upn).
+template <int W>
 __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int j, int Z, int c, uint64_t step,
                                          unsigned long long rem, unsigned long long wsel, uint32_t w2, uint32_t w3,
-                                         int lane, int* up0_out, int* upn_out) {
+                                         const Tile<W> t, int* up0_out, int* upn_out) {
+  const int lane = t.lane;
   int newn = 0;
   if (evn == CDC_MID || evn == CDC_TAIL) {
     const int N1 = (evn == CDC_MID) ? sl.N[j] : sl.N[Z - 1];
@@ -424,9 +485,9 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
   if (evn == CDC_MID && j > 0) {
     const int N1 = sl.N[j];
     const float4 q1 = sl.Q[j];
-    __syncwarp();
-    move_up(sl.Q, j, Z, lane); move_up(sl.N, j, Z, lane);
-    move_up(sl.T, j, Z - 1, lane); move_up(sl.R, j, Z - 1, lane); move_up(sl.P, j, Z - 1, lane);
+    t.sync();
+    move_up(sl.Q, j, Z, t); move_up(sl.N, j, Z, t);
+    move_up(sl.T, j, Z - 1, t); move_up(sl.R, j, Z - 1, t); move_up(sl.P, j, Z - 1, t);
     if (lane == 0) {
       const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
       const float ra = __fdiv_rn((float)newn, (float)N1);
@@ -443,9 +504,9 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
     const int N0 = sl.N[0];
     const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
     const int nd = (evn == SDC_HEAD) ? 1 : newn;
-    __syncwarp();
-    move_up(sl.Q, 0, Z, lane); move_up(sl.N, 0, Z, lane);
-    move_up(sl.T, 0, Z - 1, lane); move_up(sl.R, 0, Z - 1, lane); move_up(sl.P, 0, Z - 1, lane);
+    t.sync();
+    move_up(sl.Q, 0, Z, t); move_up(sl.N, 0, Z, t);
+    move_up(sl.T, 0, Z - 1, t); move_up(sl.R, 0, Z - 1, t); move_up(sl.P, 0, Z - 1, t);
     if (lane == 0) {
       const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
       const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
@@ -458,7 +519,7 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
     const int Nt = sl.N[Z - 1];
     const int nn = (evn == SDC_TAIL) ? Nt - 1 : newn;
     const int nd = (evn == SDC_TAIL) ? 1 : Nt - newn;
-    __syncwarp();
+    t.sync();
     if (lane == 0) {
       const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
       const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
@@ -468,20 +529,22 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
     }
     *up0_out = Z - 2; *upn_out = 2;
   }
-  __syncwarp();
+  t.sync();
   return newn;
 }
 
 // Apply a destruction (CD of pair j, SD at head or tail): sets the pairs to
 // recompute (up0, upn).
-__device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, int lane, int* up0_out, int* upn_out) {
+template <int W>
+__device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, const Tile<W> t, int* up0_out, int* upn_out) {
+  const int lane = t.lane;
   if (evn == CDD) {  // ensemble_kernel.cu:312-323
     const int n = sl.N[j] + sl.N[j + 1];
     const float4 a = sl.Q[j], b = sl.Q[j + 1];
     const bool endp = (j == Z - 2) || (j == 0);
-    __syncwarp();
-    move_down(sl.Q, j + 2, Z, lane); move_down(sl.N, j + 2, Z, lane);
-    move_down(sl.T, j + 1, Z - 1, lane); move_down(sl.R, j + 1, Z - 1, lane); move_down(sl.P, j + 1, Z - 1, lane);
+    t.sync();
+    move_down(sl.Q, j + 2, Z, t); move_down(sl.N, j + 2, Z, t);
+    move_down(sl.T, j + 1, Z - 1, t); move_down(sl.R, j + 1, Z - 1, t); move_down(sl.P, j + 1, Z - 1, t);
     if (lane == 0) {
       const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
       const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
@@ -491,34 +554,35 @@ __device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, int 
     *up0_out = j - 1; *upn_out = 2;
   } else if (evn == SDD_HEAD) {  // ensemble_kernel.cu:492-494
     const int n = sl.N[1] + 1;
-    __syncwarp();
-    move_down(sl.Q, 1, Z, lane); move_down(sl.N, 1, Z, lane);
-    move_down(sl.T, 1, Z - 1, lane); move_down(sl.R, 1, Z - 1, lane); move_down(sl.P, 1, Z - 1, lane);
+    t.sync();
+    move_down(sl.Q, 1, Z, t); move_down(sl.N, 1, Z, t);
+    move_down(sl.T, 1, Z - 1, t); move_down(sl.R, 1, Z - 1, t); move_down(sl.P, 1, Z - 1, t);
     if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
     *up0_out = 0; *upn_out = 1;
   } else {  // SDD_TAIL, ensemble_kernel.cu:495-498
-    __syncwarp();
+    t.sync();
     if (lane == 0) { sl.N[Z - 2] += 1; sl.Q[Z - 2] = make_float4(0.f, 0.f, 0.f, 0.f); }
     *up0_out = Z - 3; *upn_out = 1;
   }
-  __syncwarp();
+  t.sync();
 }
 
 // ------------------------------------------------------------------ step kernel
-template <bool FLOW, bool CORR>
+template <bool FLOW, bool CORR, int W>
 __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict__ ens, int n_ens,
                                                  const long long* __restrict__ prefix, long long total,
                                                  unsigned int* work, int slot_cap, int pmax,
                                                  const volatile int* abort_flag, int* status) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  Slot sl = make_slot(smem + (size_t)wib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
+  const Tile<W> t;
+  const int lane = t.lane;
+  const int tib = threadIdx.x / W;
+  Slot sl = make_slot(smem + (size_t)tib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
 
   for (;;) {
     unsigned int item = 0;
     if (lane == 0) item = atomicAdd(work, 1u);
-    item = __shfl_sync(FULL_MASK, item, 0);
+    item = t.shfl(item, 0);
     if ((long long)item >= total) break;
     if (abort_flag != nullptr && *abort_flag != 0) {
       if (lane == 0) atomicOr(status, 1);
@@ -543,7 +607,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     const long long t_end = E.t_end_ticks;
     const float4* gq = E.QN + (size_t)c * cap;
     const float* gt = E.tau + (size_t)c * cap;
-    for (int s = lane; s < Z; s += 32) {
+    for (int s = lane; s < Z; s += W) {
       const float4 q = gq[s];
       sl.Q[s] = make_float4(q.x, q.y, q.z, m_q2(q.x, q.y, q.z));
       sl.N[s] = (int)q.w;
@@ -563,14 +627,14 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
-      for (int j = lane; j < p; j += 32) {
+      for (int j = lane; j < p; j += W) {
         sl.Csh[j * 3 + 0] = E.corr_shift[l0 * p * 3 + j * 3 + 0];
         sl.Csh[j * 3 + 1] = E.corr_shift[l0 * p * 3 + j * 3 + 1];
         sl.Csh[j * 3 + 2] = E.corr_shift[l0 * p * 3 + j * 3 + 2];
         sl.Cacc[j] = make_float2(0.f, 0.f);
       }
     }
-    __syncwarp();
+    t.sync();
 
     // bit0 NaN, bit1 inf, bit2 scale overflow (pending from incremental updates)
     int pend = 0;
@@ -579,7 +643,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // equilibrium keeps quantised rates in the slot; the overflow rule can
       // only lower the scale, and is kept only if an event follows (the oracle
       // applies it inside a step)
-      S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
+      S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
     }
     bool ends_dirty = false;
     // per-lane exclusive/inclusive prefix of the element array and its total;
@@ -599,17 +663,17 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         float a[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) a[q] = __fmul_rn(dt_prev, E.kap[q]);
-        for (int s = lane; s < Z; s += 32) {
+        for (int s = lane; s < Z; s += W) {
           const float4 q = sl.Q[s];
           const float nx = __fmaf_rn(a[2], q.z, __fmaf_rn(a[1], q.y, __fmaf_rn(a[0], q.x, q.x)));
           const float ny = __fmaf_rn(a[5], q.z, __fmaf_rn(a[4], q.y, __fmaf_rn(a[3], q.x, q.y)));
           const float nz = __fmaf_rn(a[8], q.z, __fmaf_rn(a[7], q.y, __fmaf_rn(a[6], q.x, q.z)));
           sl.Q[s] = make_float4(nx, ny, nz, m_q2(nx, ny, nz));
         }
-        __syncwarp();
+        t.sync();
       }
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
-      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples(E, sl, Z, c, T, lane);
+      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W>(E, sl, Z, c, T, t);
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207)
       if (stall != 0 || T >= t_end || (long long)step >= step_lim) {
         if (stall == 0 && T < t_end && wd_tighter) stall = ST_WATCHDOG;
@@ -625,7 +689,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (4) rates: flow recomputes everything; equilibrium refreshes the chain
       // ends when a strand next to an end changed
       if (FLOW) {
-        S = full_rates<true>(E, sl, Z, S, wz1, lane, &pend);
+        S = full_rates<true, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
       } else if (ends_dirty) {
         int over = 0;
@@ -634,13 +698,13 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
           over = (fexp(ev) + S > LIMIT_E) ? 4 : 0;
           sl.R[np + lane] = quant(ev, pow2f(S));
         }
-        pend |= __reduce_or_sync(FULL_MASK, over);
-        if (pend & 4) S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
+        pend |= t.or_(over);
+        if (pend & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
         ends_dirty = false;
         rescan = true;
-        __syncwarp();
+        t.sync();
       } else if (pend & 4) {
-        S = full_rates<false>(E, sl, Z, S, wz1, lane, &pend);
+        S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
       }
       if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
@@ -649,14 +713,14 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
       if (rescan) {
         const int ne = np + NEND;
-        cw = ((ne + 31) >> 5) | 1;
+        cw = ((ne + W - 1) / W) | 1;
         j0 = lane * cw;
         const int j1 = min(j0 + cw, ne);
         unsigned long long part = 0;
         for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
-        incl = warp_incl_scan_u64(part, lane);
+        incl = tile_scan(t, part);
         excl = incl - part;
-        tot = __shfl_sync(FULL_MASK, incl, 31);
+        tot = t.shfl(incl, W - 1);
         rescan = false;
       }
       // (6) dt = 1/sum W (ensemble_kernel.cu:262-272)
@@ -666,17 +730,17 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
       // (7) Philox words of this event (one evaluation per 32 events)
-      if ((step & 31ull) == 0 || done == 0) {
-        const uint64_t ctr = (step & ~31ull) + (uint64_t)lane;
+      if ((step & (uint64_t)(W - 1)) == 0 || done == 0) {
+        const uint64_t ctr = (step & ~(uint64_t)(W - 1)) + (uint64_t)lane;
         const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
         r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
       }
-      const int src = (int)(step & 31ull);
-      const uint32_t w0 = __shfl_sync(FULL_MASK, r0, src);
-      const uint32_t w1 = __shfl_sync(FULL_MASK, r1, src);
+      const int src = (int)(step & (uint64_t)(W - 1));
+      const uint32_t w0 = t.shfl(r0, src);
+      const uint32_t w1 = t.shfl(r1, src);
       // (8) pick (ensemble_kernel.cu:274-501): pr uniform in [0, tot)
       const unsigned long long pr = __umul64hi(tot, ((unsigned long long)w1 << 32) | w0);
-      const int L = __ffs(__ballot_sync(FULL_MASK, incl > pr)) - 1;
+      const int L = __ffs(t.ballot(incl > pr)) - 1;
       int jj = 0;
       unsigned long long r = 0;
       if (lane == L) {
@@ -684,8 +748,8 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         jj = j0;
         while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
       }
-      jj = __shfl_sync(FULL_MASK, jj, L);
-      r = __shfl_sync(FULL_MASK, r, L);
+      jj = t.shfl(jj, L);
+      r = t.shfl(r, L);
       int evn, j = -1;
       unsigned long long rem = 0, wsel = 0;
       if (jj < np) {
@@ -709,7 +773,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       int up0 = 0, upn = 0;
       bool slide = false;
       if (evn == SDP || evn == SDM) {
-        __syncwarp();
+        t.sync();
         if (lane == 0) {
           const int d = (evn == SDP) ? 1 : -1;
           sl.N[j] += d; sl.N[j + 1] -= d;
@@ -718,23 +782,23 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
         slide = !ends_dirty;
       } else if (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) {
-        apply_destroy(sl, evn, j, Z, lane, &up0, &upn);
+        apply_destroy<W>(sl, evn, j, Z, t, &up0, &upn);
         Z -= 1;
         ends_dirty = true;
       } else if (Z >= cap) {
         code |= (uint32_t)NULL_FLAG << 24;  // creation refused at capacity (ensemble_kernel.cu:380,423,451)
       } else {
-        const uint32_t w2 = __shfl_sync(FULL_MASK, r2, src);
-        const uint32_t w3 = __shfl_sync(FULL_MASK, r3, src);
-        const int newn = apply_create(E, sl, evn, j, Z, c, step, rem, wsel, w2, w3, lane, &up0, &upn);
+        const uint32_t w2 = t.shfl(r2, src);
+        const uint32_t w3 = t.shfl(r3, src);
+        const int newn = apply_create<W>(E, sl, evn, j, Z, c, step, rem, wsel, w2, w3, t, &up0, &upn);
         Z += 1;
         ends_dirty = true;
         code |= (uint32_t)newn << 8;
       }
-      __syncwarp();
+      t.sync();
       if (!FLOW && upn > 0) {
         unsigned long long dl;
-        pend |= update_pairs(E, sl, Z, S, up0, upn, lane, &dl);
+        pend |= update_pairs<W>(E, sl, Z, S, up0, upn, t, &dl);
         if (slide) {
           // patch the prefix sums with the deltas of pairs j-1, j, j+1 (even
           // lanes 0, 2, 4); pair j lies in lane L's chunk, its neighbours in L's
@@ -742,7 +806,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
           const int jL = L * cw;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
-            const unsigned long long d = __shfl_sync(FULL_MASK, dl, 2 * k);
+            const unsigned long long d = t.shfl(dl, 2 * k);
             const int own = (k == 0) ? ((j == jL) ? L - 1 : L) : (k == 1) ? L : ((j + 1 == jL + cw) ? L + 1 : L);
             if (lane >= own) incl += d;
             if (lane > own) excl += d;
@@ -763,7 +827,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     // ---- flow: stress at the end of the window (ensemble_kernel.cu:504-538)
     if (FLOW) {
       float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      for (int i = lane; i < Z; i += 32) {
+      for (int i = lane; i < Z; i += W) {
         const float4 q = sl.Q[i];
         const float w = __ldg(&E.INV3N[sl.N[i]]);
         s[0] = __fmaf_rn(-__fmul_rn(q.x, q.x), w, s[0]);
@@ -775,7 +839,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         s[6] = __fadd_rn(s[6], __fsqrt_rn(q.w));
       }
 #pragma unroll
-      for (int q = 0; q < 7; ++q) s[q] = warp_sum_f(s[q]);
+      for (int q = 0; q < 7; ++q) s[q] = t.sum(s[q]);
       if (lane == 0) {
         float* o = E.out_stress + (size_t)c * 8;
 #pragma unroll
@@ -788,7 +852,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
-      for (int j = lane; j < p; j += 32) {
+      for (int j = lane; j < p; j += W) {
         E.corr_shift[l0 * p * 3 + j * 3 + 0] = sl.Csh[j * 3 + 0];
         E.corr_shift[l0 * p * 3 + j * 3 + 1] = sl.Csh[j * 3 + 1];
         E.corr_shift[l0 * p * 3 + j * 3 + 2] = sl.Csh[j * 3 + 2];
@@ -806,7 +870,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     // ---- chain back to HBM
     float4* wq = E.QN + (size_t)c * cap;
     float* wt = E.tau + (size_t)c * cap;
-    for (int s = lane; s < Z; s += 32) {
+    for (int s = lane; s < Z; s += W) {
       const float4 q = sl.Q[s];
       wq[s] = make_float4(q.x, q.y, q.z, (float)sl.N[s]);
       wt[s] = (s < Z - 1) ? sl.T[s] : 0.0f;
@@ -818,7 +882,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       atomicAdd(&E.counters[0], (unsigned long long)done);
       atomicAdd(&E.counters[1], 1ull);
     }
-    __syncwarp();
+    t.sync();
   }
 }
 
@@ -1003,12 +1067,22 @@ __global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
 }
 
 // ------------------------------------------------------------------ launchers
-template <bool FLOW, bool CORR>
-static void* step_fn() { return (void*)k_step<FLOW, CORR>; }
+template <bool FLOW, bool CORR, int W>
+static void* step_fn() { return (void*)k_step<FLOW, CORR, W>; }
 
-static void* pick_step(bool flow, bool corr) {
-  if (flow) return step_fn<true, false>();
-  return corr ? step_fn<false, true>() : step_fn<false, false>();
+template <int W>
+static void* pick_step_w(bool flow, bool corr) {
+  if (flow) return step_fn<true, false, W>();
+  return corr ? step_fn<false, true, W>() : step_fn<false, false, W>();
+}
+static void* pick_step(bool flow, bool corr, int lanes) {
+  return lanes == 16 ? pick_step_w<16>(flow, corr) : pick_step_w<32>(flow, corr);
+}
+
+static int tile_lanes(const LaunchCfg& cfg) { return cfg.lanes == 16 ? 16 : 32; }
+static size_t step_smem(const LaunchCfg& cfg) {
+  const int tiles = cfg.warps_per_block * 32 / tile_lanes(cfg);
+  return step_slot_bytes(cfg.slot_cap, cfg.pmax) * tiles;
 }
 
 static cudaError_t prep_step(void* fn, size_t sm) {
@@ -1019,19 +1093,21 @@ static cudaError_t prep_step(void* fn, size_t sm) {
 }
 
 int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg) {
-  const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
-  void* fn = pick_step(flow, corr);
+  const size_t sm = step_smem(cfg);
+  void* fn = pick_step(flow, corr, tile_lanes(cfg));
   if (prep_step(fn, sm) != cudaSuccess) return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, cfg.warps_per_block * 32, sm) != cudaSuccess) return 0;
   return nb;
 }
 
+size_t step_block_smem(const LaunchCfg& cfg) { return step_smem(cfg); }
+
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
                         unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st) {
-  const size_t sm = step_slot_bytes(cfg.slot_cap, cfg.pmax) * cfg.warps_per_block;
-  void* fn = pick_step(flow, corr);
+  const size_t sm = step_smem(cfg);
+  void* fn = pick_step(flow, corr, tile_lanes(cfg));
   cudaError_t err = prep_step(fn, sm);
   if (err != cudaSuccess) return err;
   void* args[] = {(void*)&d_ens, (void*)&n_ens, (void*)&d_prefix, (void*)&total, (void*)&d_work,

@@ -72,6 +72,8 @@ typedef struct dsm_params {
   const int32_t* nk_chain; /* per-chain N_K (polydisperse melt) or NULL */
   int32_t warps_per_block; /* step-kernel block size in warps; 0 = autotuned */
   int32_t s0;              /* initial fixed-point scale exponent; 0 = 40 */
+  int32_t lanes_per_chain; /* 32: one chain per warp, 16: two chains per warp; 0 = auto */
+  int32_t pad_;
 } dsm_params;
 
 typedef struct dsm_sim dsm_sim;
@@ -140,6 +142,12 @@ int dsm_gt_raw(dsm_sim* sim, double* gsum, int64_t* count);
 int dsm_last_window(const dsm_sim* sim, float* kernel_ms, uint64_t* events, int32_t* grid,
                     int32_t* blocks_per_sm);
 
+/* Constraint-dynamics lifetime law p_cd(beta, N_K) of common/pcd_tau.h:26-66:
+ * out[0..5] = alpha, tau_0, tau_max, tau_d, g, normdt (tau_K units).  tau_d is
+ * the disentanglement time the GUI uses to turn a Weissenberg number into a
+ * shear rate, kappa_xy = Wi / tau_d (GUI/mainwindow.cpp:836). */
+int dsm_pcd(double beta, int32_t nk, double* out);
+
 /* Correlator geometry of a simulation: levels, p, m */
 int dsm_corr_shape(const dsm_sim* sim, int32_t* levels, int32_t* p, int32_t* m);
 
@@ -193,6 +201,51 @@ int dsm_advance_noalloc(const dsm_params* params, dsm_float4* d_QN, float* d_tau
                         float* d_stress_out, double t_end, int64_t step_limit, void* stream, uint64_t* events);
 /* Message of the last failed dsm_advance_noalloc of the calling thread */
 const char* dsm_noalloc_last_error(void);
+
+/* ---------------------------------------------------------------------
+ * Serving loop (no counterpart in the reference, which runs one ensemble per
+ * process through main_cuda).  A server owns a thread that admits submitted
+ * requests (each a dsm_params, monodisperse) while their device memory fits
+ * in hbm_budget_bytes (0: 15/16 of the free memory), keeps their ensembles
+ * resident and advances every admitted one per tick in batched launches
+ * (dsm_advance_batch).  Equilibrium requests with eq_type=1 produce G(t);
+ * flow requests (kappa != 0) produce the stress at t = k*sync_dt up to t_end
+ * (the tau.dat series).  max_active > 0 caps the ensembles resident at once
+ * (1 = plain one-at-a-time serving).  tick_s: target duration of one tick in
+ * seconds (0: 0.05); each tick shares the measured event rate equally among
+ * the admitted requests (processor sharing, capped by each request's remaining
+ * work and by what its chains can do serially in one tick).  tick_s < 0: every
+ * request advances to t_end (flow: to its next output time) in one launch.
+ * --------------------------------------------------------------------- */
+typedef struct dsm_server dsm_server;
+enum { DSM_REQ_QUEUED = 0, DSM_REQ_ACTIVE = 1, DSM_REQ_DONE = 2, DSM_REQ_FAILED = 3 };
+
+int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double tick_s,
+                   dsm_server** out);
+/* Queue a request; *id identifies it.  DSM_ERR_MEMORY if it can never fit. */
+int dsm_serve_submit(dsm_server* srv, const dsm_params* params, uint64_t* id);
+/* State, latency (arrival to completion, s; -1 while unfinished), queueing
+ * delay (arrival to admission, s; -1 while queued), kMC events so far. */
+int dsm_serve_status(dsm_server* srv, uint64_t id, int32_t* state, double* latency_s, double* queue_s,
+                     uint64_t* events);
+/* Wait until every submitted request finished; DSM_ERR_WATCHDOG on timeout. */
+int dsm_serve_wait_all(dsm_server* srv, double timeout_s);
+/* Results of a finished request (n: in = capacity, out = points) */
+int dsm_serve_result_gt(dsm_server* srv, uint64_t id, float* t, float* G, int32_t* n);
+int dsm_serve_result_stress(dsm_server* srv, uint64_t id, double* t, dsm_stress_plus* out, int32_t* n);
+/* Totals since dsm_serve_open */
+typedef struct dsm_serve_totals {
+  uint64_t events;       /* kMC events of all requests */
+  double busy_s;         /* seconds inside batched advances */
+  uint64_t ticks;        /* batched advances */
+  uint64_t completed;    /* requests finished (done or failed) */
+  uint64_t peak_bytes;   /* most device memory admitted at once */
+  int32_t peak_active;   /* most ensembles resident at once */
+  int32_t pad_;
+} dsm_serve_totals;
+int dsm_serve_stats(dsm_server* srv, dsm_serve_totals* out);
+/* Stop the server thread and release every resident ensemble */
+void dsm_serve_close(dsm_server* srv);
 
 /* ---------------------------------------------------------------------
  * Reference driver entry point (common/main_cuda.cu:34), same signature and

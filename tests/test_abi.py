@@ -49,3 +49,16 @@ def test_invalid_arguments(dsm_mod):
 
 def test_cli_built(dsm_mod):
     assert (ROOT / "gpu_dsm_gb300" / "gpu_DSM").exists()
+
+
+def test_pcd_export_matches_reference(dsm_mod):
+    """dsm_pcd (host code, no GPU) reproduces the reference's compiled p_cd fits."""
+    import json
+
+    d = json.loads((ROOT / "tests" / "golden" / "pcd_reference.json").read_text())
+    for r in d["rows"]:
+        ours = dsm_mod.pcd(r["beta"], r["nk"])
+        for k in ("alpha", "tau_0", "tau_max", "tau_d", "g", "normdt"):
+            assert ours[k] == pytest.approx(r[k], rel=1e-5, abs=1e-12), (r["beta"], r["nk"], k)
+    with pytest.raises(dsm_mod.DSMError):
+        dsm_mod.pcd(0.0, 10)

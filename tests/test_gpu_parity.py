@@ -128,3 +128,33 @@ def test_set_get_roundtrip(dsm_mod, oracle_mod, tmp_path):
     o.run(40.0)
     assert_bitexact(gpu_state(g2), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash", "S"),
                     what="loaded")
+
+
+@pytest.mark.parametrize("nk,n,kappa,z_max", [(25, 1024, (0.0,) * 9, 0), (200, 256, (0.0,) * 9, 0),
+                                              (50, 256, (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 0),
+                                              (30, 256, (0.0,) * 9, 14)])
+def test_two_chains_per_warp_bitexact(dsm_mod, oracle_mod, nk, n, kappa, z_max):
+    """16 lanes per chain (two chains per warp) reproduce the oracle exactly."""
+    g, o = pair(dsm_mod, oracle_mod, nk=nk, n=n, seed=13, kappa=kappa, z_max=z_max, lanes=16)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    for t in (15.0, 40.0):
+        g.advance(t)
+        o.run(t)
+    assert_bitexact(gpu_state(g), o.get_state(), what=f"lanes=16 nk={nk}")
+
+
+def test_two_chains_per_warp_correlator(dsm_mod, oracle_mod):
+    g, o = pair(dsm_mod, oracle_mod, nk=25, n=512, seed=1, corr=True, sync_dt=1.0, t_end=300.0,
+                corr_p=16, corr_m=2, lanes=16)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(120.0)
+    g.advance(300.0)
+    o.run(300.0)
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash"), what="corr lanes=16")
+    gs, gc = g.gt_raw()
+    os_, oc = o.gt_raw()
+    assert np.array_equal(gc, oc)
+    mask = oc > 0
+    assert (np.abs(gs[mask] - os_[mask]) / np.abs(os_[mask]).max()).max() < 1e-5
