@@ -213,6 +213,8 @@ def run_gpu(args):
     wall = time.perf_counter() - t0
     clocks = clk.stop()
     lw = ens.last_window()
+    sched = ens.schedule()
+    launches_per_step = max(1, len(sched))  # size classes + overflow launch, or one launch
     heads, qn, tau = ens.get_chains()
     zmean = float(heads["Z"].mean())
     if world > 1:
@@ -292,6 +294,19 @@ def run_gpu(args):
 
     if rank != 0:
         return 0
+    serve = shear = None
+    if world == 1:
+        ens.close()
+    if not args.no_shear and world == 1:
+        try:
+            shear = run_shear(args, local)
+        except Exception as e:  # reported, never silently replaced
+            shear = {"failed": repr(e)}
+    if not args.no_serve and world == 1:
+        try:
+            serve = run_serve(args, local)
+        except Exception as e:  # reported, never silently replaced
+            serve = {"failed": repr(e)}
     cpu = None
     if not args.no_cpu:
         try:
@@ -302,14 +317,142 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": kms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic equilibrium melt",
             "config": config(args.window, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clocks, "gpu_launches": args.steps,
+            "clocks": clocks, "gpu_launches": args.steps * launches_per_step, "shear": shear, "serve": serve,
             "detail": {"events": events_all, "wall_s": wall, "kernel_ms_total": kms, "mean_Z": zmean,
-                       "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"]}}
+                       "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"], "schedule": sched}}
     print(json.dumps(line))
     ens.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------- shear start-up
+def run_shear(args, device: int = 0) -> dict:
+    """Steady shear start-up: four ensembles of 32768 chains, N_K=100, beta=1,
+    kappa_xy = Wi / tau_d for Wi in {0.1, 1, 10, 100}, advanced together by
+    dsm_advance_batch (one persistent launch) with a stress output per window
+    of t_end/1000 = 500 tau_K (t_end = 5e5).  A bounded sample: the first
+    --shear-windows output windows after equilibrium start."""
+    import gpu_dsm_gb300 as dsm
+
+    nk, n, t_end = 100, 32768, 5.0e5
+    dt_out = t_end / 1000.0
+    tau_d = dsm.pcd(1.0, nk)["tau_d"]
+    ens = [dsm.Ensemble(nk=nk, n_chains=n, beta=1.0, kappa=(0.0, wi / tau_d, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),
+                        sync_dt=dt_out, t_end=t_end, seed=4, stream=k, device=device)
+           for k, wi in enumerate((0.1, 1.0, 10.0, 100.0))]
+    for e in ens:
+        e.init_equilibrium()
+    ev_tot, secs, series = 0, 0.0, []
+    t = 0.0
+    for w in range(args.shear_windows):
+        t += dt_out
+        t0 = time.perf_counter()
+        ev = dsm.advance_batch(ens, t)
+        secs += time.perf_counter() - t0
+        ev_tot += int(np.sum(ev))
+        series.append([float(e.stress()[0][3]) for e in ens])
+    for e in ens:
+        e.close()
+    return {"workload": "4 x 32768 chains, N_K=100, beta=1, shear Wi {0.1,1,10,100}, kappa_xy=Wi/tau_d, "
+                        f"tau_d={tau_d:.4g}, output every {dt_out:g} tau_K",
+            "windows": args.shear_windows, "events": ev_tot, "events_per_s": ev_tot / secs, "wall_s": secs,
+            "sigma_xy_per_window": series,
+            "timing": "host wall clock around dsm_advance_batch (launch + window + stress readback)"}
+
+
+# ---------------------------------------------------------------- serving
+def serve_stream(n: int, seed: int, t_scale: float):
+    """Rheology request stream: N_K log-uniform [20, 500], beta in {0.5, 1, 2},
+    1024-65536 chains log-uniform, half equilibrium G(t) (sample every tau_K,
+    p=16, m=2), half steady shear at Wi log-uniform [0.1, 100]
+    (kappa_xy = Wi / tau_d(beta, N_K)) with 100 stress outputs; t_end
+    log-uniform [1e4, 1e6] tau_K times t_scale."""
+    import gpu_dsm_gb300 as dsm
+
+    rng = np.random.default_rng(seed)
+    lu = lambda a, b: float(np.exp(rng.uniform(math.log(a), math.log(b))))
+    reqs = []
+    for i in range(n):
+        nk = int(round(lu(20, 500)))
+        beta = float(rng.choice([0.5, 1.0, 2.0]))
+        n_cha = int(round(lu(1024, 65536)))
+        shear = bool(rng.integers(0, 2))
+        wi = lu(0.1, 100.0)
+        t_end = lu(1.0e4, 1.0e6) * t_scale
+        r = dict(nk=nk, beta=beta, n_chains=n_cha, t_end=t_end, seed=seed * 1000 + i, stream=i)
+        if shear:
+            kxy = wi / dsm.pcd(beta, nk)["tau_d"]
+            r.update(kappa=(0.0, kxy, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), sync_dt=t_end / 100.0)
+        else:
+            r.update(eq_type=1, sync_dt=1.0, corr_p=16, corr_m=2)
+        reqs.append(r)
+    return reqs
+
+
+def prior_events(r) -> float:
+    return (0.2 * r["nk"] + 2.0) * r["n_chains"] * r["t_end"]
+
+
+def serve_once(reqs, arrivals, *, max_active, chunk_s, device):
+    import gpu_dsm_gb300 as dsm
+
+    srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s)
+    ids = []
+    t0 = time.perf_counter()
+    for r, a in zip(reqs, arrivals):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(**r))
+    srv.wait_all(3600.0)
+    wall = time.perf_counter() - t0
+    st = [srv.status(i) for i in ids]
+    out = []
+    for r, i in zip(reqs, ids):
+        out.append(srv.result_gt(i)[1] if r.get("eq_type") == 1 else srv.result_stress(i)[1])
+    tot = srv.stats()
+    srv.close()
+    lat = np.array([x["latency_s"] for x in st])
+    failed = sum(1 for x in st if x["state"] != dsm.api.REQ_DONE)
+    ev = sum(x["events"] for x in st)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "events_per_s": ev / wall, "makespan_s": wall, "events": int(ev),
+            "failed": failed, "chunks": tot["chunks"], "peak_active": tot["peak_active"],
+            "peak_bytes": tot["peak_bytes"], "busy_s": tot["busy_s"], "setup_s": tot["setup_s"],
+            "finish_s": tot["finish_s"]}, out
+
+
+def run_serve(args, device: int = 0) -> dict:
+    """Served (continuous batching) against plain (one request at a time, one
+    launch per request or output interval) on the same Poisson arrivals.
+    Offered load = 1.2 x the plain form's throughput, measured first on a
+    calibration stream (seed 12) submitted at once."""
+    cal = serve_stream(args.serve_cal, 12, args.serve_scale)
+    c, _ = serve_once(cal, [0.0] * len(cal), max_active=1, chunk_s=-1.0, device=device)
+    reqs = serve_stream(args.serve_requests, 11, args.serve_scale)
+    est = np.array([prior_events(r) for r in reqs])
+    cal_prior = sum(prior_events(r) for r in cal)
+    # plain throughput in prior-estimated events per second of wall time
+    plain_rate = cal_prior / c["makespan_s"]
+    lam = 1.2 * plain_rate / est.mean()
+    rng = np.random.default_rng(11)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=len(reqs)))
+    arrivals -= arrivals[0]
+    served, out_s = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device)
+    plain, out_p = serve_once(reqs, arrivals, max_active=1, chunk_s=-1.0, device=device)
+    err = 0.0
+    for r, a, b in zip(reqs, out_s, out_p):
+        if r.get("eq_type") == 1 and len(a) and len(b):
+            err = max(err, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)))
+    return {"requests": len(reqs), "t_end_scale": args.serve_scale, "arrival_rate_per_s": lam,
+            "offered_load_vs_plain": 1.2, "chunk_s": args.serve_chunk, "served": served, "plain": plain,
+            "p99_speedup": plain["p99_s"] / served["p99_s"], "p50_speedup": plain["p50_s"] / served["p50_s"],
+            "throughput_ratio": served["events_per_s"] / plain["events_per_s"],
+            "gt_max_rel_diff_served_vs_plain": err,
+            "stream": "Poisson arrivals (seed 11); N_K log-uniform [20,500], beta {0.5,1,2}, 1024-65536 chains, "
+                      "50% G(t) / 50% shear Wi log-uniform [0.1,100], t_end log-uniform [1e4,1e6] x t_end_scale"}
 
 
 def main():
@@ -324,6 +467,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--chains", type=int, default=65536, help="chains per GPU (65536 = headline workload)")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per chain (16 or 32; 0 = library default)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream leg")
+    ap.add_argument("--no-shear", action="store_true", help="skip the shear start-up leg")
+    ap.add_argument("--shear-only", action="store_true", help="run only the shear start-up leg")
+    ap.add_argument("--shear-windows", type=int, default=2)
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-cal", type=int, default=16)
+    ap.add_argument("--serve-scale", type=float, default=1.0e-3, help="t_end multiplier of the request stream")
+    ap.add_argument("--serve-chunk", type=float, default=0.05, help="target chunk duration of the served form (s)")
     args = ap.parse_args()
     global N_CHAINS
     N_CHAINS = args.chains
@@ -331,6 +483,16 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.shear_only:
+        from gpu_dsm_gb300 import build as native
+        native.build()
+        print(json.dumps({"shear": run_shear(args)}))
+        return 0
+    if args.serve_only:
+        from gpu_dsm_gb300 import build as native
+        native.build()
+        print(json.dumps({"serve": run_serve(args)}))
+        return 0
     return run_gpu(args)
 
 

@@ -18,6 +18,7 @@ _PKG = Path(__file__).resolve().parent
 _LIB: Optional[C.CDLL] = None
 
 DSM_OK = 0
+DSM_PENDING = 1
 DSM_ABORTED = -1
 
 
@@ -49,7 +50,7 @@ class DsmParams(C.Structure):
         ("warps_per_block", C.c_int32),
         ("s0", C.c_int32),
         ("lanes_per_chain", C.c_int32),
-        ("pad_", C.c_int32),
+        ("stream_priority", C.c_int32),
     ]
 
 
@@ -66,7 +67,8 @@ class StressPlus(C.Structure):
 
 class ServeTotals(C.Structure):
     _fields_ = [("events", C.c_uint64), ("busy_s", C.c_double), ("ticks", C.c_uint64), ("completed", C.c_uint64),
-                ("peak_bytes", C.c_uint64), ("peak_active", C.c_int32), ("pad_", C.c_int32)]
+                ("peak_bytes", C.c_uint64), ("peak_active", C.c_int32), ("pad_", C.c_int32),
+                ("setup_s", C.c_double), ("finish_s", C.c_double)]
 
 
 HEAD_DTYPE = np.dtype([("Z", np.int32), ("time", np.float32), ("dummy", np.float32), ("stall_flag", np.int32)])
@@ -110,6 +112,22 @@ def load_library() -> C.CDLL:
     lib.dsm_advance_batch.restype = C.c_int
     lib.dsm_save_file.argtypes = [vp, C.c_char_p]
     lib.dsm_load_file.argtypes = [vp, C.c_char_p]
+    lib.dsm_advance_series.argtypes = [vp, C.c_double, i32, vp, vp, C.POINTER(u64)]
+    lib.dsm_advance_series.restype = C.c_int
+    lib.dsm_advance_start.argtypes = [vp, C.c_double, i64]
+    lib.dsm_series_start.argtypes = [vp, vp, i32]
+    lib.dsm_poll.argtypes = [vp, C.POINTER(u64), vp, C.POINTER(i32)]
+    lib.dsm_abort.argtypes = [vp]
+    for fn in ("dsm_advance_start", "dsm_series_start", "dsm_poll", "dsm_abort"):
+        getattr(lib, fn).restype = C.c_int
+    lib.dsm_autotune.argtypes = [vp, C.c_double, vp, C.POINTER(C.c_float)]
+    lib.dsm_autotune.restype = C.c_int
+    lib.dsm_window_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
+    lib.dsm_window_stats.restype = C.c_int
+    lib.dsm_set_schedule.argtypes = [vp, i32, i32, i32, C.c_float]
+    lib.dsm_set_schedule.restype = C.c_int
+    lib.dsm_get_schedule.argtypes = [vp, C.POINTER(i32), vp]
+    lib.dsm_get_schedule.restype = C.c_int
     lib.dsm_pcd.argtypes = [C.c_double, i32, vp]
     lib.dsm_pcd.restype = C.c_int
     lib.dsm_serve_open.argtypes = [i32, u64, i32, C.c_double, C.POINTER(vp)]
@@ -275,6 +293,41 @@ class Ensemble:
         self._check(rc)
         return int(ev.value)
 
+    def advance_series(self, dt: float, n: int, abort: Optional[np.ndarray] = None):
+        """n windows of dt tau_K as one CUDA graph replay (dsm_advance_series).
+        Returns (kMC events, stress after each window as an (n, 8) array for
+        flow ensembles, else None)."""
+        ev = C.c_uint64()
+        out = (StressPlus * n)() if self.params.kappa[:] != [0.0] * 9 and any(self.params.kappa[:]) else None
+        self._check(self._lib.dsm_advance_series(self._h, dt, n, _ptr(abort),
+                                                 None if out is None else C.cast(out, C.c_void_p), C.byref(ev)))
+        st = None if out is None else np.array([out[i].as_array() for i in range(n)], np.float32)
+        return ev.value, st
+
+    # ------------------------------------------------------- asynchronous form
+    def advance_start(self, t_end: float, step_limit: int = -1) -> None:
+        """Enqueue a window on the ensemble's own stream and return (dsm_advance_start)."""
+        self._check(self._lib.dsm_advance_start(self._h, t_end, step_limit))
+        self._pending_n = 1
+
+    def series_start(self, t_ends) -> None:
+        """Enqueue windows ending at t_ends as one graph replay (dsm_series_start)."""
+        te = np.ascontiguousarray(t_ends, dtype=np.float64)
+        self._check(self._lib.dsm_series_start(self._h, _ptr(te), len(te)))
+        self._pending_n = len(te)
+
+    def poll(self):
+        """None while running; then (events, stress (n, 8) or None)."""
+        ev, nout = C.c_uint64(), C.c_int32()
+        n = max(1, getattr(self, "_pending_n", 1))
+        out = (StressPlus * n)()
+        rc = self._lib.dsm_poll(self._h, C.byref(ev), C.cast(out, C.c_void_p), C.byref(nout))
+        if rc == DSM_PENDING:
+            return None
+        self._check(rc)
+        st = np.array([out[i].as_array() for i in range(nout.value)], np.float32) if nout.value else None
+        return ev.value, st
+
     def last_window(self) -> dict:
         """Step-kernel device time (ms, CUDA events on its stream), events and launch shape of the
         last advance()."""
@@ -308,6 +361,34 @@ class Ensemble:
         self._check(self._lib.dsm_gt(self._h, _ptr(t), _ptr(g), C.byref(n)))
         return t[: n.value].copy(), g[: n.value].copy()
 
+    def autotune(self, window: float) -> dict:
+        """Pick the fastest launch schedule: one real window of ``window`` tau_K
+        per candidate (the ensemble advances); returns the choice."""
+        best = np.zeros(4, np.int32)
+        ms = C.c_float()
+        self._check(self._lib.dsm_autotune(self._h, window, _ptr(best), C.byref(ms)))
+        return {"small_slot": int(best[0]), "large_grid": int(best[1]), "lanes": int(best[2]),
+                "candidates": int(best[3]), "kernel_ms": ms.value}
+
+    def window_stats(self) -> dict:
+        """Counters of the last window: events, chains done in their first slot, chains deferred."""
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(self._lib.dsm_window_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"events": a.value, "chains_done": b.value, "deferred": c.value}
+
+    def set_schedule(self, small_slot: int = 0, large_grid: int = 0, lanes: int = 0, z_margin_sd: float = 0.0) -> None:
+        """Size-class launch schedule of a polydisperse ensemble (dsm_set_schedule)."""
+        self._check(self._lib.dsm_set_schedule(self._h, small_slot, large_grid, lanes, z_margin_sd))
+
+    def schedule(self) -> list:
+        """[{slot, warps_per_block, lanes, grid, chains}, ...]; empty for one launch over all chains."""
+        n = C.c_int32()
+        info = np.zeros(15, np.int32)
+        self._check(self._lib.dsm_get_schedule(self._h, C.byref(n), _ptr(info)))
+        keys = ("slot", "warps_per_block", "lanes", "grid", "chains")
+        m = n.value + 1 if n.value else 0
+        return [dict(zip(keys, info[5 * i:5 * i + 5].tolist())) for i in range(m)]
+
     def save(self, path: str) -> None:
         self._check(self._lib.dsm_save_file(self._h, os.fsencode(path)))
 
@@ -338,15 +419,15 @@ class Server:
 
     Requests (keyword arguments of ``make_params``) are admitted while their
     ensembles fit in ``hbm_budget`` bytes of device memory, stay resident and
-    are advanced together, one batched launch per kind and size class per
-    tick of about ``tick_s`` seconds.  ``max_active=1, tick_s=-1`` is the plain
-    form: one request at a time, each in as few launches as its outputs allow.
+    run concurrently, each on its own stream in chunks of about ``chunk_s``
+    seconds.  ``max_active=1, chunk_s=-1`` is the plain form: one request at a
+    time, one launch per request (equilibrium) or per output (flow).
     """
 
-    def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, tick_s: float = 0.0):
+    def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_s: float = 0.0):
         self._lib = load_library()
         h = C.c_void_p()
-        rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, tick_s, C.byref(h))
+        rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, chunk_s, C.byref(h))
         if rc != DSM_OK:
             raise DSMError(rc, "dsm_serve_open")
         self._h = h
@@ -398,7 +479,9 @@ class Server:
         rc = self._lib.dsm_serve_stats(self._h, C.byref(t))
         if rc != DSM_OK:
             raise DSMError(rc, "dsm_serve_stats")
-        return {n: getattr(t, n) for n, _ in ServeTotals._fields_ if n != "pad_"}
+        d = {n: getattr(t, n) for n, _ in ServeTotals._fields_ if n != "pad_"}
+        d["chunks"] = d.pop("ticks")
+        return d
 
     def close(self) -> None:
         if getattr(self, "_h", None):

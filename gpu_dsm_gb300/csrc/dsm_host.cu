@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -112,9 +113,62 @@ int dsm::corr_levels_for(double t_end, double dt, int p, int m) {
   return v < 1.0 ? 1 : (int)v;
 }
 
+static int plan_single(dsm_sim* s);
+static int default_schedule(dsm_sim* s);
+static void series_free(dsm_sim* s);
+static int enqueue_readback(dsm_sim* s);
+static int window_collect(dsm_sim* s, uint64_t* events);
+
 static bool is_flow(const float* k) {
   for (int q = 0; q < 9; ++q) if (k[q] != 0.0f) return true;
   return false;
+}
+
+// ------------------------------------------------------------------ host words
+// Small pinned, mapped host words of every handle (abort flag polled by the
+// running kernel; end-of-window counters and stress sums copied back
+// asynchronously) come from one slab allocated once per process: pinning
+// memory per handle costs milliseconds.
+namespace {
+constexpr int kSlab = 4096;
+std::mutex g_slab_mu;
+dsm::HostWords* g_slab = nullptr;
+std::vector<int> g_slab_free;
+}  // namespace
+
+dsm::HostWords* dsm::host_words_take() {
+  std::lock_guard<std::mutex> lk(g_slab_mu);
+  if (!g_slab) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, sizeof(HostWords) * kSlab, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
+      return nullptr;
+    g_slab = (HostWords*)p;
+    for (int i = kSlab - 1; i >= 0; --i) g_slab_free.push_back(i);
+  }
+  if (g_slab_free.empty()) return nullptr;
+  const int i = g_slab_free.back();
+  g_slab_free.pop_back();
+  std::memset(&g_slab[i], 0, sizeof(HostWords));
+  return &g_slab[i];
+}
+
+void dsm::host_words_give(HostWords* w) {
+  if (!w) return;
+  std::lock_guard<std::mutex> lk(g_slab_mu);
+  g_slab_free.push_back((int)(w - g_slab));
+}
+
+void dsm::keep_pool_memory(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done.push_back(device);
 }
 
 // ------------------------------------------------------------------ lifecycle
@@ -176,10 +230,17 @@ int dsm::sim_setup(dsm_sim* s) {
   s->nsamples = s->corr ? (int64_t)std::ceil(P.t_end / P.sync_dt) : 0;
 
   CK(cudaSetDevice(P.device));
-  CK(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
-  cudaDeviceProp prop;
-  CK(cudaGetDeviceProperties(&prop, P.device));
-  s->sm_count = prop.multiProcessorCount;
+  {
+    int lo = 0, hi = 0;  // least (numerically largest) and greatest priority
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    s->prio = std::max(hi, std::min(lo, P.stream_priority));
+  }
+  CK(cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, s->prio));
+  CK(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, P.device));
+  // device buffers come from the device's stream-ordered pool, which keeps
+  // freed memory for reuse: creating and destroying ensembles (a serving loop)
+  // then costs no device-wide synchronisation
+  keep_pool_memory(P.device);
 
   // device memory budget
   const size_t n = (size_t)P.n_chains, cap = (size_t)s->cap;
@@ -194,46 +255,49 @@ int dsm::sim_setup(dsm_sim* s) {
   std::vector<float> tb;
   TableOffsets to;
   make_tables(nkmax, be, s->prefact, tb, to);
-  CK(cudaMalloc(&s->d_tables, tb.size() * sizeof(float)));
-  CK(cudaMemcpy(s->d_tables, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMallocAsync((void**)&s->d_tables, tb.size() * sizeof(float), s->st));
+  CK(cudaMemcpyAsync(s->d_tables, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice, s->st));
 
   // state
-  CK(cudaMalloc(&s->d_QN, n * cap * sizeof(float4)));
-  CK(cudaMalloc(&s->d_tau, n * cap * sizeof(float)));
-  CK(cudaMalloc(&s->d_cs, n * sizeof(ChainState)));
-  CK(cudaMalloc(&s->d_stress, n * 8 * sizeof(float)));
-  CK(cudaMemset(s->d_QN, 0, n * cap * sizeof(float4)));
-  CK(cudaMemset(s->d_tau, 0, n * cap * sizeof(float)));
-  CK(cudaMemset(s->d_cs, 0, n * sizeof(ChainState)));
-  CK(cudaMemset(s->d_stress, 0, n * 8 * sizeof(float)));
+  CK(cudaMallocAsync((void**)&s->d_QN, n * cap * sizeof(float4), s->st));
+  CK(cudaMallocAsync((void**)&s->d_tau, n * cap * sizeof(float), s->st));
+  CK(cudaMallocAsync((void**)&s->d_cs, n * sizeof(ChainState), s->st));
+  CK(cudaMallocAsync((void**)&s->d_stress, n * 8 * sizeof(float), s->st));
+  CK(cudaMemsetAsync(s->d_QN, 0, n * cap * sizeof(float4), s->st));
+  CK(cudaMemsetAsync(s->d_tau, 0, n * cap * sizeof(float), s->st));
+  CK(cudaMemsetAsync(s->d_cs, 0, n * sizeof(ChainState), s->st));
+  CK(cudaMemsetAsync(s->d_stress, 0, n * 8 * sizeof(float), s->st));
   if (s->corr) {
     const size_t L = s->levels, pp = s->cp;
-    CK(cudaMalloc(&s->d_cshift, n * L * pp * 3 * sizeof(float)));
-    CK(cudaMalloc(&s->d_cacc, n * L * pp * sizeof(double)));
-    CK(cudaMalloc(&s->d_cavg, n * L * 3 * sizeof(float)));
-    CK(cudaMalloc(&s->d_ccnt, n * L * sizeof(int4)));
-    CK(cudaMalloc(&s->d_gsum, L * pp * sizeof(double)));
-    CK(cudaMalloc(&s->d_gcnt, L * pp * sizeof(long long)));
+    CK(cudaMallocAsync((void**)&s->d_cshift, n * L * pp * 3 * sizeof(float), s->st));
+    CK(cudaMallocAsync((void**)&s->d_cacc, n * L * pp * sizeof(double), s->st));
+    CK(cudaMallocAsync((void**)&s->d_cavg, n * L * 3 * sizeof(float), s->st));
+    CK(cudaMallocAsync((void**)&s->d_ccnt, n * L * sizeof(int4), s->st));
+    CK(cudaMallocAsync((void**)&s->d_gsum, L * pp * sizeof(double), s->st));
+    CK(cudaMallocAsync((void**)&s->d_gcnt, L * pp * sizeof(long long), s->st));
   }
   if (s->poly) {
-    CK(cudaMalloc(&s->d_pcd_by_nk, s->pcd_by_nk.size() * sizeof(PcdDev)));
-    CK(cudaMemcpy(s->d_pcd_by_nk, s->pcd_by_nk.data(), s->pcd_by_nk.size() * sizeof(PcdDev), cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&s->d_nk_chain, n * sizeof(int32_t)));
-    CK(cudaMemcpy(s->d_nk_chain, s->nk_chain.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMallocAsync((void**)&s->d_pcd_by_nk, s->pcd_by_nk.size() * sizeof(PcdDev), s->st));
+    CK(cudaMemcpyAsync(s->d_pcd_by_nk, s->pcd_by_nk.data(), s->pcd_by_nk.size() * sizeof(PcdDev), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMallocAsync((void**)&s->d_nk_chain, n * sizeof(int32_t), s->st));
+    CK(cudaMemcpyAsync(s->d_nk_chain, s->nk_chain.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
   }
-  CK(cudaMalloc(&s->d_ens, sizeof(EnsDev)));
-  CK(cudaMalloc(&s->d_prefix, 2 * sizeof(long long)));
-  CK(cudaMalloc(&s->d_work, sizeof(unsigned int)));
-  CK(cudaMalloc(&s->d_status, sizeof(int)));
-  CK(cudaMalloc(&s->d_counters, 4 * sizeof(unsigned long long)));
-  CK(cudaMalloc(&s->d_red, 16 * sizeof(double)));
+  CK(cudaMallocAsync((void**)&s->d_ens, sizeof(EnsDev), s->st));
+  CK(cudaMallocAsync((void**)&s->d_prefix, 2 * sizeof(long long), s->st));
+  CK(cudaMallocAsync((void**)&s->d_work, sizeof(unsigned int), s->st));
+  CK(cudaMallocAsync((void**)&s->d_status, sizeof(int), s->st));
+  CK(cudaMallocAsync((void**)&s->d_counters, 4 * sizeof(unsigned long long), s->st));
+  CK(cudaMallocAsync((void**)&s->d_red, 16 * sizeof(double), s->st));
   CK(cudaEventCreate(&s->ev0));
   CK(cudaEventCreate(&s->ev1));
-  CK(cudaHostAlloc(&s->h_abort, sizeof(int), cudaHostAllocMapped));
-  *s->h_abort = 0;
-  CK(cudaHostGetDevicePointer((void**)&s->d_abort, (void*)s->h_abort, 0));
+  CK(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
+  s->hw = host_words_take();
+  if (!s->hw) return fail(s, DSM_ERR_CUDA, "pinned host memory for the abort flag and counters");
+  s->hw->abort = 0;
+  s->h_abort = &s->hw->abort;
+  CK(cudaHostGetDevicePointer((void**)&s->d_abort, (void*)&s->hw->abort, 0));
   const long long pre[2] = {0, (long long)P.n_chains};
-  CK(cudaMemcpy(s->d_prefix, pre, sizeof(pre), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(s->d_prefix, pre, sizeof(pre), cudaMemcpyHostToDevice, s->st));
 
   // device descriptor
   EnsDev& E = s->h;
@@ -254,7 +318,7 @@ int dsm::sim_setup(dsm_sim* s) {
   E.QN = s->d_QN; E.tau = s->d_tau; E.cs = s->d_cs;
   E.corr_shift = s->d_cshift; E.corr_acc = s->d_cacc; E.corr_avg = s->d_cavg; E.corr_cnt = s->d_ccnt;
   E.out_stress = s->d_stress; E.counters = s->d_counters;
-  CK(cudaMemcpy(s->d_ens, &E, sizeof(E), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(E), cudaMemcpyHostToDevice, s->st));
 
   // launch shape
   s->cfg.slot_cap = s->cap;
@@ -264,27 +328,139 @@ int dsm::sim_setup(dsm_sim* s) {
   if (P.lanes_per_chain != 0 && P.lanes_per_chain != 16 && P.lanes_per_chain != 32)
     return fail(s, DSM_ERR_INVALID, "lanes_per_chain must be 16 or 32");
   s->cfg.lanes = P.lanes_per_chain > 0 ? P.lanes_per_chain : 32;
-  const size_t smem = step_block_smem(s->cfg);
-  if (smem > (size_t)prop.sharedMemPerBlockOptin)
+  {
+    const int rc = s->poly ? plan_classes(s, 0, 0, 0, 0.f) : default_schedule(s);
+    if (rc != DSM_OK) return rc;
+  }
+  CK(cudaStreamSynchronize(s->st));  // host-side sources of the copies above
+  s->ready = true;
+  return DSM_OK;
+}
+
+// Largest slot (strands) at which the step kernel keeps `bps_want` blocks of
+// `cfg.warps_per_block` warps resident per SM (0 if even one strand does not)
+static int largest_slot(bool flow, bool corr, LaunchCfg cfg, int bps_want, int hi) {
+  int lo = 0;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    cfg.slot_cap = mid;
+    if (step_max_blocks_per_sm(flow, corr, cfg) >= bps_want) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One launch over all chains with slots of the full capacity
+static int plan_single(dsm_sim* s) {
+  s->classes.clear();
+  ++s->sched_version;
+  s->cfg.slot_cap = s->cap;
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
+  if (step_block_smem(s->cfg) > (size_t)smem_optin)
     return fail(s, DSM_ERR_INVALID, "chain capacity z_max=" + std::to_string(s->cap) + " does not fit one shared-memory slot");
   const int bps = step_max_blocks_per_sm(s->flow, s->corr, s->cfg);
   if (bps < 1) return fail(s, DSM_ERR_CUDA, "step kernel cannot be resident (occupancy 0)");
   s->blocks_per_sm = bps;
   const int tiles = s->cfg.warps_per_block * 32 / s->cfg.lanes;
-  const long long want = ((long long)P.n_chains + tiles - 1) / tiles;
+  const long long want = ((long long)s->P.n_chains + tiles - 1) / tiles;
   s->grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
-  s->ready = true;
+  return DSM_OK;
+}
+
+int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float margin_sd) {
+  s->classes.clear();
+  ++s->sched_version;
+  const dsm_params& P = s->P;
+  const int n = P.n_chains;
+  LaunchCfg sc = s->cfg;
+  if (lanes == 16 || lanes == 32) sc.lanes = lanes;
+  sc.warps_per_block = 4;
+  // full occupancy of the step kernel is 4 blocks x 4 warps per SM (register bound)
+  const int full_cap = largest_slot(s->flow, s->corr, sc, 4, s->cap);
+  if (small_cap <= 0) small_cap = full_cap;
+  // one slot size fits all chains at full occupancy (or no useful split)
+  if (small_cap >= s->cap || small_cap < 8) return plan_single(s);
+  // chains whose strand count is expected to stay below the small slot
+  // (mean + margin_sd sd of 1 + Binomial(N_K - 1, 1/(1+beta)), plus 2) go there
+  const double pe = 1.0 / (1.0 + (double)P.beta);
+  const double msd = margin_sd > 0.f ? (double)margin_sd : 5.0;
+  std::vector<int> big, small;
+  int nk_big = 0;
+  double w_big = 0.0, w_all = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const int nk = s->nk_chain[i];
+    const double m = 1.0 + (nk - 1) * pe, sd = std::sqrt(std::max(0.0, (nk - 1) * pe * (1.0 - pe)));
+    const double zb = std::min((double)nk, m + msd * sd + 2.0);
+    // work per tau_K: events ~ N_K, cost per event ~ strands + fixed part
+    const double w = (double)nk * (m + 40.0);
+    w_all += w;
+    if (zb > small_cap) { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
+    else small.push_back(i);
+  }
+  auto by_nk = [&](int a, int b) { return s->nk_chain[a] != s->nk_chain[b] ? s->nk_chain[a] > s->nk_chain[b] : a < b; };
+  std::sort(big.begin(), big.end(), by_nk);
+  std::sort(small.begin(), small.end(), by_nk);
+  std::vector<int> order(big);
+  order.insert(order.end(), small.begin(), small.end());
+  if (!s->d_order) {
+    CK(cudaMallocAsync((void**)&s->d_order, (size_t)n * sizeof(int), s->st));
+    CK(cudaMallocAsync((void**)&s->d_defer, (size_t)n * sizeof(int), s->st));
+    CK(cudaMallocAsync((void**)&s->d_works, 4 * sizeof(unsigned int), s->st));
+    CK(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, s->prio));
+    CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+  }
+  CK(cudaMemcpyAsync(s->d_order, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s->st));
+  const int tiles_per_sm_full = 16;
+  SizeClass B, Sm;
+  if (!big.empty()) {
+    B.cfg = LaunchCfg{1, std::min(s->cap, nk_big), s->cfg.pmax, 32};
+    B.bps = step_max_blocks_per_sm(s->flow, s->corr, B.cfg);
+    if (B.bps < 1) return fail(s, DSM_ERR_INVALID, "largest chains do not fit one shared-memory slot");
+    B.first = 0;
+    B.count = (long long)big.size();
+    int g = big_grid > 0 ? big_grid
+                         : (int)std::ceil(w_big / std::max(w_all, 1.0) * tiles_per_sm_full * s->sm_count);
+    g = (int)std::max<long long>(1, std::min<long long>(g, std::min<long long>(B.count, (long long)B.bps * s->sm_count)));
+    B.grid = g;
+  }
+  Sm.cfg = LaunchCfg{4, small_cap, s->cfg.pmax, sc.lanes};
+  Sm.bps = step_max_blocks_per_sm(s->flow, s->corr, Sm.cfg);
+  if (Sm.bps < 1) return fail(s, DSM_ERR_INVALID, "small slot does not fit shared memory");
+  Sm.first = B.count;
+  Sm.count = (long long)small.size();
+  {
+    const int tiles = 4 * 32 / Sm.cfg.lanes;
+    Sm.grid = (int)std::max<long long>(1, std::min<long long>((Sm.count + tiles - 1) / tiles,
+                                                                (long long)Sm.bps * s->sm_count));
+  }
+  s->cleanup = SizeClass{};
+  s->cleanup.cfg = LaunchCfg{1, s->cap, s->cfg.pmax, 32};
+  s->cleanup.bps = step_max_blocks_per_sm(s->flow, s->corr, s->cleanup.cfg);
+  if (s->cleanup.bps < 1) return fail(s, DSM_ERR_INVALID, "chain capacity does not fit one shared-memory slot");
+  s->cleanup.grid = s->cleanup.bps * s->sm_count;
+  if (B.count > 0) s->classes.push_back(B);
+  s->classes.push_back(Sm);
+  s->blocks_per_sm = Sm.bps;
+  s->grid = Sm.grid;
   return DSM_OK;
 }
 
 extern "C" void dsm_destroy(dsm_sim* s) {
   if (!s) return;
   if (s->st) cudaStreamSynchronize(s->st);
+  if (s->st) series_free(s);
+  if (s->side) cudaStreamSynchronize(s->side);
   void* ptrs[] = {s->d_tables, s->d_QN, s->d_tau, s->d_cs, s->d_stress, s->d_cshift, s->d_cacc, s->d_cavg,
                   s->d_ccnt, s->d_gsum, s->d_gcnt, s->d_pcd_by_nk, s->d_nk_chain, s->d_ens, s->d_prefix,
-                  s->d_work, s->d_status, s->d_counters, s->d_red};
-  for (void* p : ptrs) if (p) cudaFree(p);
-  if (s->h_abort) cudaFreeHost((void*)s->h_abort);
+                  s->d_work, s->d_status, s->d_counters, s->d_red, s->d_order, s->d_defer, s->d_works};
+  // stream-ordered frees: no device-wide synchronisation
+  for (void* p : ptrs) if (p) cudaFreeAsync(p, s->st);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->side) cudaStreamDestroy(s->side);
+  dsm::host_words_give(s->hw);
+  if (s->ev_done) cudaEventDestroy(s->ev_done);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->st) cudaStreamDestroy(s->st);
@@ -292,6 +468,124 @@ extern "C" void dsm_destroy(dsm_sim* s) {
 }
 
 extern "C" const char* dsm_last_error(const dsm_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+// Default launch schedule of a monodisperse ensemble.  Equilibrium chains run
+// two per warp (16 lanes each) with slots of the size that keeps 4 blocks of 4
+// warps per SM, when the chains' strand count (mean + 5 sd of its equilibrium
+// law) fits such a slot: 32 chains per SM instead of 16 (measured +14 % at
+// N_K = 200).  A chain that still outgrows the slot finishes in the overflow
+// launch.  Otherwise, and for flow, one warp per chain with full-capacity slots.
+static int default_schedule(dsm_sim* s) {
+  if (s->flow || s->P.lanes_per_chain != 0) return plan_single(s);
+  LaunchCfg c = s->cfg;
+  c.lanes = 16;
+  c.warps_per_block = 4;
+  const int cap16 = largest_slot(s->flow, s->corr, c, 4, s->cap);
+  const double pe = 1.0 / (1.0 + (double)s->P.beta), nk = (double)s->P.nk;
+  const double zb = 1.0 + (nk - 1.0) * pe + 5.0 * std::sqrt(std::max(0.0, (nk - 1.0) * pe * (1.0 - pe))) + 2.0;
+  if (cap16 >= s->cap) {
+    s->cfg.lanes = 16;
+    return plan_single(s);
+  }
+  if (cap16 >= 8 && zb <= cap16) {
+    s->cfg.lanes = 16;
+    return plan_classes(s, cap16, 0, 16, 0.f);
+  }
+  return plan_single(s);
+}
+
+extern "C" int dsm_set_schedule(dsm_sim* s, int32_t small_slot, int32_t large_grid, int32_t lanes,
+                                float z_margin_sd) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  if (lanes != 0 && lanes != 16 && lanes != 32) return fail(s, DSM_ERR_INVALID, "lanes must be 16 or 32");
+  CK(cudaStreamSynchronize(s->st));
+  if (lanes) s->cfg.lanes = lanes;
+  // monodisperse ensembles keep one launch with full-capacity slots unless a
+  // smaller slot is asked for (chains that outgrow it finish in the overflow launch)
+  if (!s->poly && small_slot <= 0) return plan_single(s);
+  return plan_classes(s, small_slot, large_grid, lanes, z_margin_sd);
+}
+
+// ------------------------------------------------------------------ autotuner
+// Online: every candidate schedule runs one real window of the simulation
+// (trajectories do not depend on the schedule, so nothing is restored and no
+// trial is wasted) and the one with the most events per kernel millisecond is
+// kept.
+extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* best_ms) {
+  if (!s || !s->ready || !(window > 0.0) || s->pending) return DSM_ERR_INVALID;
+  struct Cand { int small, grid, lanes; };
+  std::vector<Cand> cands;
+  for (int lanes : {32, 16}) {
+    if (!s->poly) cands.push_back({0, 0, lanes});  // one launch, full-capacity slots
+    // small slot: the largest with 4, 3 or 2 blocks of 4 warps per SM
+    LaunchCfg c = s->cfg;
+    c.lanes = lanes;
+    c.warps_per_block = 4;
+    std::vector<int> smalls;
+    for (int bps : {4, 3, 2}) {
+      const int cap = largest_slot(s->flow, s->corr, c, bps, s->cap);
+      if (cap >= 8 && std::find(smalls.begin(), smalls.end(), cap) == smalls.end()) smalls.push_back(cap);
+    }
+    for (int sm : smalls) {
+      if (!s->poly) {
+        // a smaller slot pays only if the chains' strand counts stay below it
+        const double pe = 1.0 / (1.0 + (double)s->P.beta), nk = (double)s->P.nk;
+        const double zb = 1.0 + (nk - 1.0) * pe + 5.0 * std::sqrt((nk - 1.0) * pe * (1.0 - pe)) + 2.0;
+        if (sm >= s->cap || zb > sm) continue;
+      }
+      const int rc = plan_classes(s, sm, 0, lanes, 0.f);
+      if (rc != DSM_OK) return rc;
+      const int g0 = s->classes.size() > 1 ? s->classes[0].grid : 0;
+      if (g0 == 0) { cands.push_back({sm, 0, lanes}); continue; }
+      for (int g : {std::max(1, g0 / 2), g0, 2 * g0}) cands.push_back({sm, g, lanes});
+    }
+  }
+  int bi = -1;
+  double brate = 0.0;
+  float bms = 0.f;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    const Cand& c = cands[i];
+    s->cfg.lanes = c.lanes;
+    int rc = (s->poly || c.small > 0) ? plan_classes(s, c.small, c.grid, c.lanes, 0.f) : plan_single(s);
+    if (rc != DSM_OK) return rc;
+    rc = sim_launch_window(s, s->t_done + window, -1);
+    if (rc == DSM_OK) rc = sim_finish_window(s, nullptr);
+    if (rc != DSM_OK) return rc;
+    const double rate = (double)s->last_events / std::max(1e-6, (double)s->last_kernel_ms);
+    if (bi < 0 || rate > brate) { bi = (int)i; brate = rate; bms = s->last_kernel_ms; }
+  }
+  const Cand& b = cands[bi];
+  s->cfg.lanes = b.lanes;
+  const int rc = (s->poly || b.small > 0) ? plan_classes(s, b.small, b.grid, b.lanes, 0.f) : plan_single(s);
+  if (best) { best[0] = b.small; best[1] = b.grid; best[2] = b.lanes; best[3] = (int32_t)cands.size(); }
+  if (best_ms) *best_ms = bms;
+  return rc;
+}
+
+extern "C" int dsm_window_stats(const dsm_sim* s, uint64_t* events, uint64_t* chains_done, uint64_t* deferred) {
+  if (!s || !s->hw) return DSM_ERR_INVALID;
+  if (events) *events = s->hw->cnt[0];
+  if (chains_done) *chains_done = s->hw->cnt[1];
+  if (deferred) *deferred = s->hw->cnt[2];
+  return DSM_OK;
+}
+
+extern "C" int dsm_get_schedule(const dsm_sim* s, int32_t* n_classes, int32_t* info) {
+  if (!s || !n_classes) return DSM_ERR_INVALID;
+  *n_classes = (int32_t)s->classes.size();
+  if (info) {
+    for (int i = 0; i < 15; ++i) info[i] = 0;
+    int i = 0;
+    auto put = [&](const SizeClass& k, long long count) {
+      info[5 * i + 0] = k.cfg.slot_cap; info[5 * i + 1] = k.cfg.warps_per_block; info[5 * i + 2] = k.cfg.lanes;
+      info[5 * i + 3] = k.grid; info[5 * i + 4] = (int32_t)count;
+      ++i;
+    };
+    for (const SizeClass& k : s->classes) put(k, k.count);
+    if (!s->classes.empty()) put(s->cleanup, 0);
+  }
+  return DSM_OK;
+}
 
 extern "C" int dsm_corr_shape(const dsm_sim* s, int32_t* levels, int32_t* p, int32_t* m) {
   if (!s) return DSM_ERR_INVALID;
@@ -424,42 +718,306 @@ extern "C" int dsm_set_ext(dsm_sim* s, const int64_t* T, const uint64_t* steps, 
 }
 
 // ------------------------------------------------------------------ time evolution
+// Per-chain event cap of one launch: a chain whose dt collapses (rates blowing
+// up) stops with stall code 5 instead of keeping the GPU busy.  The cap is
+// 100x the expected events of a window of dt_tau (<sum W> ~ 0.25 N_K per
+// tau_K), at least 2^24.
+static int64_t window_watchdog(const dsm_sim* s, double dt_tau) {
+  if (s->watchdog_events > 0) return s->watchdog_events;
+  const double expect = 0.25 * (double)s->nkmax * std::max(0.0, dt_tau) * 100.0;
+  return (int64_t)std::max(16777216.0, std::min(expect, 9.0e18));
+}
+
+// The step launch(es) of one window on s->st (the descriptor already holds
+// the window): one launch over all chains, or the size classes
+static int enqueue_step(dsm_sim* s) {
+  if (s->classes.empty()) {
+    CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
+    CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->corr, s->cfg,
+                   s->d_abort, s->d_status, s->grid, s->st));
+    return DSM_OK;
+  }
+  // size classes: large-slot chains on the side stream first (their blocks
+  // are placed first), small-slot chains on the main stream; then the chains
+  // that outgrew their slot, in slots of the ensemble's full capacity
+  CK(cudaMemsetAsync(s->d_works, 0, 4 * sizeof(unsigned int), s->st));
+  CK(cudaEventRecord(s->ev_fork, s->st));
+  CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+  for (const SizeClass& k : s->classes) {
+    const bool large = k.cfg.warps_per_block == 1;
+    StepList l;
+    l.order = s->d_order + k.first;
+    l.defer = s->d_defer;
+    l.n_defer = s->d_works + 3;
+    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, s->d_works + (large ? 1 : 0), s->flow, s->corr, k.cfg,
+                   s->d_abort, s->d_status, k.grid, large ? s->side : s->st, l));
+  }
+  CK(cudaEventRecord(s->ev_join, s->side));
+  CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
+  StepList l;
+  l.order = s->d_defer;
+  l.dyn_total = s->d_works + 3;
+  CK(launch_step(s->d_ens, 1, s->d_prefix, 0, s->d_works + 2, s->flow, s->corr, s->cleanup.cfg, s->d_abort,
+                 s->d_status, s->cleanup.grid, s->st, l));
+  return DSM_OK;
+}
+
 int dsm::sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit) {
   EnsDev& E = s->h;
   E.t_end_ticks = (int64_t)std::llrint(t_end * TICKS);
   s->t_window = t_end;
   E.step_limit = step_limit < 0 ? INT64_MAX : step_limit;
-  // Per-chain event cap of one launch: a chain whose dt collapses (rates blowing
-  // up) stops with stall code 5 instead of keeping the GPU busy.  The cap is
-  // 100x the expected events of the window (<sum W> ~ 0.25 N_K per tau_K), at
-  // least 2^24.
-  double expect = 0.0;
-  {
-    int64_t tmin = INT64_MAX;
-    (void)tmin;
-    expect = 0.25 * (double)s->nkmax * std::max(0.0, t_end - s->t_done) * 100.0;
-  }
-  const double wd = std::max(16777216.0, std::min(expect, 9.0e18));
-  E.watchdog_events = s->watchdog_events > 0 ? s->watchdog_events : (int64_t)wd;
+  E.watchdog_events = window_watchdog(s, t_end - s->t_done);
   CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
-  CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
   CK(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st));
   CK(cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), s->st));
   CK(cudaEventRecord(s->ev0, s->st));
-  CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->corr, s->cfg,
-                 s->d_abort, s->d_status, s->grid, s->st));
+  const int rc = enqueue_step(s);
+  if (rc != DSM_OK) return rc;
   CK(cudaEventRecord(s->ev1, s->st));
   return DSM_OK;
 }
 
-int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
-  unsigned long long cnt[4];
-  int status = 0;
-  CK(cudaMemcpyAsync(cnt, s->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
-  CK(cudaMemcpyAsync(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
-  if (s->flow) CK(launch_stress_reduce_dev(s->d_ens, s->d_red, s->st));
+// ------------------------------------------------------------------ graph series
+// n windows as one CUDA graph: per window a one-thread kernel sets the end
+// time and event cap from a device array, then the step launch(es), then
+// (flow) the stress sums of the window into their own slot; at the end the
+// sums and counters go to pinned host memory.  One graph is captured per
+// (n, launch schedule) and replayed with new end times.
+static void series_free(dsm_sim* s) {
+  for (auto& g : s->ser_graphs) cudaGraphExecDestroy(g.second);
+  s->ser_graphs.clear();
+  if (s->ser_d) cudaFreeAsync(s->ser_d, s->st);
+  if (s->ser_h) cudaFreeHost(s->ser_h);
+  s->ser_d = nullptr;
+  s->ser_h = nullptr;
+  s->ser_cap = 0;
+}
+
+static long long* ser_win_h(dsm_sim* s) { return (long long*)s->ser_h; }
+static double* ser_out_h(dsm_sim* s) { return (double*)((char*)s->ser_h + (size_t)s->ser_cap * 2 * sizeof(long long)); }
+
+static int series_capture(dsm_sim* s, int n, cudaGraphExec_t* exec) {
+  const size_t win_bytes = (size_t)s->ser_cap * 2 * sizeof(long long);
+  long long* d_win = (long long*)s->ser_d;
+  double* d_out = (double*)((char*)s->ser_d + win_bytes);
   CK(cudaStreamSynchronize(s->st));
+  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+  int rc = DSM_OK;
+  auto cap = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == DSM_OK) rc = fail(s, DSM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  cap(cudaMemcpyAsync(d_win, s->ser_h, win_bytes, cudaMemcpyHostToDevice, s->st), "series window copy");
+  cap(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st), "memset");
+  cap(cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), s->st), "memset");
+  // timing events must be real event-record nodes (a plain record inside a
+  // capture only orders streams)
+  cap(cudaEventRecordWithFlags(s->ev0, s->st, cudaEventRecordExternal), "event");
+  for (int w = 0; w < n && rc == DSM_OK; ++w) {
+    cap(launch_window_begin(s->d_ens, d_win, s->ser_cap, w, s->st), "window begin");
+    if (rc == DSM_OK) rc = enqueue_step(s);
+    if (s->flow && rc == DSM_OK) cap(launch_stress_reduce_dev(s->d_ens, d_out + 9 * w, s->st), "stress");
+  }
+  cap(cudaEventRecordWithFlags(s->ev1, s->st, cudaEventRecordExternal), "event");
+  cap(cudaMemcpyAsync(ser_out_h(s), d_out, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st), "copy");
+  cap(cudaMemcpyAsync(s->hw->cnt, s->d_counters, sizeof(s->hw->cnt), cudaMemcpyDeviceToHost, s->st), "copy");
+  cap(cudaMemcpyAsync(&s->hw->status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st), "copy");
+  cudaGraph_t g = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(s->st, &g);
+  if (rc != DSM_OK) { if (g) cudaGraphDestroy(g); return rc; }
+  CK(ee);
+  const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(ie);
+  return DSM_OK;
+}
+
+// Graph for n windows with buffers for at least n; recaptured when the launch
+// schedule changed
+static int series_prepare(dsm_sim* s, int n, cudaGraphExec_t* exec) {
+  if (s->ser_version != s->sched_version || n > s->ser_cap) {
+    int cap = std::max(n, s->ser_cap);
+    if (s->ser_version == s->sched_version || cap < 16) cap = std::max(cap, 16);
+    series_free(s);
+    const size_t bytes = (size_t)cap * (2 * sizeof(long long) + 9 * sizeof(double));
+    CK(cudaMallocAsync(&s->ser_d, bytes, s->st));
+    CK(cudaHostAlloc(&s->ser_h, bytes, cudaHostAllocDefault));
+    s->ser_cap = cap;
+    s->ser_version = s->sched_version;
+  }
+  for (auto& g : s->ser_graphs)
+    if (g.first == n) { *exec = g.second; return DSM_OK; }
+  cudaGraphExec_t e = nullptr;
+  const int rc = series_capture(s, n, &e);
+  if (rc != DSM_OK) return rc;
+  s->ser_graphs.push_back({n, e});
+  *exec = e;
+  return DSM_OK;
+}
+
+// Enqueue windows ending at ends[0..n) (ascending, after the current time)
+static int series_start(dsm_sim* s, const double* ends, int n) {
+  double t_prev = s->t_done;
+  for (int w = 0; w < n; ++w) {
+    if (!(ends[w] >= t_prev) || ends[w] * TICKS >= 9.0e18)
+      return fail(s, DSM_ERR_INVALID, "series end times must ascend from the current time");
+    t_prev = ends[w];
+  }
+  cudaGraphExec_t exec = nullptr;
+  const int rc = series_prepare(s, n, &exec);
+  if (rc != DSM_OK) return rc;
+  long long* h_win = ser_win_h(s);
+  t_prev = s->t_done;
+  for (int w = 0; w < n; ++w) {
+    h_win[w] = (long long)std::llrint(ends[w] * TICKS);  // as dsm_advance(ends[w])
+    h_win[s->ser_cap + w] = (long long)window_watchdog(s, ends[w] - t_prev);
+    t_prev = ends[w];
+  }
+  s->t_window = t_prev;
+  s->ser_n = n;
+  EnsDev& E = s->h;
+  E.step_limit = INT64_MAX;
+  CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
+  CK(cudaGraphLaunch(exec, s->st));
+  CK(cudaEventRecord(s->ev_done, s->st));
+  return DSM_OK;
+}
+
+static void stress_out(const double* r, dsm_stress_plus* o) {
+  const double d = r[8] > 0 ? r[8] : 1.0;
+  o->xx = (float)(r[0] / d); o->yy = (float)(r[1] / d); o->zz = (float)(r[2] / d);
+  o->xy = (float)(r[3] / d); o->yz = (float)(r[4] / d); o->zx = (float)(r[5] / d);
+  o->Lpp = (float)(r[6] / d); o->Z = (float)(r[7] / d);
+}
+
+static int series_collect(dsm_sim* s, dsm_stress_plus* out, uint64_t* events) {
   CK(cudaGetLastError());
+  const int n = s->ser_n;
+  const double* h_out = ser_out_h(s);
+  const unsigned long long ev = s->hw->cnt[0];
+  if (events) *events = ev;
+  s->events_total += ev;
+  s->last_events = ev;
+  s->t_done = s->t_window;
+  CK(cudaEventElapsedTime(&s->last_kernel_ms, s->ev0, s->ev1));
+  if (s->flow) {
+    for (int q = 0; q < 9; ++q) s->hw->red[q] = h_out[9 * (n - 1) + q];
+    if (out) for (int w = 0; w < n; ++w) stress_out(h_out + 9 * w, &out[w]);
+  }
+  if (s->hw->status & 1) return DSM_ABORTED;
+  return DSM_OK;
+}
+
+// wait for the pending work of s, forwarding the caller's abort flag
+static int wait_pending(dsm_sim* s, const volatile int32_t* abort_flag) {
+  if (abort_flag) {
+    while (cudaEventQuery(s->ev_done) == cudaErrorNotReady) {
+      if (*abort_flag) *s->h_abort = 1;
+      std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+  }
+  CK(cudaEventSynchronize(s->ev_done));
+  return DSM_OK;
+}
+
+static std::vector<double> series_ends(const dsm_sim* s, double dt, int n) {
+  std::vector<double> e(n);
+  for (int w = 0; w < n; ++w) e[w] = s->t_done + dt * (w + 1);  // as dsm_advance(t + dt*(w+1))
+  return e;
+}
+
+extern "C" int dsm_advance_series(dsm_sim* s, double dt, int32_t n, const volatile int32_t* abort_flag,
+                                  dsm_stress_plus* out, uint64_t* events) {
+  if (!s || !s->ready || n < 1 || !(dt > 0.0) || s->pending) return DSM_ERR_INVALID;
+  *s->h_abort = (abort_flag && *abort_flag) ? 1 : 0;
+  const std::vector<double> e = series_ends(s, dt, n);
+  int rc = series_start(s, e.data(), n);
+  if (rc == DSM_OK) rc = wait_pending(s, abort_flag);
+  if (rc == DSM_OK) rc = series_collect(s, out, events);
+  *s->h_abort = 0;
+  return rc;
+}
+
+// ------------------------------------------------------------------ asynchronous form
+extern "C" int dsm_advance_start(dsm_sim* s, double t_end, int64_t step_limit) {
+  if (!s || !s->ready || s->pending) return DSM_ERR_INVALID;
+  if (!(t_end >= 0.0) || t_end * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
+  *s->h_abort = 0;
+  int rc = sim_launch_window(s, t_end, step_limit);
+  if (rc == DSM_OK) rc = enqueue_readback(s);
+  if (rc == DSM_OK) s->pending = 1;
+  return rc;
+}
+
+extern "C" int dsm_series_start(dsm_sim* s, const double* t_ends, int32_t n) {
+  if (!s || !s->ready || !t_ends || n < 1 || s->pending) return DSM_ERR_INVALID;
+  *s->h_abort = 0;
+  const int rc = series_start(s, t_ends, n);
+  if (rc == DSM_OK) s->pending = 2;
+  return rc;
+}
+
+extern "C" int dsm_poll(dsm_sim* s, uint64_t* events, dsm_stress_plus* out, int32_t* n_out) {
+  if (!s || !s->ready || !s->pending) return DSM_ERR_INVALID;
+  const cudaError_t q = cudaEventQuery(s->ev_done);
+  if (q == cudaErrorNotReady) return DSM_PENDING;
+  CK(q);
+  const int kind = s->pending;
+  s->pending = 0;
+  if (kind == 2) {
+    if (n_out) *n_out = s->ser_n;
+    return series_collect(s, out, events);
+  }
+  const int rc = window_collect(s, events);
+  if (n_out) *n_out = s->flow ? 1 : 0;
+  if (out && s->flow) stress_out(s->hw->red, out);
+  return rc;
+}
+
+extern "C" int dsm_set_priority(dsm_sim* s, int32_t priority) {
+  if (!s || !s->ready || s->pending) return DSM_ERR_INVALID;
+  int lo = 0, hi = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  const int pr = std::max(hi, std::min(lo, (int)priority));
+  if (pr == s->prio) return DSM_OK;
+  // the handle is idle: everything enqueued so far has completed or is ordered
+  // before the new streams' work by the synchronisation below
+  CK(cudaStreamSynchronize(s->st));
+  if (s->side) CK(cudaStreamSynchronize(s->side));
+  cudaStream_t st = nullptr, side = nullptr;
+  CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, pr));
+  if (s->side) CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, pr));
+  cudaStreamDestroy(s->st);
+  s->st = st;
+  if (s->side) { cudaStreamDestroy(s->side); s->side = side; }
+  s->prio = pr;
+  return DSM_OK;
+}
+
+extern "C" int dsm_abort(dsm_sim* s) {
+  if (!s || !s->ready) return DSM_ERR_INVALID;
+  *s->h_abort = 1;
+  return DSM_OK;
+}
+
+// End of a window on s->st: counters, status and (flow) the stress sums into
+// pinned memory, then the done event
+static int enqueue_readback(dsm_sim* s) {
+  CK(cudaMemcpyAsync(s->hw->cnt, s->d_counters, sizeof(s->hw->cnt), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(&s->hw->status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  if (s->flow) {
+    CK(launch_stress_reduce_dev(s->d_ens, s->d_red, s->st));
+    CK(cudaMemcpyAsync(s->hw->red, s->d_red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  }
+  CK(cudaEventRecord(s->ev_done, s->st));
+  return DSM_OK;
+}
+
+// Host bookkeeping of a completed window (its readback has landed)
+static int window_collect(dsm_sim* s, uint64_t* events) {
+  CK(cudaGetLastError());
+  const unsigned long long* cnt = s->hw->cnt;
+  const int status = s->hw->status;
   if (events) *events = cnt[0];
   s->events_total += cnt[0];
   s->t_done = std::max(s->t_done, s->t_window);
@@ -469,21 +1027,24 @@ int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
   return DSM_OK;
 }
 
+int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
+  const int rc = enqueue_readback(s);
+  if (rc != DSM_OK) return rc;
+  CK(cudaStreamSynchronize(s->st));
+  return window_collect(s, events);
+}
+
 extern "C" int dsm_advance(dsm_sim* s, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
                            uint64_t* events) {
   if (!s || !s->ready) return DSM_ERR_INVALID;
   if (!(t_end >= 0.0) || t_end * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
   *s->h_abort = (abort_flag && *abort_flag) ? 1 : 0;
+  if (s->pending) return fail(s, DSM_ERR_INVALID, "an asynchronous advance is pending (dsm_poll it first)");
   int rc = sim_launch_window(s, t_end, step_limit);
-  if (rc) return rc;
-  if (abort_flag) {
-    // forward the caller's flag into the mapped word the kernel polls
-    while (cudaStreamQuery(s->st) == cudaErrorNotReady) {
-      if (*abort_flag) *s->h_abort = 1;
-      std::this_thread::sleep_for(std::chrono::microseconds(200));
-    }
-  }
-  rc = sim_finish_window(s, events);
+  if (rc == DSM_OK) rc = enqueue_readback(s);
+  // forward the caller's flag into the mapped word the kernel polls
+  if (rc == DSM_OK) rc = wait_pending(s, abort_flag);
+  if (rc == DSM_OK) rc = window_collect(s, events);
   *s->h_abort = 0;
   return rc;
 }
@@ -495,9 +1056,9 @@ extern "C" int dsm_stress(dsm_sim* s, dsm_stress_plus* out, int32_t* count) {
     // zero-length flow-free pass (same kernel path as a window end)
     return fail(s, DSM_ERR_INVALID, "dsm_stress is defined for flow ensembles (kappa != 0)");
   }
-  double r[9];
-  CK(cudaMemcpyAsync(r, s->d_red, sizeof(r), cudaMemcpyDeviceToHost, s->st));
+  // sums of the last window end, copied back with its counters
   CK(cudaStreamSynchronize(s->st));
+  const double* r = s->hw->red;
   const double c = r[8];
   const double d = c > 0 ? c : 1.0;
   out->xx = (float)(r[0] / d); out->yy = (float)(r[1] / d); out->zz = (float)(r[2] / d);
@@ -708,15 +1269,20 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     cudaEventDestroy(j);
   }
   if (ready) cudaEventDestroy(ready);
-  for (int i = 0; i < n && rc == DSM_OK; ++i)
-    if (sims[i]->flow) CK(launch_stress_reduce_dev(sims[i]->d_ens, sims[i]->d_red, s->st));
+  for (int i = 0; i < n && rc == DSM_OK; ++i) {
+    dsm_sim* q = sims[i];
+    if (q->flow) {
+      CK(launch_stress_reduce_dev(q->d_ens, q->d_red, s->st));
+      CK(cudaMemcpyAsync(q->hw->red, q->d_red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    }
+    CK(cudaMemcpyAsync(q->hw->cnt, q->d_counters, sizeof(q->hw->cnt), cudaMemcpyDeviceToHost, s->st));
+  }
   for (void* p : tmp) cudaFreeAsync(p, s->st);
   CK(cudaStreamSynchronize(s->st));
   CK(cudaGetLastError());
   if (rc != DSM_OK) return rc;
   for (int i = 0; i < n; ++i) {
-    unsigned long long cnt[4];
-    CK(cudaMemcpy(cnt, sims[i]->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    const unsigned long long* cnt = sims[i]->hw->cnt;
     if (events) events[i] = cnt[0];
     sims[i]->events_total += cnt[0];
     sims[i]->last_events = cnt[0];

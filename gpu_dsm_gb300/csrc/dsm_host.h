@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -22,6 +23,28 @@ HostPcd make_pcd(double beta, double nk);
 void make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off);
 int corr_levels_for(double t_end, double dt, int p, int m);
 
+}  // namespace dsm
+
+namespace dsm {
+// Pinned, mapped host words of one handle
+struct HostWords {
+  int abort;
+  int status;
+  unsigned long long cnt[4];
+  double red[16];
+  double pad_[3];
+};
+HostWords* host_words_take();
+void host_words_give(HostWords* w);
+void keep_pool_memory(int device);
+
+// One persistent launch of a polydisperse ensemble's size-class plan: chains
+// order[first .. first+count) with slots of cfg.slot_cap strands
+struct SizeClass {
+  LaunchCfg cfg{4, 0, 0, 32};
+  long long first = 0, count = 0;
+  int grid = 0, bps = 0;
+};
 }  // namespace dsm
 
 struct dsm_sim {
@@ -66,10 +89,34 @@ struct dsm_sim {
   double* d_red = nullptr;
   volatile int* h_abort = nullptr;
   int* d_abort = nullptr;
+  dsm::HostWords* hw = nullptr;
+  // size classes (polydisperse ensembles whose largest chains do not fit a
+  // full-occupancy slot): classes[0] large slots, classes[1] small slots, run
+  // concurrently; chains that outgrow a slot finish in the cleanup launch
+  std::vector<dsm::SizeClass> classes;
+  dsm::SizeClass cleanup;
+  int* d_order = nullptr;
+  int* d_defer = nullptr;
+  unsigned int* d_works = nullptr;  // [0] small, [1] large, [2] cleanup, [3] deferred count
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int prio = 0;  // CUDA stream priority of st and side
+  int sched_version = 0;  // bumped whenever the launch schedule changes
+  cudaEvent_t ev_done = nullptr;  // end of the last enqueued window / series, readback included
+  int pending = 0;                // asynchronous work in flight: 1 window, 2 series
+  // captured window series (dsm_advance_series / dsm_series_start): one graph
+  // per window count, buffers for ser_cap windows
+  std::vector<std::pair<int, cudaGraphExec_t>> ser_graphs;
+  int ser_cap = 0, ser_n = 0, ser_version = -1;
+  void* ser_d = nullptr;  // device: [cap end ticks][cap event caps][cap x 9 stress sums]
+  void* ser_h = nullptr;  // pinned host mirror
 };
 
 namespace dsm {
 int sim_setup(dsm_sim* s);
+// Size-class plan of a polydisperse ensemble; small_cap / big_grid / lanes
+// <= 0 pick the defaults (full-occupancy small slot, large-class grid by work share)
+int plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float margin_sd);
 int sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit);
 int sim_finish_window(dsm_sim* s, uint64_t* events);
 }  // namespace dsm

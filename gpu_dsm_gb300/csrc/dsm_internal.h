@@ -89,15 +89,30 @@ struct LaunchCfg {
 
 __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax);
 
+// Work list of one step launch.  Items are order[0 .. n) (global chain ids
+// across the launched ensembles; order == NULL: the identity over [0, total)),
+// n = *dyn_total when dyn_total is given.  With defer set, a chain whose
+// strand count reaches the slot capacity while its ensemble allows more
+// strands stops at that step boundary (state written back exactly as at a
+// window end) and its id is appended to defer, for a launch with larger slots.
+struct StepList {
+  const int* order = nullptr;
+  const unsigned int* dyn_total = nullptr;
+  int* defer = nullptr;
+  unsigned int* n_defer = nullptr;
+};
+
 // kernels (dsm_kernels.cu)
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
                         unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
-                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st);
+                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
+                        const StepList& lst = StepList{});
 int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg);
 size_t step_block_smem(const LaunchCfg& cfg);
 cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
                                  cudaStream_t st);
+cudaError_t launch_window_begin(EnsDev* d_ens, const long long* d_win, int n, int w, cudaStream_t st);
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st);
 
 }  // namespace dsm

@@ -572,38 +572,49 @@ template <bool FLOW, bool CORR, int W>
 __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict__ ens, int n_ens,
                                                  const long long* __restrict__ prefix, long long total,
                                                  unsigned int* work, int slot_cap, int pmax,
-                                                 const volatile int* abort_flag, int* status) {
+                                                 const volatile int* abort_flag, int* status, StepList lst) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Tile<W> t;
   const int lane = t.lane;
   const int tib = threadIdx.x / W;
   Slot sl = make_slot(smem + (size_t)tib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
+  const long long n_items = lst.dyn_total != nullptr ? (long long)*lst.dyn_total : total;
 
   for (;;) {
     unsigned int item = 0;
     if (lane == 0) item = atomicAdd(work, 1u);
     item = t.shfl(item, 0);
-    if ((long long)item >= total) break;
+    if ((long long)item >= n_items) break;
     if (abort_flag != nullptr && *abort_flag != 0) {
       if (lane == 0) atomicOr(status, 1);
       break;
     }
+    const long long gid = lst.order != nullptr ? (long long)lst.order[item] : (long long)item;
     int e = 0;
-    while (e + 1 < n_ens && prefix[e + 1] <= (long long)item) ++e;
+    while (e + 1 < n_ens && prefix[e + 1] <= gid) ++e;
     const EnsDev& E = ens[e];
-    const int c = (int)((long long)item - prefix[e]);
+    const int c = (int)(gid - prefix[e]);
     const int cap = E.cap;
+    // slot smaller than the ensemble's capacity: the chain may outgrow it
+    const int zlim = cap > slot_cap ? slot_cap : 0x7fffffff;
 
     // ---- load chain into the slot
     const ChainState st = E.cs[c];
+    if (st.Z > slot_cap) {  // does not fit at all: hand it to a larger slot
+      if (lane == 0) {
+        lst.defer[atomicAdd(lst.n_defer, 1u)] = (int)gid;
+        atomicAdd(&E.counters[2], 1ull);
+      }
+      continue;
+    }
     int Z = st.Z, S = st.S, stall = st.stall;
     long long T = st.T;
     uint64_t step = st.step, hash = st.hash;
     float dt_prev = st.dt_prev;
-    const long long k_next0 = st.k_next;
-    // stop at step_lim; if the watchdog cap is the tighter one, stopping there is a stall
-    const bool wd_tighter = (E.watchdog_events < E.step_limit - (long long)step);
-    const long long step_lim = wd_tighter ? (long long)step + E.watchdog_events : E.step_limit;
+    // stop at step_lim; if the watchdog cap is the tighter one, stopping there
+    // is a stall (step_lim then differs from E.step_limit)
+    const long long step_lim = (E.watchdog_events < E.step_limit - (long long)step)
+                                   ? (long long)step + E.watchdog_events : E.step_limit;
     const long long t_end = E.t_end_ticks;
     const float4* gq = E.QN + (size_t)c * cap;
     const float* gt = E.tau + (size_t)c * cap;
@@ -638,7 +649,6 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
 
     // bit0 NaN, bit1 inf, bit2 scale overflow (pending from incremental updates)
     int pend = 0;
-    const int S_stored = S;
     if (!FLOW) {
       // equilibrium keeps quantised rates in the slot; the overflow rule can
       // only lower the scale, and is kept only if an event follows (the oracle
@@ -655,7 +665,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     int cw = 1, j0 = 0;
 
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-    long long done = 0;
+    bool words = false;  // Philox words of the current batch of W events loaded
 
     for (;;) {
       // (1) flow: deformation by the previous dt (ensemble_kernel.cu:135-146)
@@ -674,13 +684,15 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       }
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
       if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W>(E, sl, Z, c, T, t);
-      // (3) reach / stall / window checks (ensemble_kernel.cu:199-207)
-      if (stall != 0 || T >= t_end || (long long)step >= step_lim) {
-        if (stall == 0 && T < t_end && wd_tighter) stall = ST_WATCHDOG;
+      // (3) reach / stall / window checks (ensemble_kernel.cu:199-207); a full
+      // slot (a creation could need strand Z+1) ends the launch for this chain
+      // at this step boundary, exactly like a window end
+      if (stall != 0 || T >= t_end || (long long)step >= step_lim || Z >= zlim) {
+        if (stall == 0 && T < t_end && (long long)step >= step_lim && step_lim != E.step_limit) stall = ST_WATCHDOG;
         dt_prev = 0.0f;
         break;
       }
-      if (abort_flag != nullptr && (done & 4095) == 4095 && *abort_flag != 0) {
+      if (abort_flag != nullptr && (step & 4095) == 4095 && *abort_flag != 0) {
         if (lane == 0) atomicOr(status, 1);
         dt_prev = 0.0f;
         break;
@@ -730,10 +742,11 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
       // (7) Philox words of this event (one evaluation per 32 events)
-      if ((step & (uint64_t)(W - 1)) == 0 || done == 0) {
+      if ((step & (uint64_t)(W - 1)) == 0 || !words) {
         const uint64_t ctr = (step & ~(uint64_t)(W - 1)) + (uint64_t)lane;
         const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
         r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
+        words = true;
       }
       const int src = (int)(step & (uint64_t)(W - 1));
       const uint32_t w0 = t.shfl(r0, src);
@@ -820,12 +833,13 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       }
       hash = (hash ^ (uint64_t)code) * 0x100000001B3ull;
       ++step;
-      ++done;
       dt_prev = dt;
     }
 
+    // stopped early because the slot is full (an abort ends the launch anyway)
+    const bool deferred = E.cap > slot_cap && Z >= slot_cap && stall == 0 && T < t_end && (long long)step < step_lim;
     // ---- flow: stress at the end of the window (ensemble_kernel.cu:504-538)
-    if (FLOW) {
+    if (FLOW && !deferred) {
       float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       for (int i = lane; i < Z; i += W) {
         const float4 q = sl.Q[i];
@@ -848,7 +862,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       }
     }
     // ---- correlator level 0 back to HBM (compensated FP32 sums -> FP64)
-    long long k_next = k_next0;
+    long long k_next = -1;  // -1: unchanged (no correlator)
     if (CORR) {
       const int p = E.corr_p;
       const size_t l0 = (size_t)c * E.corr_levels;
@@ -876,11 +890,21 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       wt[s] = (s < Z - 1) ? sl.T[s] : 0.0f;
     }
     if (lane == 0) {
+      // the launch's start values are still in HBM: events done, stored scale
       ChainState* cs = &E.cs[c];
-      cs->Z = Z; cs->S = (done > 0) ? S : S_stored; cs->stall = stall; cs->dt_prev = dt_prev;
-      cs->T = T; cs->step = step; cs->hash = hash; cs->k_next = k_next;
-      atomicAdd(&E.counters[0], (unsigned long long)done);
-      atomicAdd(&E.counters[1], 1ull);
+      const unsigned long long done = step - cs->step;
+      // a rescale at load is kept only if an event followed (as in the oracle)
+      if (done > 0) cs->S = S;
+      cs->Z = Z; cs->stall = stall; cs->dt_prev = dt_prev;
+      cs->T = T; cs->step = step; cs->hash = hash;
+      if (k_next >= 0) cs->k_next = k_next;
+      atomicAdd(&E.counters[0], done);
+      if (deferred) {
+        lst.defer[atomicAdd(lst.n_defer, 1u)] = (int)(prefix[e] + c);
+        atomicAdd(&E.counters[2], 1ull);
+      } else {
+        atomicAdd(&E.counters[1], 1ull);
+      }
     }
     t.sync();
   }
@@ -1066,6 +1090,12 @@ __global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
   if (threadIdx.x < 9) out[threadIdx.x] = red[threadIdx.x][0];
 }
 
+// Window w of a captured series: end time d_win[w] and event cap d_win[n+w]
+__global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win, int n, int w) {
+  ens->t_end_ticks = d_win[w];
+  ens->watchdog_events = d_win[n + w];
+}
+
 // ------------------------------------------------------------------ launchers
 template <bool FLOW, bool CORR, int W>
 static void* step_fn() { return (void*)k_step<FLOW, CORR, W>; }
@@ -1105,13 +1135,15 @@ size_t step_block_smem(const LaunchCfg& cfg) { return step_smem(cfg); }
 
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
                         unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
-                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st) {
+                        const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
+                        const StepList& lst) {
   const size_t sm = step_smem(cfg);
   void* fn = pick_step(flow, corr, tile_lanes(cfg));
   cudaError_t err = prep_step(fn, sm);
   if (err != cudaSuccess) return err;
+  StepList l = lst;
   void* args[] = {(void*)&d_ens, (void*)&n_ens, (void*)&d_prefix, (void*)&total, (void*)&d_work,
-                  (void*)&cfg.slot_cap, (void*)&cfg.pmax, (void*)&abort_flag, (void*)&d_status};
+                  (void*)&cfg.slot_cap, (void*)&cfg.pmax, (void*)&abort_flag, (void*)&d_status, (void*)&l};
   return cudaLaunchKernel(fn, dim3(grid), dim3(cfg.warps_per_block * 32), args, sm, st);
 }
 
@@ -1128,6 +1160,10 @@ cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, 
 cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
                                  cudaStream_t st) {
   k_gt_reduce<<<levels * p, 256, 0, st>>>(d_ens, d_gsum, d_count);
+  return cudaGetLastError();
+}
+cudaError_t launch_window_begin(EnsDev* d_ens, const long long* d_win, int n, int w, cudaStream_t st) {
+  k_window_begin<<<1, 1, 0, st>>>(d_ens, d_win, n, w);
   return cudaGetLastError();
 }
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st) {

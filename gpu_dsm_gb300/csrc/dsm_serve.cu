@@ -2,15 +2,20 @@
 //
 // A server thread admits queued requests while the device-memory budget allows
 // (their ensembles are created and initialised on the device and stay
-// resident), then repeatedly advances every active ensemble by one tick in
-// batched persistent launches (dsm_advance_batch: one launch per kind and
-// shared-memory size class, on separate streams).  A request that reaches its
-// t_end is completed (G(t) or its stress time series kept on the host), its
-// device memory released, and queued requests are admitted in its place, so
-// requests that arrive while others run share the GPU with them.  With
-// max_active = 1 the same loop is the plain one-ensemble-at-a-time form.
-// The reference runs one ensemble per process (common/main_cuda.cu); there is
-// no serving counterpart in it.
+// resident) and keeps every admitted ensemble busy on its own CUDA stream:
+// whenever one finishes a chunk of work it gets the next one at once
+// (dsm_advance_start for equilibrium requests, dsm_series_start for flow
+// requests, whose stress outputs of a chunk run as one CUDA graph replay), so
+// the kernels of all admitted requests overlap on the device and share its SMs
+// through the hardware block scheduler.  Chunks are sized so that each takes
+// about chunk_s seconds with every resident chain advancing at the same pace.
+// A request that reaches its t_end is completed (G(t) or its stress series
+// kept on the host), its device memory released, and queued requests are
+// admitted in its place.  With max_active = 1 and chunk_s < 0 the same loop is
+// the plain form: one request at a time, each equilibrium request in one
+// launch, each flow output one launch followed by a host round trip (the
+// reference's flow loop).  The reference runs one ensemble per process
+// (common/main_cuda.cu); there is no serving counterpart in it.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -37,6 +42,8 @@ using clk = std::chrono::steady_clock;
 
 enum : int32_t { RQ_QUEUED = 0, RQ_ACTIVE = 1, RQ_DONE = 2, RQ_FAILED = 3 };
 
+constexpr int kMaxSeries = 256;  // flow outputs per graph replay
+
 struct Req {
   uint64_t id = 0;
   dsm_params P{};
@@ -47,8 +54,13 @@ struct Req {
   size_t bytes = 0;
   uint64_t events = 0;
   bool flow = false, corr = false;
-  double rate = 0.0;  // kMC events per tau_K of the whole ensemble (last tick)
-  int64_t k_out = 0;  // flow: stress outputs written
+  double rate = 0.0;      // kMC events per tau_K of the whole ensemble (last chunk)
+  int64_t k_out = 0;      // flow: stress outputs written
+  int64_t n_outputs = 0;  // flow: outputs at min(t_end, k * sync_dt), k = 1..n_outputs
+  bool inflight = false;
+  double target = 0.0;    // end time of the chunk in flight
+  std::vector<double> ends;
+  std::vector<dsm_stress_plus> sbuf;
   std::vector<double> out_t;
   std::vector<dsm_stress_plus> out_s;
   std::vector<float> gt_t, gt_g;
@@ -72,220 +84,295 @@ size_t ensemble_bytes(const dsm_params& P) {
   return b + (1u << 20);
 }
 
+// time of flow output k (1-based): the same product wherever it is computed
+double output_time(const Req* r, int64_t k) { return std::min(r->P.t_end, (double)k * r->P.sync_dt); }
+
 }  // namespace
 
 struct dsm_server {
   int device = 0;
   uint64_t budget = 0, used = 0;
   int max_active = 0;
-  double tick_s = 0.05;      // target tick duration; < 0: whole-request windows
-  double rate_est = 1.0e9;   // aggregate kMC events/s of recent ticks
-  int sm_count = 152, blocks_per_sm = 4;
+  double chunk_s = 0.05;     // target duration of one chunk; < 0: whole-request windows
+  double rate_est = 1.0e9;   // aggregate kMC events/s while work is in flight
+  int prio_least = 0, prio_greatest = 0;  // CUDA stream priority range
   std::mutex mu;
-  std::condition_variable cv;
-  std::thread th;
+  std::condition_variable cv;       // request state changes (waiters)
+  std::condition_variable cv_work;  // work for the loader / finisher threads
+  std::thread th, loader, finisher;
   bool stop = false;
-  std::deque<Req*> queue;
-  std::vector<Req*> active;
+  std::deque<Req*> queue;      // submitted, not admitted
+  std::deque<Req*> to_load;    // admitted: ensemble to create and initialise
+  std::vector<Req*> loaded;    // ready to run
+  std::deque<Req*> to_finish;  // done: results to read, ensemble to release
+  std::vector<Req*> active;    // running (server thread only)
+  int resident = 0;            // admitted and not yet released
   std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
   uint64_t next_id = 1;
   uint64_t events = 0, ticks = 0, completed = 0, peak_bytes = 0;
   int peak_active = 0;
-  double busy_s = 0.0;
+  double busy_s = 0.0, setup_s = 0.0, finish_s = 0.0;
   std::string err;
 
   void run();
-  void plan_tick(std::vector<double>& targets);
-  void admit(std::vector<Req*>& fresh);
-  void finish(Req* r);
+  void load_loop();
+  void finish_loop();
+  void admit();
+  int start_chunk(Req* r, double chains_total);
+  void fail_req(Req* r, const std::string& why);
 };
 
-// Next time at which a flow request writes its stress: k*sync_dt, the last
-// one clipped to t_end (the output loop of common/main_cuda.cu)
-static double next_output(const Req* r) {
-  return std::min(r->P.t_end, (double)(r->k_out + 1) * r->P.sync_dt);
-}
-
-// Windows of one tick.  The tick's event budget B = rate_est * tick_s is
-// shared equally by the active requests (processor sharing), each capped by
-// its remaining work and by what its chains can do one after another in one
-// tick (per resident chain slot, rate_est * tick_s / min(chains, slots)):
-// water-filling, so small requests finish in few ticks and a tick stays near
-// tick_s.  Flow requests also stop at their next stress output time.
-void dsm_server::plan_tick(std::vector<double>& targets) {
-  const size_t k = active.size();
-  std::vector<double> cap(k), alloc(k);
-  double chains = 0.0;
-  for (Req* r : active) chains += r->P.n_chains;
-  const double B = rate_est * tick_s;
-  double slots = 0.0;
-  for (Req* r : active) {
-    const int lanes = r->P.lanes_per_chain > 0 ? r->P.lanes_per_chain : 32;
-    slots = std::max(slots, (double)sm_count * blocks_per_sm * (128.0 / lanes));
-  }
-  const double per_chain = B / std::max(1.0, std::min(chains, slots));
-  for (size_t i = 0; i < k; ++i) {
-    Req* r = active[i];
-    const double remaining = (r->P.t_end - r->t_cur) * r->rate;
-    cap[i] = std::min(remaining, per_chain * r->P.n_chains);
-  }
-  if (tick_s < 0) {
-    for (size_t i = 0; i < k; ++i) alloc[i] = std::numeric_limits<double>::infinity();
-  } else {
-    std::vector<size_t> ord(k);
-    for (size_t i = 0; i < k; ++i) ord[i] = i;
-    std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return cap[a] < cap[b]; });
-    double left = B;
-    size_t n_left = k;
-    for (size_t j = 0; j < k; ++j) {
-      const size_t i = ord[j];
-      const double share = left / (double)n_left;
-      alloc[i] = std::min(cap[i], share);
-      left -= alloc[i];
-      --n_left;
-    }
-  }
-  for (size_t i = 0; i < k; ++i) {
-    Req* r = active[i];
-    // at least ~4 events per chain so that a tick always makes progress
-    const double win = std::max(alloc[i], 4.0 * r->P.n_chains) / std::max(r->rate, 1.0);
-    double t = std::isfinite(win) ? r->t_cur + win : r->P.t_end;
-    t = std::min(t, r->P.t_end);
-    if (r->flow) t = std::min(t, next_output(r));
-    targets[i] = t;
-  }
-}
-
-void dsm_server::admit(std::vector<Req*>& fresh) {
+// Admission (under the lock): in arrival order while the budget and the cap on
+// resident ensembles allow; a request larger than the whole budget still runs
+// alone.  Creation and initialisation happen on the loader thread.
+void dsm_server::admit() {
   std::lock_guard<std::mutex> lk(mu);
-  while (!queue.empty() && (max_active <= 0 || (int)active.size() + (int)fresh.size() < max_active)) {
+  bool any = false;
+  while (!queue.empty() && (max_active <= 0 || resident < max_active)) {
     Req* r = queue.front();
-    const bool fits = used + r->bytes <= budget;
-    if (!fits && !(active.empty() && fresh.empty())) break;
+    if (used + r->bytes > budget && resident > 0) break;
     queue.pop_front();
     used += r->bytes;
-    fresh.push_back(r);
+    ++resident;
     peak_bytes = std::max<uint64_t>(peak_bytes, used);
-    peak_active = std::max<int>(peak_active, (int)(active.size() + fresh.size()));
+    peak_active = std::max(peak_active, resident);
+    to_load.push_back(r);
+    any = true;
+  }
+  if (any) cv_work.notify_all();
+}
+
+// Loader thread: create and initialise admitted ensembles, so that the server
+// thread never waits for SMs held by other requests' kernels
+void dsm_server::load_loop() {
+  cudaSetDevice(device);
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return stop || !to_load.empty(); });
+      if (stop) return;
+      r = to_load.front();
+      to_load.pop_front();
+    }
+    const auto t0 = clk::now();
+    dsm_sim* sim = nullptr;
+    int rc = dsm_create(&r->P, &sim);
+    if (rc == DSM_OK) rc = dsm_init_equilibrium(sim);
+    std::string why;
+    if (rc != DSM_OK) {
+      why = sim ? dsm_last_error(sim) : "dsm_create failed";
+      if (sim) dsm_destroy(sim);
+      sim = nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    setup_s += std::chrono::duration<double>(clk::now() - t0).count();
+    if (rc != DSM_OK) {
+      used -= r->bytes;
+      --resident;
+      r->state = RQ_FAILED;
+      r->err = why;
+      r->t_done = clk::now();
+      ++completed;
+      cv.notify_all();
+      continue;
+    }
+    r->sim = sim;
+    r->state = RQ_ACTIVE;
+    r->t_admit = clk::now();
+    loaded.push_back(r);
   }
 }
 
-void dsm_server::finish(Req* r) {
-  if (r->corr) {
-    int32_t n = 8192;
-    r->gt_t.assign(n, 0.f);
-    r->gt_g.assign(n, 0.f);
-    if (dsm_gt(r->sim, r->gt_t.data(), r->gt_g.data(), &n) == DSM_OK) {
-      r->gt_t.resize(n);
-      r->gt_g.resize(n);
-    } else {
-      r->gt_t.clear();
-      r->gt_g.clear();
+// Finisher thread: read results (G(t)) and release the ensemble; the request
+// completes when its results are on the host
+void dsm_server::finish_loop() {
+  cudaSetDevice(device);
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return stop || !to_finish.empty(); });
+      if (stop && to_finish.empty()) return;
+      r = to_finish.front();
+      to_finish.pop_front();
     }
+    const auto t0 = clk::now();
+    if (r->corr) {
+      int32_t n = 8192;
+      r->gt_t.assign(n, 0.f);
+      r->gt_g.assign(n, 0.f);
+      if (dsm_gt(r->sim, r->gt_t.data(), r->gt_g.data(), &n) == DSM_OK) {
+        r->gt_t.resize(n);
+        r->gt_g.resize(n);
+      } else {
+        r->gt_t.clear();
+        r->gt_g.clear();
+      }
+    }
+    dsm_destroy(r->sim);
+    r->sim = nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    finish_s += std::chrono::duration<double>(clk::now() - t0).count();
+    used -= r->bytes;
+    --resident;
+    r->t_done = clk::now();
+    r->state = RQ_DONE;
+    ++completed;
+    cv.notify_all();
   }
-  dsm_destroy(r->sim);
+}
+
+// Next chunk of r on its own stream.  Each resident chain advances by about
+// the same number of events per chunk: the chunk's share of rate_est * chunk_s
+// is the request's share of the resident chains (at least 64 events per chain).
+int dsm_server::start_chunk(Req* r, double chains_total) {
+  const double n = (double)r->P.n_chains;
+  double dtau = std::numeric_limits<double>::infinity();
+  if (chunk_s > 0.0) {
+    const double ev = std::max(rate_est * chunk_s * n / std::max(chains_total, 1.0), 64.0 * n);
+    dtau = ev / std::max(r->rate, 1.0);
+  }
+  if (r->flow) {
+    const int64_t left = r->n_outputs - r->k_out;
+    int64_t k = 1;
+    if (chunk_s > 0.0) {
+      k = (int64_t)std::floor(dtau / r->P.sync_dt);
+      k = std::max<int64_t>(1, std::min<int64_t>({k, left, kMaxSeries}));
+      int64_t p2 = 1;  // a power of two: few distinct graphs per request
+      while (p2 * 2 <= k) p2 *= 2;
+      k = p2;
+    }
+    r->ends.resize(k);
+    for (int64_t w = 0; w < k; ++w) r->ends[w] = output_time(r, r->k_out + w + 1);
+    r->sbuf.resize(k);
+    r->target = r->ends[k - 1];
+    if (chunk_s > 0.0) return dsm_series_start(r->sim, r->ends.data(), (int32_t)k);
+    return dsm_advance_start(r->sim, r->target, -1);
+  }
+  r->target = std::min(r->P.t_end, r->t_cur + dtau);
+  return dsm_advance_start(r->sim, r->target, -1);
+}
+
+void dsm_server::fail_req(Req* r, const std::string& why) {
+  if (r->sim) dsm_destroy(r->sim);
   r->sim = nullptr;
   std::lock_guard<std::mutex> lk(mu);
   used -= r->bytes;
+  --resident;
+  r->state = RQ_FAILED;
+  r->err = why;
   r->t_done = clk::now();
-  r->state = RQ_DONE;
   ++completed;
   cv.notify_all();
 }
 
 void dsm_server::run() {
   cudaSetDevice(device);
+  clk::time_point t_mark = clk::now();
+  uint64_t ev_mark = 0;
   for (;;) {
+    bool idle = false;
     {
       std::unique_lock<std::mutex> lk(mu);
       if (stop) break;
-      if (queue.empty() && active.empty()) {
+      idle = queue.empty() && loaded.empty() && active.empty();
+      if (idle && resident == 0) {
         cv.wait_for(lk, std::chrono::milliseconds(1));
+        t_mark = clk::now();
+        ev_mark = events;
         continue;
       }
     }
-    std::vector<Req*> fresh;
-    admit(fresh);
-    for (Req* r : fresh) {
-      dsm_sim* s = nullptr;
-      int rc = dsm_create(&r->P, &s);
-      if (rc == DSM_OK) rc = dsm_init_equilibrium(s);
+    admit();
+    bool changed = false;
+    {
       std::lock_guard<std::mutex> lk(mu);
-      if (rc != DSM_OK) {
-        r->err = s ? dsm_last_error(s) : "dsm_create failed";
-        if (s) dsm_destroy(s);
-        used -= r->bytes;
-        r->state = RQ_FAILED;
-        r->t_done = clk::now();
-        cv.notify_all();
-        continue;
+      if (!loaded.empty()) {
+        // keep arrival order (request ids ascend with arrival)
+        for (Req* r : loaded) active.push_back(r);
+        loaded.clear();
+        std::sort(active.begin(), active.end(), [](const Req* x, const Req* y) { return x->id < y->id; });
+        changed = true;
       }
-      r->sim = s;
-      r->state = RQ_ACTIVE;
-      r->t_admit = clk::now();
-      active.push_back(r);
     }
-    if (active.empty()) continue;
-    const size_t k = active.size();
-    std::vector<dsm_sim*> sims(k);
-    std::vector<double> targets(k);
-    plan_tick(targets);
-    for (size_t i = 0; i < k; ++i) sims[i] = active[i]->sim;
-    std::vector<uint64_t> ev(k, 0);
-    const auto t0 = clk::now();
-    const int rc = dsm_advance_batch(sims.data(), (int32_t)k, targets.data(), nullptr, ev.data());
-    const double dt_tick = std::chrono::duration<double>(clk::now() - t0).count();
-    busy_s += dt_tick;
-    ++ticks;
-    if (rc == DSM_OK) {
-      uint64_t tot = 0;
-      for (uint64_t e : ev) tot += e;
-      if (dt_tick > 0 && tot > 0) rate_est = 0.7 * rate_est + 0.3 * ((double)tot / dt_tick);
-      int32_t grid = 0, bps = 0;
-      if (dsm_last_window(sims[0], nullptr, nullptr, &grid, &bps) == DSM_OK && bps > 0) blocks_per_sm = bps;
-    }
-    if (rc != DSM_OK) {
-      std::lock_guard<std::mutex> lk(mu);
-      err = dsm_last_error(sims[0]);
-      for (Req* r : active) {
-        dsm_destroy(r->sim);
-        r->sim = nullptr;
-        used -= r->bytes;
-        r->state = RQ_FAILED;
-        r->err = err;
-        r->t_done = clk::now();
-      }
-      active.clear();
-      cv.notify_all();
-      continue;
+    // older requests on higher-priority streams: when SMs free up, the block
+    // scheduler places the oldest requests' blocks first, the younger ones
+    // fill what is left (first come, first served with backfill)
+    const int levels = prio_least - prio_greatest;
+    double chains_total = 0.0;
+    for (size_t i = 0; i < active.size(); ++i) {
+      Req* r = active[i];
+      chains_total += r->P.n_chains;
+      if (changed && !r->inflight) dsm_set_priority(r->sim, prio_greatest + std::min<int>((int)i, levels));
     }
     std::vector<Req*> still;
-    for (size_t i = 0; i < k; ++i) {
-      Req* r = active[i];
-      const double dtau = targets[i] - r->t_cur;
-      if (dtau > 0 && ev[i] > 0) r->rate = (double)ev[i] / dtau;
-      r->t_cur = targets[i];
-      r->events += ev[i];
-      events += ev[i];
-      if (r->flow && r->t_cur == next_output(r)) {
-        dsm_stress_plus sp;
-        if (dsm_stress(r->sim, &sp, nullptr) == DSM_OK) {
-          r->out_t.push_back(r->t_cur);
-          r->out_s.push_back(sp);
-        }
-        ++r->k_out;
+    bool progressed = false;
+    for (Req* r : active) {
+      if (!r->inflight) {
+        const int rc = start_chunk(r, chains_total);
+        if (rc != DSM_OK) { fail_req(r, dsm_last_error(r->sim)); progressed = true; continue; }
+        r->inflight = true;
+        ++ticks;
       }
-      if (r->t_cur >= r->P.t_end) finish(r);
-      else still.push_back(r);
+      uint64_t ev = 0;
+      int32_t nout = 0;
+      const int rc = dsm_poll(r->sim, &ev, r->flow ? r->sbuf.data() : nullptr, &nout);
+      if (rc == DSM_PENDING) { still.push_back(r); continue; }
+      progressed = true;
+      r->inflight = false;
+      if (rc != DSM_OK) { fail_req(r, dsm_last_error(r->sim)); continue; }
+      const double dtau = r->target - r->t_cur;
+      if (dtau > 0 && ev > 0) r->rate = (double)ev / dtau;
+      r->t_cur = r->target;
+      r->events += ev;
+      events += ev;
+      if (r->flow) {
+        for (int32_t w = 0; w < nout && w < (int32_t)r->ends.size(); ++w) {
+          r->out_t.push_back(r->ends[w]);
+          r->out_s.push_back(r->sbuf[w]);
+        }
+        r->k_out += (int64_t)r->ends.size();
+      }
+      if (r->t_cur >= r->P.t_end) {
+        std::lock_guard<std::mutex> lk(mu);
+        to_finish.push_back(r);
+        cv_work.notify_all();
+      } else {
+        still.push_back(r);
+      }
     }
-    active.swap(still);
+    if (still.size() != active.size()) {
+      // a request left: re-rank the others' priorities before their next chunks
+      active.swap(still);
+      for (size_t i = 0; i < active.size(); ++i)
+        if (!active[i]->inflight) dsm_set_priority(active[i]->sim, prio_greatest + std::min<int>((int)i, levels));
+    } else {
+      active.swap(still);
+    }
+    // aggregate rate over the last >= 20 ms with work in flight
+    const auto now = clk::now();
+    const double el = std::chrono::duration<double>(now - t_mark).count();
+    if (el >= 0.02) {
+      if (events > ev_mark) rate_est = 0.5 * rate_est + 0.5 * ((double)(events - ev_mark) / el);
+      if (!active.empty()) busy_s += el;
+      t_mark = now;
+      ev_mark = events;
+    }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
   // shutdown: release what is still resident
-  for (Req* r : active) if (r->sim) dsm_destroy(r->sim);
+  for (Req* r : active) {
+    if (r->sim) {
+      if (r->inflight) dsm_abort(r->sim);
+      dsm_destroy(r->sim);
+      r->sim = nullptr;
+    }
+  }
   active.clear();
 }
 
-extern "C" int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double tick_s,
+extern "C" int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double chunk_s,
                               dsm_server** out) {
   if (!out) return DSM_ERR_INVALID;
   *out = nullptr;
@@ -296,11 +383,11 @@ extern "C" int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t
   s->device = device;
   s->budget = hbm_budget_bytes > 0 ? std::min<uint64_t>(hbm_budget_bytes, fre - (fre >> 4)) : (uint64_t)(fre - (fre >> 4));
   s->max_active = max_active;
-  s->tick_s = tick_s != 0.0 ? tick_s : 0.05;
-  int sms = 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0)
-    s->sm_count = sms;
+  s->chunk_s = chunk_s != 0.0 ? chunk_s : 0.05;
+  cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest);
   s->th = std::thread([s] { s->run(); });
+  s->loader = std::thread([s] { s->load_loop(); });
+  s->finisher = std::thread([s] { s->finish_loop(); });
   *out = s;
   return DSM_OK;
 }
@@ -313,9 +400,14 @@ extern "C" int dsm_serve_submit(dsm_server* s, const dsm_params* p, uint64_t* id
   r->P.device = s->device;
   r->flow = is_flow(*p);
   r->corr = !r->flow && p->eq_type == 1 && p->sync_dt > 0 && p->t_end > 0;
+  if (r->flow) {
+    if (!(p->sync_dt > 0) || !(p->t_end > 0)) return DSM_ERR_INVALID;
+    r->n_outputs = (int64_t)std::ceil(p->t_end / p->sync_dt - 1e-9);
+    if (r->n_outputs < 1) r->n_outputs = 1;
+  }
   r->bytes = ensemble_bytes(*p);
   // prior for the events per tau_K of the ensemble (about 0.2 N_K + 2 per
-  // chain at beta = 1); replaced by the measured value after the first tick
+  // chain at beta = 1); replaced by the measured value after the first chunk
   r->rate = (0.2 * (double)p->nk + 2.0) * (double)p->n_chains;
   r->t_arrive = clk::now();
   std::lock_guard<std::mutex> lk(s->mu);
@@ -349,11 +441,9 @@ extern "C" int dsm_serve_wait_all(dsm_server* s, double timeout_s) {
   std::unique_lock<std::mutex> lk(s->mu);
   const auto dl = clk::now() + std::chrono::duration_cast<clk::duration>(std::chrono::duration<double>(timeout_s));
   for (;;) {
-    bool all = s->queue.empty() && s->active.empty();
-    if (all) {
-      for (auto& kv : s->reqs)
-        if (kv.second->state == RQ_QUEUED || kv.second->state == RQ_ACTIVE) { all = false; break; }
-    }
+    bool all = true;
+    for (auto& kv : s->reqs)
+      if (kv.second->state == RQ_QUEUED || kv.second->state == RQ_ACTIVE) { all = false; break; }
     if (all) return DSM_OK;
     if (s->cv.wait_until(lk, dl) == std::cv_status::timeout) return DSM_ERR_WATCHDOG;
   }
@@ -395,6 +485,8 @@ extern "C" int dsm_serve_stats(dsm_server* s, dsm_serve_totals* out) {
   out->completed = s->completed;
   out->peak_bytes = s->peak_bytes;
   out->peak_active = s->peak_active;
+  out->setup_s = s->setup_s;
+  out->finish_s = s->finish_s;
   return DSM_OK;
 }
 
@@ -404,7 +496,13 @@ extern "C" void dsm_serve_close(dsm_server* s) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
     s->cv.notify_all();
+    s->cv_work.notify_all();
   }
   if (s->th.joinable()) s->th.join();
+  if (s->loader.joinable()) s->loader.join();
+  if (s->finisher.joinable()) s->finisher.join();
+  // requests loaded or finishing when the server stopped
+  for (Req* r : s->loaded) if (r->sim) dsm_destroy(r->sim);
+  for (Req* r : s->to_finish) if (r->sim) dsm_destroy(r->sim);
   delete s;
 }

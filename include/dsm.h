@@ -31,6 +31,7 @@ extern "C" {
 #define DSM_ERR_MEMORY (-4)     /* device memory budget exceeded */
 #define DSM_ERR_WATCHDOG (-5)   /* a chain exceeded the per-launch event cap */
 #define DSM_ERR_NOT_BUILT (-6)  /* library built without the CUDA kernels */
+#define DSM_PENDING 1           /* dsm_poll: the asynchronous advance is still running */
 
 typedef struct dsm_float4 { float x, y, z, w; } dsm_float4;
 
@@ -73,7 +74,8 @@ typedef struct dsm_params {
   int32_t warps_per_block; /* step-kernel block size in warps; 0 = autotuned */
   int32_t s0;              /* initial fixed-point scale exponent; 0 = 40 */
   int32_t lanes_per_chain; /* 32: one chain per warp, 16: two chains per warp; 0 = auto */
-  int32_t pad_;
+  int32_t stream_priority; /* CUDA priority of the handle's streams (0 = default; lower
+                              values are scheduled first, clamped to the device's range) */
 } dsm_params;
 
 typedef struct dsm_sim dsm_sim;
@@ -116,6 +118,35 @@ int dsm_set_ext(dsm_sim* sim, const int64_t* time_ticks, const uint64_t* steps, 
 int dsm_advance(dsm_sim* sim, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
                 uint64_t* events);
 
+/* Advance through n windows of dt tau_K from the current time (window w ends
+ * at t + dt*(w+1), the times dsm_advance calls would use) as one CUDA graph
+ * launch, captured on the first call for this n and launch schedule and
+ * replayed afterwards.  Flow ensembles: out[w] (n entries, may be NULL)
+ * receives the stress at the end of window w, as dsm_stress would after each
+ * window.  Replaces the host loop of time_step_call_block +
+ * calc_stress_call_block per output time (common/main_cuda.cu flow loop,
+ * common/ensemble_call_block.cu:106-379,452-505). */
+int dsm_advance_series(dsm_sim* sim, double dt, int32_t n, const volatile int32_t* abort_flag,
+                       dsm_stress_plus* out, uint64_t* events);
+
+/* Asynchronous forms: enqueue a window (dsm_advance_start) or windows ending
+ * at t_ends[0..n) (ascending; dsm_series_start, one graph replay as in
+ * dsm_advance_series) on the handle's own stream and return at once; dsm_poll
+ * returns DSM_PENDING while it runs and, once done, the events, the stress
+ * (flow: 1 entry for a window, n for a series; may be NULL) with *n_out its
+ * count, and the status dsm_advance / dsm_advance_series would have returned.
+ * One asynchronous advance per handle at a time; handles on the same GPU run
+ * concurrently.  dsm_abort sets the handle's abort word (the running kernels
+ * stop within 4096 events per chain; dsm_poll then returns DSM_ABORTED). */
+int dsm_advance_start(dsm_sim* sim, double t_end, int64_t step_limit);
+int dsm_series_start(dsm_sim* sim, const double* t_ends, int32_t n);
+int dsm_poll(dsm_sim* sim, uint64_t* events, dsm_stress_plus* out, int32_t* n_out);
+int dsm_abort(dsm_sim* sim);
+/* Move an idle handle to streams of another CUDA priority (lower values are
+ * scheduled first; clamped to the device's range).  Used by the serving loop
+ * to favour older requests. */
+int dsm_set_priority(dsm_sim* sim, int32_t priority);
+
 /* Advance n ensembles (same device) to their own t_end[i] / step_limit[i]
  * (step_limit may be NULL) in one persistent launch per kind (equilibrium,
  * equilibrium with G(t), flow).  No counterpart in the reference, which runs
@@ -147,6 +178,40 @@ int dsm_last_window(const dsm_sim* sim, float* kernel_ms, uint64_t* events, int3
  * the disentanglement time the GUI uses to turn a Weissenberg number into a
  * shear rate, kappa_xy = Wi / tau_d (GUI/mainwindow.cpp:836). */
 int dsm_pcd(double beta, int32_t nk, double* out);
+
+/* Launch schedule of a polydisperse ensemble whose longest chains do not fit
+ * a full-occupancy shared-memory slot.  Chains are sorted by N_K and split in
+ * two size classes run as concurrent persistent launches: small slots
+ * (small_slot strands, 4 warps per block) and one warp per block with slots
+ * for the longest chains (large_grid blocks); a chain that outgrows its slot
+ * stops at a step boundary and finishes in a third launch with slots of the
+ * full capacity.  A chain goes to the small class when the mean of its
+ * equilibrium strand count plus z_margin_sd standard deviations fits the
+ * small slot.  Results do not depend on the schedule.  Arguments <= 0 choose
+ * the defaults (largest slot with 4 blocks per SM; large-class blocks in
+ * proportion to its share of the work; lanes of the handle; 5 sd).  No
+ * counterpart in the reference (one thread per chain, ensemble_kernel.cu). */
+int dsm_set_schedule(dsm_sim* sim, int32_t small_slot, int32_t large_grid, int32_t lanes, float z_margin_sd);
+/* Current schedule: n_classes (0 = one launch over all chains), then per
+ * class {slot strands, warps per block, lanes, grid, chains} in info[5*i..]
+ * (info holds 15 ints: two classes and the overflow launch, which has no
+ * fixed chain count). */
+int dsm_get_schedule(const dsm_sim* sim, int32_t* n_classes, int32_t* info);
+
+/* Autotuner (online): runs one real window of `window` tau_K with each
+ * candidate schedule (lanes per chain 32/16; the small slot at 4/3/2 blocks per
+ * SM when the strand-count bound fits it; for polydisperse ensembles the
+ * large-class grid at 1/2, 1 and 2 times its default) and keeps the one with
+ * the most kMC events per kernel millisecond.  The ensemble advances by
+ * candidates x window; its trajectory is the one it would have had without
+ * the autotuner.  best (may be NULL) receives {small_slot, large_grid, lanes,
+ * candidates}; best_ms the winner's kernel time.  No counterpart in the
+ * reference (fixed launch shapes). */
+int dsm_autotune(dsm_sim* sim, double window, int32_t* best, float* best_ms);
+
+/* Counters of the last window: kMC events, chains that completed the window
+ * in their first slot, chains moved to a larger slot on the way. */
+int dsm_window_stats(const dsm_sim* sim, uint64_t* events, uint64_t* chains_done, uint64_t* deferred);
 
 /* Correlator geometry of a simulation: levels, p, m */
 int dsm_corr_shape(const dsm_sim* sim, int32_t* levels, int32_t* p, int32_t* m);
@@ -207,20 +272,19 @@ const char* dsm_noalloc_last_error(void);
  * process through main_cuda).  A server owns a thread that admits submitted
  * requests (each a dsm_params, monodisperse) while their device memory fits
  * in hbm_budget_bytes (0: 15/16 of the free memory), keeps their ensembles
- * resident and advances every admitted one per tick in batched launches
- * (dsm_advance_batch).  Equilibrium requests with eq_type=1 produce G(t);
- * flow requests (kappa != 0) produce the stress at t = k*sync_dt up to t_end
- * (the tau.dat series).  max_active > 0 caps the ensembles resident at once
- * (1 = plain one-at-a-time serving).  tick_s: target duration of one tick in
- * seconds (0: 0.05); each tick shares the measured event rate equally among
- * the admitted requests (processor sharing, capped by each request's remaining
- * work and by what its chains can do serially in one tick).  tick_s < 0: every
- * request advances to t_end (flow: to its next output time) in one launch.
+ * resident and keeps each one busy on its own stream with chunks of about
+ * chunk_s seconds (0: 0.05), every resident chain advancing at the same pace,
+ * so that the kernels of all admitted requests overlap on the GPU.
+ * Equilibrium requests with eq_type=1 produce G(t); flow requests (kappa != 0)
+ * produce the stress at t = min(t_end, k*sync_dt), k = 1, 2, ... (the tau.dat
+ * series), a chunk of outputs per CUDA graph replay.  max_active > 0 caps the
+ * ensembles resident at once; max_active = 1 with chunk_s < 0 is the plain
+ * form (one request at a time, one launch per request or flow output).
  * --------------------------------------------------------------------- */
 typedef struct dsm_server dsm_server;
 enum { DSM_REQ_QUEUED = 0, DSM_REQ_ACTIVE = 1, DSM_REQ_DONE = 2, DSM_REQ_FAILED = 3 };
 
-int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double tick_s,
+int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double chunk_s,
                    dsm_server** out);
 /* Queue a request; *id identifies it.  DSM_ERR_MEMORY if it can never fit. */
 int dsm_serve_submit(dsm_server* srv, const dsm_params* params, uint64_t* id);
@@ -236,12 +300,14 @@ int dsm_serve_result_stress(dsm_server* srv, uint64_t id, double* t, dsm_stress_
 /* Totals since dsm_serve_open */
 typedef struct dsm_serve_totals {
   uint64_t events;       /* kMC events of all requests */
-  double busy_s;         /* seconds inside batched advances */
-  uint64_t ticks;        /* batched advances */
+  double busy_s;         /* seconds with work in flight */
+  uint64_t ticks;        /* chunks launched */
   uint64_t completed;    /* requests finished (done or failed) */
   uint64_t peak_bytes;   /* most device memory admitted at once */
   int32_t peak_active;   /* most ensembles resident at once */
   int32_t pad_;
+  double setup_s;        /* host seconds creating and initialising admitted ensembles */
+  double finish_s;       /* host seconds reading results and releasing ensembles */
 } dsm_serve_totals;
 int dsm_serve_stats(dsm_server* srv, dsm_serve_totals* out);
 /* Stop the server thread and release every resident ensemble */

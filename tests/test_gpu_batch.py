@@ -37,3 +37,34 @@ def test_batch_equals_separate(dsm_mod, oracle_mod):
     o.run(12.5)
     o.run(40.0)
     assert_bitexact(gpu_state(batch[1]), o.get_state(), what="batch vs oracle")
+
+
+def test_async_handles_overlap(dsm_mod, oracle_mod):
+    """Windows and graph series enqueued on several handles at once (each on
+    its own stream) and polled give the synchronous results."""
+    import time
+
+    kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    specs = [dict(nk=30, n_chains=400, seed=3), dict(nk=45, n_chains=300, kappa=kap, seed=3, stream=1)]
+    a = [dsm_mod.Ensemble(**s) for s in specs]
+    b = [dsm_mod.Ensemble(**s) for s in specs]
+    for e in a + b:
+        e.init_equilibrium()
+    a[0].advance_start(20.0)
+    a[1].series_start([4.0, 8.0, 12.0])
+    res = [None, None]
+    t0 = time.time()
+    while any(r is None for r in res) and time.time() - t0 < 60:
+        for i in range(2):
+            if res[i] is None:
+                res[i] = a[i].poll()
+    ev0 = b[0].advance(20.0)
+    st1 = []
+    ev1 = 0
+    for t in (4.0, 8.0, 12.0):
+        ev1 += b[1].advance(t)
+        st1.append(b[1].stress()[0])
+    assert res[0][0] == ev0 and res[1][0] == ev1
+    assert np.array_equal(res[1][1], np.array(st1, np.float32))
+    for x, y in zip(a, b):
+        assert_bitexact(gpu_state(x), gpu_state(y), what="async vs sync")

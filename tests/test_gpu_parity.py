@@ -16,9 +16,12 @@ def test_init_bitexact(dsm_mod, oracle_mod):
     assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "S", "T", "step"), what="init")
 
 
+@pytest.mark.parametrize("lanes", [0, 32])
 @pytest.mark.parametrize("nk,n,steps", [(25, 1024, 3000), (200, 128, 4000), (3, 64, 500), (1, 16, 200)])
-def test_fixed_steps_bitexact(dsm_mod, oracle_mod, nk, n, steps):
-    g, o = pair(dsm_mod, oracle_mod, nk=nk, n=n, seed=7)
+def test_fixed_steps_bitexact(dsm_mod, oracle_mod, nk, n, steps, lanes):
+    """Default schedule (equilibrium: 16 lanes per chain, small slots) and one
+    warp per chain give the oracle's states after a fixed event count."""
+    g, o = pair(dsm_mod, oracle_mod, nk=nk, n=n, seed=7, lanes=lanes)
     g.init_equilibrium()
     o.init_equilibrium()
     ev = g.advance(1.0e9, step_limit=steps)
@@ -158,3 +161,104 @@ def test_two_chains_per_warp_correlator(dsm_mod, oracle_mod):
     assert np.array_equal(gc, oc)
     mask = oc > 0
     assert (np.abs(gs[mask] - os_[mask]) / np.abs(os_[mask]).max()).max() < 1e-5
+
+
+def _lognormal_nk(n, seed, mean, sd, lo, hi):
+    rng = np.random.default_rng(seed)
+    return np.clip(np.round(np.exp(rng.normal(np.log(mean), sd, size=n))), lo, hi).astype(np.int32)
+
+
+@pytest.mark.parametrize("small_slot,margin,kappa", [
+    (0, 0.0, (0.0,) * 9),
+    (40, 0.01, (0.0,) * 9),
+    (40, 0.01, (0.0, 1.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)),
+])
+def test_size_classes_bitexact(dsm_mod, oracle_mod, small_slot, margin, kappa):
+    """Polydisperse chains up to N_K=1200 in size classes (large slots, small
+    slots, overflow launch for chains that outgrow theirs) give the oracle's
+    trajectories exactly, whatever the schedule."""
+    nkc = _lognormal_nk(400, 21, 120, 0.9, 10, 1200)
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=400, seed=17, nk_chain=nkc, kappa=kappa)
+    if small_slot:
+        g.set_schedule(small_slot=small_slot, z_margin_sd=margin)
+    sch = g.schedule()
+    assert len(sch) == 3 and sch[0]["warps_per_block"] == 1 and sch[1]["warps_per_block"] == 4
+    assert sch[0]["chains"] + sch[1]["chains"] == 400
+    g.init_equilibrium()
+    o.init_equilibrium()
+    deferred = 0
+    for t in (4.0, 10.0):
+        g.advance(t)
+        o.run(t)
+        deferred += g.window_stats()["deferred"]
+    st = gpu_state(g)
+    assert np.all(st["QN"][:, :, 3].sum(axis=1) == nkc)
+    assert_bitexact(st, o.get_state(), what=f"size classes slot={small_slot}")
+    if small_slot:
+        assert deferred > 0  # the overflow launch ran
+    if any(kappa):
+        sg, cg = g.stress()
+        so, co = o.stress()
+        assert cg == co
+        scale = np.abs(so[:6]).max() + 1e-6
+        assert np.all(np.abs(sg[:6] - so[:6]) <= 1e-4 * scale + 1e-6)
+
+
+def test_autotune_keeps_trajectory(dsm_mod, oracle_mod):
+    """The autotuner's trial windows are ordinary windows under different
+    schedules: the run stays on the oracle's trajectory."""
+    nkc = _lognormal_nk(300, 5, 150, 0.64, 10, 900)
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=300, seed=23, nk_chain=nkc, corr=True, sync_dt=1.0,
+                t_end=20.0, corr_p=16, corr_m=2)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(3.0)
+    best = g.autotune(0.5)
+    assert best["lanes"] in (16, 32) and best["candidates"] >= 2 and best["kernel_ms"] > 0
+    assert g.get_ext()["T"].min() >= (3.0 + 0.5 * best["candidates"]) * 2.0 ** 32 - 1
+    g.advance(15.0)
+    o.run(15.0)
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash"), what="after autotune")
+    gs, gc = g.gt_raw()
+    os_, oc = o.gt_raw()
+    assert np.array_equal(gc, oc)
+    mask = oc > 0
+    assert (np.abs(gs[mask] - os_[mask]) / np.abs(os_[mask]).max()).max() < 1e-5
+
+
+def test_graph_series_equals_windows(dsm_mod, oracle_mod):
+    """n windows replayed from one captured CUDA graph equal n dsm_advance
+    calls (state bit for bit, stress after every window) and the oracle."""
+    kap = (0.0, 3.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    spec = dict(nk=40, n_chains=300, kappa=kap, seed=29)
+    a = dsm_mod.Ensemble(**spec)
+    b = dsm_mod.Ensemble(**spec)
+    o = oracle_mod.Oracle(**spec)
+    for x in (a, b, o):
+        x.init_equilibrium()
+    sa = []
+    for w in range(1, 6):
+        a.advance(2.5 * w)
+        sa.append(a.stress()[0])
+    ev1, sb = b.advance_series(2.5, 5)
+    assert np.array_equal(np.array(sa, np.float32), sb)
+    assert_bitexact(gpu_state(b), gpu_state(a), what="series vs windows")
+    o.run(12.5)
+    assert_bitexact(gpu_state(b), o.get_state(), what="series vs oracle")
+    # replay of the same graph for the next 5 windows
+    for w in range(6, 11):
+        a.advance(2.5 * w)
+    ev2, sb2 = b.advance_series(2.5, 5)
+    assert ev2 > 0 and np.array_equal(sb2[-1], a.stress()[0].astype(np.float32))
+    assert_bitexact(gpu_state(b), gpu_state(a), what="series replay")
+
+
+def test_graph_series_size_classes(dsm_mod, oracle_mod):
+    nkc = _lognormal_nk(300, 31, 150, 0.64, 10, 900)
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=300, seed=37, nk_chain=nkc)
+    g.set_schedule(small_slot=48, z_margin_sd=0.01)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    ev, _ = g.advance_series(1.5, 4)
+    assert ev == o.run(6.0)
+    assert_bitexact(gpu_state(g), o.get_state(), what="series with size classes")
