@@ -395,10 +395,10 @@ def prior_events(r) -> float:
     return (0.2 * r["nk"] + 2.0) * r["n_chains"] * r["t_end"]
 
 
-def serve_once(reqs, arrivals, *, max_active, chunk_s, device):
+def serve_once(reqs, arrivals, *, max_active, chunk_s, device, policy="fcfs"):
     import gpu_dsm_gb300 as dsm
 
-    srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s)
+    srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s, policy=policy)
     ids = []
     t0 = time.perf_counter()
     for r, a in zip(reqs, arrivals):
@@ -410,8 +410,12 @@ def serve_once(reqs, arrivals, *, max_active, chunk_s, device):
     wall = time.perf_counter() - t0
     st = [srv.status(i) for i in ids]
     out = []
-    for r, i in zip(reqs, ids):
+    for r, i, x in zip(reqs, ids, st):
+        if x["state"] != dsm.api.REQ_DONE:
+            out.append(np.zeros(0, np.float32))
+            continue
         out.append(srv.result_gt(i)[1] if r.get("eq_type") == 1 else srv.result_stress(i)[1])
+    errors = sorted({x.get("error", "") for x in st if x["state"] != dsm.api.REQ_DONE})
     tot = srv.stats()
     srv.close()
     lat = np.array([x["latency_s"] for x in st])
@@ -419,7 +423,7 @@ def serve_once(reqs, arrivals, *, max_active, chunk_s, device):
     ev = sum(x["events"] for x in st)
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "events_per_s": ev / wall, "makespan_s": wall, "events": int(ev),
-            "failed": failed, "chunks": tot["chunks"], "peak_active": tot["peak_active"],
+            "failed": failed, "errors": errors[:5], "chunks": tot["chunks"], "peak_active": tot["peak_active"],
             "peak_bytes": tot["peak_bytes"], "busy_s": tot["busy_s"], "setup_s": tot["setup_s"],
             "finish_s": tot["finish_s"]}, out
 
@@ -440,14 +444,21 @@ def run_serve(args, device: int = 0) -> dict:
     rng = np.random.default_rng(11)
     arrivals = np.cumsum(rng.exponential(1.0 / lam, size=len(reqs)))
     arrivals -= arrivals[0]
-    served, out_s = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device)
+    served, out_s = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device, policy="fcfs")
     plain, out_p = serve_once(reqs, arrivals, max_active=1, chunk_s=-1.0, device=device)
+    equal = None
+    if args.serve_equal_pace:
+        equal, _ = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device,
+                              policy="equal_pace")
     err = 0.0
     for r, a, b in zip(reqs, out_s, out_p):
         if r.get("eq_type") == 1 and len(a) and len(b):
             err = max(err, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)))
     return {"requests": len(reqs), "t_end_scale": args.serve_scale, "arrival_rate_per_s": lam,
             "offered_load_vs_plain": 1.2, "chunk_s": args.serve_chunk, "served": served, "plain": plain,
+            "served_equal_pace": equal,
+            "policies": "served: first come first served with backfill (stream priority by age); "
+                        "plain: one request at a time, one launch per request / flow output",
             "p99_speedup": plain["p99_s"] / served["p99_s"], "p50_speedup": plain["p50_s"] / served["p50_s"],
             "throughput_ratio": served["events_per_s"] / plain["events_per_s"],
             "gt_max_rel_diff_served_vs_plain": err,
@@ -476,6 +487,7 @@ def main():
     ap.add_argument("--serve-cal", type=int, default=16)
     ap.add_argument("--serve-scale", type=float, default=1.0e-3, help="t_end multiplier of the request stream")
     ap.add_argument("--serve-chunk", type=float, default=0.05, help="target chunk duration of the served form (s)")
+    ap.add_argument("--serve-equal-pace", action="store_true", help="also run the equal-pace serving policy")
     args = ap.parse_args()
     global N_CHAINS
     N_CHAINS = args.chains

@@ -15,8 +15,9 @@ from .api import (  # noqa: F401
     advance_batch,
     lib_path,
     load_library,
+    gex_tables,
     make_params,
     pcd,
 )
 
-__all__ = ["DSMError", "Ensemble", "Server", "StressPlus", "advance_batch", "lib_path", "load_library", "make_params", "pcd"]
+__all__ = ["DSMError", "Ensemble", "Server", "StressPlus", "advance_batch", "lib_path", "load_library", "make_params", "pcd", "gex_tables"]

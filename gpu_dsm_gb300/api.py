@@ -51,6 +51,10 @@ class DsmParams(C.Structure):
         ("s0", C.c_int32),
         ("lanes_per_chain", C.c_int32),
         ("stream_priority", C.c_int32),
+        ("gex_a", C.c_float),
+        ("gex_b", C.c_float),
+        ("gex_mp", C.c_float),
+        ("gex_mk", C.c_float),
     ]
 
 
@@ -122,12 +126,20 @@ def load_library() -> C.CDLL:
         getattr(lib, fn).restype = C.c_int
     lib.dsm_autotune.argtypes = [vp, C.c_double, vp, C.POINTER(C.c_float)]
     lib.dsm_autotune.restype = C.c_int
+    lib.dsm_zn_hist.argtypes = [vp, vp, i32, vp, i32]
+    lib.dsm_zn_hist.restype = C.c_int
+    lib.dsm_q_sorted.argtypes = [vp, vp, C.POINTER(i64)]
+    lib.dsm_q_sorted.restype = C.c_int
+    lib.dsm_get_r1.argtypes = [vp, vp]
+    lib.dsm_get_r1.restype = C.c_int
     lib.dsm_window_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
     lib.dsm_window_stats.restype = C.c_int
     lib.dsm_set_schedule.argtypes = [vp, i32, i32, i32, C.c_float]
     lib.dsm_set_schedule.restype = C.c_int
     lib.dsm_get_schedule.argtypes = [vp, C.POINTER(i32), vp]
     lib.dsm_get_schedule.restype = C.c_int
+    lib.dsm_gex_table.argtypes = [C.c_float] * 4 + [C.c_double, vp, C.POINTER(i32), vp, C.POINTER(i32), vp]
+    lib.dsm_gex_table.restype = C.c_int
     lib.dsm_pcd.argtypes = [C.c_double, i32, vp]
     lib.dsm_pcd.restype = C.c_int
     lib.dsm_serve_open.argtypes = [i32, u64, i32, C.c_double, C.POINTER(vp)]
@@ -138,6 +150,10 @@ def load_library() -> C.CDLL:
     lib.dsm_serve_result_gt.argtypes = [vp, u64, vp, vp, C.POINTER(i32)]
     lib.dsm_serve_result_stress.argtypes = [vp, u64, vp, vp, C.POINTER(i32)]
     lib.dsm_serve_stats.argtypes = [vp, C.POINTER(ServeTotals)]
+    lib.dsm_serve_set_policy.argtypes = [vp, i32]
+    lib.dsm_serve_set_policy.restype = C.c_int
+    lib.dsm_serve_error.argtypes = [vp, u64]
+    lib.dsm_serve_error.restype = C.c_char_p
     lib.dsm_serve_close.argtypes = [vp]
     lib.dsm_serve_close.restype = None
     for fn in ("dsm_init_equilibrium", "dsm_set_chains", "dsm_get_chains", "dsm_get_ext", "dsm_set_ext",
@@ -162,11 +178,29 @@ def pcd(beta: float, nk: int) -> dict:
     return dict(zip(("alpha", "tau_0", "tau_max", "tau_d", "g", "normdt"), out.tolist()))
 
 
+def gex_tables(a: float, b: float, mp: float, mk: float, beta: float) -> dict:
+    """GEX background tables the library builds for pd_flag = 1 (dsm_gex_table):
+    M/mp and CD-weighted inverse tables, their steps, mp/Mk and the CD creation
+    prefactor (common/gamma.cpp:174-263, common/ensemble.cu:137-146)."""
+    lib = load_library()
+    cap = 4_000_000
+    m, md = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+    n, nd = C.c_int32(cap), C.c_int32(cap)
+    info = np.zeros(3, np.float64)
+    rc = lib.dsm_gex_table(a, b, mp, mk, beta, _ptr(m), C.byref(n), _ptr(md), C.byref(nd), _ptr(info))
+    if rc != DSM_OK:
+        raise DSMError(rc, "dsm_gex_table")
+    return {"M": m[: n.value].copy(), "Md": md[: nd.value].copy(), "step": float(info[0]),
+            "step_d": float(info[1]), "scale": float(np.float32(mp) / np.float32(mk)), "prefact": float(info[2])}
+
+
 def make_params(*, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[float] = (0.0,) * 9,
                 cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
                 device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
-                stream: int = 0, warps_per_block: int = 0, s0: int = 0, lanes_per_chain: int = 0) -> DsmParams:
-    """dsm_params of a monodisperse ensemble (input.dat fields, common/main_cuda.cu:55-68)."""
+                stream: int = 0, warps_per_block: int = 0, s0: int = 0, lanes_per_chain: int = 0,
+                gex: Optional[Sequence[float]] = None) -> DsmParams:
+    """dsm_params of an ensemble (input.dat fields, common/main_cuda.cu:55-68).
+    gex = (a, b, mp, Mk) of polydisp.dat switches on the GEX background (pd_flag 1)."""
     p = DsmParams()
     p.beta = beta
     p.nk = nk
@@ -174,7 +208,9 @@ def make_params(*, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[fl
     for i, k in enumerate(kappa):
         p.kappa[i] = k
     p.cd_flag = cd_flag
-    p.pd_flag = 0
+    p.pd_flag = 0 if gex is None else 1
+    if gex is not None:
+        p.gex_a, p.gex_b, p.gex_mp, p.gex_mk = (float(v) for v in gex)
     p.eq_type = eq_type
     p.sync_dt = sync_dt
     p.t_end = t_end
@@ -205,13 +241,13 @@ class Ensemble:
                  cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
                  device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
                  stream: int = 0, nk_chain: Optional[np.ndarray] = None, warps_per_block: int = 0, s0: int = 0,
-                 lanes_per_chain: int = 0):
+                 lanes_per_chain: int = 0, gex: Optional[Sequence[float]] = None):
         self._lib = load_library()
         self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
         p = make_params(beta=beta, nk=nk, n_chains=n_chains, kappa=kappa, cd_flag=cd_flag, eq_type=eq_type,
                         sync_dt=sync_dt, t_end=t_end, seed=seed, device=device, z_max=z_max, corr_p=corr_p,
                         corr_m=corr_m, corr_levels=corr_levels, stream=stream, warps_per_block=warps_per_block,
-                        s0=s0, lanes_per_chain=lanes_per_chain)
+                        s0=s0, lanes_per_chain=lanes_per_chain, gex=gex)
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
         self.params = p
         self.n_chains = n_chains
@@ -370,6 +406,25 @@ class Ensemble:
         return {"small_slot": int(best[0]), "large_grid": int(best[1]), "lanes": int(best[2]),
                 "candidates": int(best[3]), "kernel_ms": ms.value}
 
+    def distributions(self):
+        """Device-computed statistics of the -distr files: (Z histogram over
+        chains, N histogram over strands, sorted |Q| of the internal strands)."""
+        nb = self.z_max + 2
+        hz = np.zeros(nb, np.uint64)
+        hn = np.zeros(max(nb, self.nk + 2), np.uint64)
+        self._check(self._lib.dsm_zn_hist(self._h, _ptr(hz), nb, _ptr(hn), len(hn)))
+        n = C.c_int64(0)
+        self._check(self._lib.dsm_q_sorted(self._h, None, C.byref(n)))
+        q = np.zeros(max(1, n.value), np.float32)
+        self._check(self._lib.dsm_q_sorted(self._h, _ptr(q), C.byref(n)))
+        return hz, hn, q[: n.value]
+
+    def r1(self) -> np.ndarray:
+        """MSD mode (eq_type=2): first-entanglement position of every chain, (n, 3)."""
+        out = np.zeros((self.n_chains, 3), np.float32)
+        self._check(self._lib.dsm_get_r1(self._h, _ptr(out)))
+        return out
+
     def window_stats(self) -> dict:
         """Counters of the last window: events, chains done in their first slot, chains deferred."""
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
@@ -424,13 +479,19 @@ class Server:
     time, one launch per request (equilibrium) or per output (flow).
     """
 
-    def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_s: float = 0.0):
+    POLICIES = {"fcfs": 0, "equal_pace": 1}
+
+    def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_s: float = 0.0,
+                 policy: str = "fcfs"):
         self._lib = load_library()
         h = C.c_void_p()
         rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, chunk_s, C.byref(h))
         if rc != DSM_OK:
             raise DSMError(rc, "dsm_serve_open")
         self._h = h
+        rc = self._lib.dsm_serve_set_policy(h, self.POLICIES[policy])
+        if rc != DSM_OK:
+            raise DSMError(rc, "dsm_serve_set_policy")
         self.device = device
 
     def submit(self, **kw) -> int:
@@ -447,7 +508,10 @@ class Server:
         rc = self._lib.dsm_serve_status(self._h, rid, C.byref(st), C.byref(lat), C.byref(q), C.byref(ev))
         if rc != DSM_OK:
             raise DSMError(rc, "dsm_serve_status")
-        return {"state": st.value, "latency_s": lat.value, "queue_s": q.value, "events": ev.value}
+        d = {"state": st.value, "latency_s": lat.value, "queue_s": q.value, "events": ev.value}
+        if st.value == REQ_FAILED:
+            d["error"] = self._lib.dsm_serve_error(self._h, rid).decode()
+        return d
 
     def wait_all(self, timeout_s: float = 3600.0) -> None:
         rc = self._lib.dsm_serve_wait_all(self._h, timeout_s)

@@ -37,58 +37,43 @@ int read_input(const char* path, InputDat* in) {
   return DSM_OK;
 }
 
-// common/ensemble.cu:356-392
-static void write_Z_distr(const std::string& fn, const std::vector<dsm_chain_head>& h, bool cumulative) {
+// common/ensemble.cu:394-431, from the device histogram of N over all strands
+static void write_N_distr(const std::string& fn, const std::vector<uint64_t>& hist, bool cumulative) {
   std::ofstream f(fn);
   if (!f) { std::cout << "file error\n"; return; }
-  int zmin = h[0].Z, zmax = h[0].Z;
-  for (auto& c : h) { zmin = std::min(zmin, c.Z); zmax = std::max(zmax, c.Z); }
-  const size_t n = h.size();
-  for (int j = zmin; j <= zmax; ++j) {
-    size_t cnt = 0;
-    for (auto& c : h) cnt += cumulative ? (c.Z <= j) : (c.Z == j);
-    f << j << "\t" << (float)cnt / (float)n << "\n";
-  }
-}
-
-// common/ensemble.cu:394-431
-static void write_N_distr(const std::string& fn, const std::vector<dsm_chain_head>& h,
-                          const std::vector<dsm_float4>& q, int cap, bool cumulative) {
-  std::ofstream f(fn);
-  if (!f) { std::cout << "file error\n"; return; }
-  int nmin = (int)q[0].w, nmax = (int)q[0].w;
-  long long nstr = 0;
-  for (size_t i = 0; i < h.size(); ++i) {
-    for (int j = 0; j < h[i].Z; ++j) {
-      const int v = (int)q[i * cap + j].w;
-      nmin = std::min(nmin, v); nmax = std::max(nmax, v);
-      if (v == 0) std::cout << "Zero length strand in chain " << i << ", #" << j << "\n";
-    }
-    nstr += h[i].Z;
-  }
-  std::vector<long long> hist(nmax + 2, 0);
-  for (size_t i = 0; i < h.size(); ++i)
-    for (int j = 0; j < h[i].Z; ++j) hist[(int)q[i * cap + j].w]++;
-  long long run = 0;
-  for (int n = nmin; n <= nmax; ++n) {
+  int nmin = -1, nmax = -1;
+  unsigned long long nstr = 0;
+  for (size_t n = 0; n < hist.size(); ++n)
+    if (hist[n]) { if (nmin < 0) nmin = (int)n; nmax = (int)n; nstr += hist[n]; }
+  if (hist.size() > 0 && hist[0]) std::cout << "Zero length strands: " << hist[0] << "\n";
+  unsigned long long run = 0;
+  for (int n = nmin; n >= 0 && n <= nmax; ++n) {
     run += hist[n];
-    const long long cnt = cumulative ? run : hist[n];
+    const unsigned long long cnt = cumulative ? run : hist[n];
     f << n << "\t" << (float)cnt / (float)nstr << "\n";
   }
 }
 
-// common/ensemble.cu:439-484 (cumulative |Q| distribution of internal strands)
-static void write_Q_distr(const std::string& fn, const std::vector<dsm_chain_head>& h,
-                          const std::vector<dsm_float4>& q, int cap) {
+// common/ensemble.cu:356-392, from the device histogram of Z over chains
+static void write_Z_distr(const std::string& fn, const std::vector<uint64_t>& hist, int n_chains, bool cumulative) {
   std::ofstream f(fn);
   if (!f) { std::cout << "file error\n"; return; }
-  std::vector<float> Q;
-  for (size_t i = 0; i < h.size(); ++i)
-    for (int j = 1; j < h[i].Z - 1; ++j) {
-      const dsm_float4 v = q[i * cap + j];
-      Q.push_back(std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
-    }
-  std::sort(Q.begin(), Q.end());
+  int zmin = -1, zmax = -1;
+  for (size_t z = 0; z < hist.size(); ++z)
+    if (hist[z]) { if (zmin < 0) zmin = (int)z; zmax = (int)z; }
+  unsigned long long run = 0;
+  for (int j = zmin; j >= 0 && j <= zmax; ++j) {
+    run += hist[j];
+    const unsigned long long cnt = cumulative ? run : hist[j];
+    f << j << "\t" << (float)cnt / (float)n_chains << "\n";
+  }
+}
+
+// common/ensemble.cu:439-484: cumulative distribution of |Q| of the internal
+// strands, every 10th of the sorted lengths (sorted on the device)
+static void write_Q_distr(const std::string& fn, const std::vector<float>& Q) {
+  std::ofstream f(fn);
+  if (!f) { std::cout << "file error\n"; return; }
   const size_t n = Q.size();
   std::vector<float> P(n);
   for (size_t i = 0; i < n; ++i) {
@@ -100,15 +85,20 @@ static void write_Q_distr(const std::string& fn, const std::vector<dsm_chain_hea
 }
 
 int write_distributions(dsm_sim* sim, int n_chains, int cap, bool cd_flag) {
-  std::vector<dsm_chain_head> h(n_chains);
-  std::vector<dsm_float4> q((size_t)n_chains * cap);
-  int rc = dsm_get_chains(sim, h.data(), q.data(), nullptr);
+  std::vector<uint64_t> hz((size_t)cap + 2), hn((size_t)cap + 2);
+  int rc = dsm_zn_hist(sim, hz.data(), (int32_t)hz.size(), hn.data(), (int32_t)hn.size());
+  if (rc) return rc;
+  int64_t nq = 0;
+  rc = dsm_q_sorted(sim, nullptr, &nq);
+  if (rc) return rc;
+  std::vector<float> Q((size_t)nq);
+  rc = dsm_q_sorted(sim, Q.data(), &nq);
   if (rc) return rc;
   // common/main_cuda.cu:169-180
   const std::string sfx = cd_flag ? "" : "_";
-  write_Z_distr("distr_Z" + sfx + ".dat", h, false);
-  write_N_distr("distr_N" + sfx + ".dat", h, q, cap, false);
-  write_Q_distr("distr_Q" + sfx + ".dat", h, q, cap);
+  write_Z_distr("distr_Z" + sfx + ".dat", hz, n_chains, false);
+  write_N_distr("distr_N" + sfx + ".dat", hn, false);
+  write_Q_distr("distr_Q" + sfx + ".dat", Q);
   return DSM_OK;
 }
 
@@ -136,6 +126,14 @@ extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadf
   p.sync_dt = in.sync_dt; p.t_end = in.t_end;
   p.seed = (uint64_t)(uint32_t)job_ID;
   p.device = device_ID;
+  if (in.pd_flag) {
+    // GEX background: polydisp.dat holds a, b, mp, Mk (main_cuda.cu:95-103)
+    std::ifstream pf("polydisp.dat");
+    if (!(pf >> p.gex_a >> p.gex_b >> p.gex_mp >> p.gex_mk)) {
+      std::cout << "cannot read polydisp.dat\n";
+      return DSM_ERR_INVALID;
+    }
+  }
   const bool flow = std::any_of(in.kappa, in.kappa + 9, [](float k) { return k != 0.0f; });
   const int s_levels = (int)std::ceil(std::log(in.t_end / in.sync_dt / 64.0) / std::log(8.0)) + 1;
 
@@ -196,8 +194,11 @@ extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadf
       if (progress_bar) *progress_bar = (int)(100.0 * (t_step + in.sync_dt) / in.t_end);
     }
     std::cout << "time evolution done.\n";
-  } else if (in.eq_type == 1) {
-    std::cout << "G(t) calc...\n";
+  } else if (in.eq_type == 1 || in.eq_type == 2) {
+    // G(t) (correlator of the shear stresses) or MSD(t) (centre of mass), same
+    // correlator and window loop (ensemble.cu:289-339, main_cuda.cu:136-156)
+    const bool msd = in.eq_type == 2;
+    std::cout << (msd ? "MSD(t) calc...\n" : "G(t) calc...\n");
     if (progress_bar) *progress_bar = 1;
     // windows of at most 1e5 tau_K (max_sync_interval, ensemble_call_block.cu:24)
     const double win = std::max(in.sync_dt, 1.0e5);
@@ -215,14 +216,12 @@ extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadf
     std::vector<float> tt(n), gg(n);
     rc = dsm_gt(sim, tt.data(), gg.data(), &n);
     if (rc != DSM_OK) { std::cout << dsm_last_error(sim) << "\n"; dsm_destroy(sim); return rc; }
-    std::ofstream gf(filename_ID("G", job_ID));
+    std::ofstream gf(filename_ID(msd ? "MSD" : "G", job_ID));
     std::cout << "\n";
     for (int j = 0; j < n; ++j) {
       std::cout << tt[j] << '\t' << gg[j] << '\n';
       gf << tt[j] << '\t' << gg[j] << '\n';
     }
-  } else if (in.eq_type == 2) {
-    std::cout << "MSD(t) calculation is not available in this build\n";
   } else {
     std::cout << "There are no flow and no equilibrium quantity to calculate. Exiting... \n";
   }

@@ -190,7 +190,8 @@ extern "C" int dsm_create(const dsm_params* p, dsm_sim** out) {
 int dsm::sim_setup(dsm_sim* s) {
   dsm_params& P = s->P;
   if (P.nk < 1 || P.n_chains < 1 || !(P.beta > 0.0f)) return fail(s, DSM_ERR_INVALID, "invalid nk / n_chains / beta");
-  if (P.pd_flag != 0) return fail(s, DSM_ERR_INVALID, "GEX background polydispersity (pd_flag=1) is not supported");
+  if (P.pd_flag != 0 && P.nk_chain != nullptr)
+    return fail(s, DSM_ERR_INVALID, "GEX background (pd_flag=1) with per-chain N_K is not supported");
   s->flow = is_flow(P.kappa);
   s->cap = P.z_max > 0 ? P.z_max : P.nk;
   if (s->cap < 1) return fail(s, DSM_ERR_INVALID, "z_max");
@@ -219,10 +220,19 @@ int dsm::sim_setup(dsm_sim* s) {
     double acc = 0.0;
     for (int v : s->nk_chain) acc += normdt[v];
     s->prefact = (float)((acc / P.n_chains) / be);
+  } else if (P.pd_flag != 0) {
+    // GEX background: partner masses from the inverse tables, CD creation
+    // prefactor averaged over the background law (ensemble.cu:137-146)
+    const int rc = make_gex_table(P.gex_a, P.gex_b, P.gex_mp, P.gex_mk, be, &s->gex);
+    if (rc != DSM_OK) return fail(s, DSM_ERR_INVALID, "invalid GEX parameters (polydisp.dat a b mp Mk)");
+    s->prefact = (float)s->gex.prefact;
   } else {
     s->prefact = (float)(s->pcd.normdt / be);  // ensemble.cu:148
   }
-  s->corr = (!s->flow) && P.eq_type == 1 && P.sync_dt > 0 && P.t_end > 0;
+  // eq_type 1: stress relaxation G(t); 2: centre-of-mass MSD(t) (main_cuda.cu:76-82)
+  s->corr = (!s->flow) && (P.eq_type == 1 || P.eq_type == 2) && P.sync_dt > 0 && P.t_end > 0;
+  s->msd = s->corr && P.eq_type == 2;
+  s->ck = s->corr ? (s->msd ? 2 : 1) : 0;
   s->cp = P.corr_p > 0 ? P.corr_p : 64;
   s->cm = P.corr_m > 0 ? P.corr_m : 8;
   if (s->cp % s->cm != 0 || s->cp > 256) return fail(s, DSM_ERR_INVALID, "correlator p must be a multiple of m and <= 256");
@@ -282,6 +292,12 @@ int dsm::sim_setup(dsm_sim* s) {
     CK(cudaMallocAsync((void**)&s->d_nk_chain, n * sizeof(int32_t), s->st));
     CK(cudaMemcpyAsync(s->d_nk_chain, s->nk_chain.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
   }
+  if (P.pd_flag != 0) {
+    const size_t nm = s->gex.M.size(), nd = s->gex.Md.size();
+    CK(cudaMallocAsync((void**)&s->d_gex, (nm + nd) * sizeof(float), s->st));
+    CK(cudaMemcpyAsync(s->d_gex, s->gex.M.data(), nm * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->d_gex + nm, s->gex.Md.data(), nd * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  }
   CK(cudaMallocAsync((void**)&s->d_ens, sizeof(EnsDev), s->st));
   CK(cudaMallocAsync((void**)&s->d_prefix, 2 * sizeof(long long), s->st));
   CK(cudaMallocAsync((void**)&s->d_work, sizeof(unsigned int), s->st));
@@ -304,7 +320,7 @@ int dsm::sim_setup(dsm_sim* s) {
   std::memset(&E, 0, sizeof(E));
   E.n_chains = P.n_chains; E.cap = s->cap; E.nk = P.nk; E.cd_flag = P.cd_flag ? 1 : 0;
   E.flow = s->flow ? 1 : 0; E.s0 = P.s0 > 0 ? P.s0 : 40; E.poly = s->poly ? 1 : 0;
-  E.corr_type = s->corr ? 0 : -1; E.corr_p = s->cp; E.corr_m = s->cm; E.corr_levels = s->levels;
+  E.corr_type = s->corr ? (s->msd ? 1 : 0) : -1; E.corr_p = s->cp; E.corr_m = s->cm; E.corr_levels = s->levels;
   E.beta = P.beta; E.prefact = s->prefact; E.beta_d = (double)P.beta;
   for (int q = 0; q < 9; ++q) E.kap[q] = P.kappa[q];
   E.seed_lo = (uint32_t)P.seed; E.seed_hi = (uint32_t)(P.seed >> 32); E.stream = P.stream;
@@ -313,6 +329,12 @@ int dsm::sim_setup(dsm_sim* s) {
   E.t_end_ticks = 0; E.step_limit = INT64_MAX; E.watchdog_events = INT64_MAX;
   E.pcd = s->pcd.dev;
   E.pcd_by_nk = s->d_pcd_by_nk; E.nk_chain = s->d_nk_chain;
+  if (P.pd_flag != 0) {
+    E.gex = 1;
+    E.gex_n = (int32_t)s->gex.M.size(); E.gex_nd = (int32_t)s->gex.Md.size();
+    E.gex_step = s->gex.step; E.gex_step_d = s->gex.step_d; E.gex_scale = P.gex_mp / P.gex_mk;
+    E.gex_M = s->d_gex; E.gex_Md = s->d_gex + s->gex.M.size();
+  }
   E.NT = (const float4*)(s->d_tables + to.NT); E.NE = (const float4*)(s->d_tables + to.NE);
   E.FRIC = s->d_tables + to.FRIC; E.INV3N = s->d_tables + to.INV3N;
   E.QN = s->d_QN; E.tau = s->d_tau; E.cs = s->d_cs;
@@ -339,7 +361,7 @@ int dsm::sim_setup(dsm_sim* s) {
 
 // Largest slot (strands) at which the step kernel keeps `bps_want` blocks of
 // `cfg.warps_per_block` warps resident per SM (0 if even one strand does not)
-static int largest_slot(bool flow, bool corr, LaunchCfg cfg, int bps_want, int hi) {
+static int largest_slot(bool flow, int corr, LaunchCfg cfg, int bps_want, int hi) {
   int lo = 0;
   while (lo < hi) {
     const int mid = (lo + hi + 1) / 2;
@@ -358,7 +380,7 @@ static int plan_single(dsm_sim* s) {
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
   if (step_block_smem(s->cfg) > (size_t)smem_optin)
     return fail(s, DSM_ERR_INVALID, "chain capacity z_max=" + std::to_string(s->cap) + " does not fit one shared-memory slot");
-  const int bps = step_max_blocks_per_sm(s->flow, s->corr, s->cfg);
+  const int bps = step_max_blocks_per_sm(s->flow, s->ck, s->cfg);
   if (bps < 1) return fail(s, DSM_ERR_CUDA, "step kernel cannot be resident (occupancy 0)");
   s->blocks_per_sm = bps;
   const int tiles = s->cfg.warps_per_block * 32 / s->cfg.lanes;
@@ -376,7 +398,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   if (lanes == 16 || lanes == 32) sc.lanes = lanes;
   sc.warps_per_block = 4;
   // full occupancy of the step kernel is 4 blocks x 4 warps per SM (register bound)
-  const int full_cap = largest_slot(s->flow, s->corr, sc, 4, s->cap);
+  const int full_cap = largest_slot(s->flow, s->ck, sc, 4, s->cap);
   if (small_cap <= 0) small_cap = full_cap;
   // one slot size fits all chains at full occupancy (or no useful split)
   if (small_cap >= s->cap || small_cap < 8) return plan_single(s);
@@ -415,7 +437,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   SizeClass B, Sm;
   if (!big.empty()) {
     B.cfg = LaunchCfg{1, std::min(s->cap, nk_big), s->cfg.pmax, 32};
-    B.bps = step_max_blocks_per_sm(s->flow, s->corr, B.cfg);
+    B.bps = step_max_blocks_per_sm(s->flow, s->ck, B.cfg);
     if (B.bps < 1) return fail(s, DSM_ERR_INVALID, "largest chains do not fit one shared-memory slot");
     B.first = 0;
     B.count = (long long)big.size();
@@ -425,7 +447,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     B.grid = g;
   }
   Sm.cfg = LaunchCfg{4, small_cap, s->cfg.pmax, sc.lanes};
-  Sm.bps = step_max_blocks_per_sm(s->flow, s->corr, Sm.cfg);
+  Sm.bps = step_max_blocks_per_sm(s->flow, s->ck, Sm.cfg);
   if (Sm.bps < 1) return fail(s, DSM_ERR_INVALID, "small slot does not fit shared memory");
   Sm.first = B.count;
   Sm.count = (long long)small.size();
@@ -436,7 +458,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   }
   s->cleanup = SizeClass{};
   s->cleanup.cfg = LaunchCfg{1, s->cap, s->cfg.pmax, 32};
-  s->cleanup.bps = step_max_blocks_per_sm(s->flow, s->corr, s->cleanup.cfg);
+  s->cleanup.bps = step_max_blocks_per_sm(s->flow, s->ck, s->cleanup.cfg);
   if (s->cleanup.bps < 1) return fail(s, DSM_ERR_INVALID, "chain capacity does not fit one shared-memory slot");
   s->cleanup.grid = s->cleanup.bps * s->sm_count;
   if (B.count > 0) s->classes.push_back(B);
@@ -453,7 +475,7 @@ extern "C" void dsm_destroy(dsm_sim* s) {
   if (s->side) cudaStreamSynchronize(s->side);
   void* ptrs[] = {s->d_tables, s->d_QN, s->d_tau, s->d_cs, s->d_stress, s->d_cshift, s->d_cacc, s->d_cavg,
                   s->d_ccnt, s->d_gsum, s->d_gcnt, s->d_pcd_by_nk, s->d_nk_chain, s->d_ens, s->d_prefix,
-                  s->d_work, s->d_status, s->d_counters, s->d_red, s->d_order, s->d_defer, s->d_works};
+                  s->d_work, s->d_status, s->d_counters, s->d_red, s->d_order, s->d_defer, s->d_works, s->d_gex};
   // stream-ordered frees: no device-wide synchronisation
   for (void* p : ptrs) if (p) cudaFreeAsync(p, s->st);
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -480,7 +502,7 @@ static int default_schedule(dsm_sim* s) {
   LaunchCfg c = s->cfg;
   c.lanes = 16;
   c.warps_per_block = 4;
-  const int cap16 = largest_slot(s->flow, s->corr, c, 4, s->cap);
+  const int cap16 = largest_slot(s->flow, s->ck, c, 4, s->cap);
   const double pe = 1.0 / (1.0 + (double)s->P.beta), nk = (double)s->P.nk;
   const double zb = 1.0 + (nk - 1.0) * pe + 5.0 * std::sqrt(std::max(0.0, (nk - 1.0) * pe * (1.0 - pe))) + 2.0;
   if (cap16 >= s->cap) {
@@ -523,7 +545,7 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
     c.warps_per_block = 4;
     std::vector<int> smalls;
     for (int bps : {4, 3, 2}) {
-      const int cap = largest_slot(s->flow, s->corr, c, bps, s->cap);
+      const int cap = largest_slot(s->flow, s->ck, c, bps, s->cap);
       if (cap >= 8 && std::find(smalls.begin(), smalls.end(), cap) == smalls.end()) smalls.push_back(cap);
     }
     for (int sm : smalls) {
@@ -560,6 +582,17 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
   if (best) { best[0] = b.small; best[1] = b.grid; best[2] = b.lanes; best[3] = (int32_t)cands.size(); }
   if (best_ms) *best_ms = bms;
   return rc;
+}
+
+extern "C" int dsm_get_r1(dsm_sim* s, float* r1) {
+  if (!s || !s->ready || !r1) return DSM_ERR_INVALID;
+  const size_t n = s->P.n_chains;
+  std::vector<ChainState> cs(n);
+  CK(cudaMemcpyAsync(cs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  for (size_t i = 0; i < n; ++i)
+    for (int q = 0; q < 3; ++q) r1[3 * i + q] = cs[i].r1[q];
+  return DSM_OK;
 }
 
 extern "C" int dsm_window_stats(const dsm_sim* s, uint64_t* events, uint64_t* chains_done, uint64_t* deferred) {
@@ -733,7 +766,7 @@ static int64_t window_watchdog(const dsm_sim* s, double dt_tau) {
 static int enqueue_step(dsm_sim* s) {
   if (s->classes.empty()) {
     CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
-    CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->corr, s->cfg,
+    CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->ck, s->cfg,
                    s->d_abort, s->d_status, s->grid, s->st));
     return DSM_OK;
   }
@@ -749,7 +782,7 @@ static int enqueue_step(dsm_sim* s) {
     l.order = s->d_order + k.first;
     l.defer = s->d_defer;
     l.n_defer = s->d_works + 3;
-    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, s->d_works + (large ? 1 : 0), s->flow, s->corr, k.cfg,
+    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, s->d_works + (large ? 1 : 0), s->flow, s->ck, k.cfg,
                    s->d_abort, s->d_status, k.grid, large ? s->side : s->st, l));
   }
   CK(cudaEventRecord(s->ev_join, s->side));
@@ -757,7 +790,7 @@ static int enqueue_step(dsm_sim* s) {
   StepList l;
   l.order = s->d_defer;
   l.dyn_total = s->d_works + 3;
-  CK(launch_step(s->d_ens, 1, s->d_prefix, 0, s->d_works + 2, s->flow, s->corr, s->cleanup.cfg, s->d_abort,
+  CK(launch_step(s->d_ens, 1, s->d_prefix, 0, s->d_works + 2, s->flow, s->ck, s->cleanup.cfg, s->d_abort,
                  s->d_status, s->cleanup.grid, s->st, l));
   return DSM_OK;
 }
@@ -1081,7 +1114,7 @@ extern "C" int dsm_gt_raw(dsm_sim* s, double* gsum, int64_t* count) {
   return DSM_OK;
 }
 
-// G(t) points in the order and count gpu_Gt_PCS writes them
+// G(t) (or MSD(t)) points in the order and count gpu_Gt_PCS writes them
 // (ensemble.cu:298-335, correlator.cu:242-257)
 extern "C" int dsm_gt(dsm_sim* s, float* t, float* G, int32_t* n) {
   if (!s || !n) return DSM_ERR_INVALID;
@@ -1096,7 +1129,9 @@ extern "C" int dsm_gt(dsm_sim* s, float* t, float* G, int32_t* n) {
   if (actual < 0) actual = 0;
   if (*n < actual) { *n = (int32_t)actual; return fail(s, DSM_ERR_INVALID, "output capacity too small"); }
   long long im = 0;
-  const double inv = 1.0 / (3.0 * s->P.n_chains);
+  // G(t): mean of the three shear components per chain (correlator.cu:172);
+  // MSD(t): |dr|^2 summed over the components (correlator.cu:173)
+  const double inv = 1.0 / ((s->msd ? 1.0 : 3.0) * s->P.n_chains);
   for (int k = 0; k < L && im < actual; ++k)
     for (int j = (k == 0 ? 0 : dmin); j < p && im < actual; ++j) {
       if (t) t[im] = (float)(long long)((double)j * std::pow((double)m, k));
@@ -1183,13 +1218,15 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
   // different chain lengths then do not share the largest one's slot size
   struct Group {
     std::vector<int> idx;
-    bool flow, corr;
+    bool flow;
+    int corr;  // correlator kind (0 none, 1 stress, 2 MSD)
     int cap_class, cp, lanes;
   };
   auto cap_class = [](int cap) { int c = 16; while (c < cap) c <<= 1; return c; };
   std::vector<Group> groups;
   for (int i = 0; i < n; ++i) {
-    const bool fl = sims[i]->flow, co = sims[i]->corr;
+    const bool fl = sims[i]->flow;
+    const int co = sims[i]->ck;
     const int cc = cap_class(sims[i]->cap), cp = co ? sims[i]->cp : 0, ln = sims[i]->cfg.lanes;
     Group* g = nullptr;
     for (auto& x : groups)

@@ -20,6 +20,14 @@ struct HostPcd {  // p_cd fit (common/pcd_tau.h:26-66) in double + device form
 struct TableOffsets { size_t NT, NE, FRIC, INV3N; };  // float offsets into one buffer
 
 HostPcd make_pcd(double beta, double nk);
+
+// GEX background molecular-weight tables (dsm_gex.cpp)
+struct GexTable {
+  std::vector<float> M, Md;  // M/mp at probabilities j*step (plain and CD-weighted law)
+  float step = 0.f, step_d = 0.f, mp = 0.f, mk = 0.f;
+  double prefact = 0.0;      // CD creation prefactor step * sum normdt / beta
+};
+int make_gex_table(float a, float b, float mp, float mk, double beta, GexTable* out);
 void make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off);
 int corr_levels_for(double t_end, double dt, int p, int m);
 
@@ -50,7 +58,8 @@ struct SizeClass {
 struct dsm_sim {
   dsm_params P{};
   std::string err;
-  bool ready = false, flow = false, corr = false, poly = false;
+  bool ready = false, flow = false, corr = false, poly = false, msd = false;
+  int ck = 0;  // correlator kind of the step kernel: 0 none, 1 stress, 2 MSD
   int cap = 0, nkmax = 0, cp = 64, cm = 8, levels = 1;
   int64_t nsamples = 0;
   float prefact = 0.f;
@@ -82,6 +91,8 @@ struct dsm_sim {
   dsm::PcdDev* d_pcd_by_nk = nullptr;
   int32_t* d_nk_chain = nullptr;
   dsm::EnsDev* d_ens = nullptr;
+  dsm::GexTable gex;        // GEX background tables (pd_flag = 1)
+  float* d_gex = nullptr;   // device copy: M then Md
   long long* d_prefix = nullptr;
   unsigned int* d_work = nullptr;
   int* d_status = nullptr;

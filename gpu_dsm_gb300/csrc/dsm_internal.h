@@ -35,7 +35,7 @@ struct ChainState {
   uint64_t hash;      // running FNV-style hash of the event sequence
   int64_t k_next;     // next stress-sample index
   int32_t nk;         // Kuhn steps of this chain
-  int32_t pad_[3];
+  float r1[3];        // MSD mode: first entanglement in the lab frame (eq_ensemble_kernel.cu:275-277)
 };
 static_assert(sizeof(ChainState) == 64, "ChainState layout");
 
@@ -54,6 +54,12 @@ struct EnsDev {
   int64_t step_limit;        // ... or when step >= step_limit
   int64_t watchdog_events;   // max events per chain per launch (stall 5 beyond)
   PcdDev pcd;                // monodisperse partner law
+  // GEX background (pd_flag = 1): partner N_K = mp/Mk * M/mp from the inverse
+  // tables M (SD-created and initial entanglements) and Md (CD-created)
+  int32_t gex, gex_n, gex_nd, gex_pad_;
+  float gex_step, gex_step_d, gex_scale, gex_pad2_;
+  const float* gex_M;
+  const float* gex_Md;
   const PcdDev* pcd_by_nk;   // polydisperse: partner law by N_K
   const int32_t* nk_chain;   // polydisperse: N_K of every chain
   // per-N tables: NT[N] = {0.75/(N(N+1)), 0.75/(N(N-1)), (N/(N+1))^0.75, (N/(N-1))^0.75}
@@ -105,10 +111,11 @@ struct StepList {
 // kernels (dsm_kernels.cu)
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
-                        unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
+                        unsigned int* d_work, bool flow, int corr, const LaunchCfg& cfg,
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
                         const StepList& lst = StepList{});
-int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg);
+// corr: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD
+int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg);
 size_t step_block_smem(const LaunchCfg& cfg);
 cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double* d_gsum, long long* d_count,
                                  cudaStream_t st);

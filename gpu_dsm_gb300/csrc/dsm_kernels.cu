@@ -25,6 +25,10 @@
 //     base+l, so one Philox evaluation serves 32 consecutive events.
 //   * No tensor cores: nothing on this path is a dense contraction.
 #include <cstdint>
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "dsm_internal.h"
@@ -129,7 +133,56 @@ __device__ __forceinline__ float rate_f_t(const PcdDev& p, float u) {
 __device__ __forceinline__ float rate_f_dt(const PcdDev& p, float u) {
   return (u < p.Bdt_) ? m_pow(__fmaf_rn(u, p.Adt_, p.Ddt_), p.Cdt_) : p.tau_d_inv;
 }
-__device__ __forceinline__ PcdDev partner_pcd(const EnsDev& E, uint32_t w) {
+// p_cd fit constants (common/pcd_tau.h:32-66) evaluated in float for a
+// partner of N_K = nk Kuhn steps (GEX background, gpu_random.cu:212-228);
+// the oracle restates the same float operations
+__device__ __noinline__ PcdDev pcd_from_nk(float be, float nk) {
+  const float z = (nk + be) / (be + 1.0f);
+  const float g = 0.667f;
+  float alpha, tau0, tau_max, tau_d;
+  if (be != 1.0f) {
+    const float lb = m_log(be);
+    alpha = (0.053f * lb + 0.31f) * m_pow(z, -0.012f * lb - 0.024f);
+    tau0 = 0.285f * m_pow(be + 2.0f, 0.515f);
+    tau_max = (nk < 2.0f) ? tau0 : 0.025f * m_pow(be + 2.0f, 2.6f) * m_pow(z, 2.83f);
+    tau_d = (nk < 2.0f) ? tau0 : 0.036f * m_pow(be + 2.0f, 3.07f) * m_pow(z - 1.0f, 3.02f);
+  } else {
+    alpha = 0.267096f - 0.375571f * m_exp(-0.0838237f * nk);
+    tau0 = 0.460277f + 0.298913f * m_exp(-0.0705314f * nk);
+    tau_max = (nk < 4.0f) ? tau0 : 0.0156137f * m_pow(nk, 3.18849f);
+    tau_d = (nk < 4.0f) ? tau0 : 0.0740131f * m_pow(nk, 3.18363f);
+  }
+  const float pa = m_pow(tau_max, alpha), p0 = m_pow(tau0, alpha);
+  const float pam1 = m_pow(tau_max, alpha - 1.0f), p0m1 = m_pow(tau0, alpha - 1.0f);
+  const float c1 = pa - p0, cm1 = pam1 - p0m1;
+  const float rcm1c1 = (c1 == 0.0f) ? (alpha - 1.0f) / alpha / tau0 : cm1 / c1;
+  const float At = 1.0f - g;
+  const float Adt = At * alpha / (alpha - 1.0f);
+  const float Bdt = Adt * rcm1c1;
+  const float normdt = Bdt + g / tau_d;
+  PcdDev d;
+  d.At_ = c1 / At; d.Dt_ = p0; d.Ct_ = -1.0f / alpha;
+  d.Adt_ = normdt * c1 / Adt; d.Bdt_ = Bdt / normdt; d.Cdt_ = -1.0f / (alpha - 1.0f); d.Ddt_ = p0m1;
+  d.tau_d_inv = 1.0f / tau_d; d.one_minus_g = 1.0f - g; d.normdt = normdt;
+  d.pad_[0] = d.pad_[1] = 0.f;
+  return d;
+}
+
+// Partner law of a new entanglement.  Monodisperse: the ensemble's p_cd.
+// Per-chain N_K: p_cd of a partner chain drawn uniformly from the ensemble.
+// GEX background: partner mass from the inverse table (linear interpolation
+// at u / step), the CD-weighted table for CD-created entanglements.
+__device__ __forceinline__ PcdDev partner_pcd(const EnsDev& E, uint32_t w, bool cd_created) {
+  if (E.gex) {
+    const float* T = cd_created ? E.gex_Md : E.gex_M;
+    const int n = cd_created ? E.gex_nd : E.gex_n;
+    const float x = __fdiv_rn(u01(w), cd_created ? E.gex_step_d : E.gex_step);
+    int i = (int)floorf(x);
+    float di = __fsub_rn(x, (float)i);
+    if (i > n - 2) { i = n - 2; di = 1.0f; }
+    const float mw = __fadd_rn(__fmul_rn(__ldg(&T[i]), __fsub_rn(1.0f, di)), __fmul_rn(__ldg(&T[i + 1]), di));
+    return pcd_from_nk(E.beta, __fmul_rn(mw, E.gex_scale));
+  }
   if (!E.poly) return E.pcd;
   const uint32_t idx = __umulhi(w, (uint32_t)E.n_chains);
   return E.pcd_by_nk[__ldg(&E.nk_chain[idx])];
@@ -159,6 +212,21 @@ __device__ __forceinline__ float shift_minus(const EnsDev& E, int N1, float q1, 
   return (N1 > 1) ? w : 0.0f;
 }
 
+// One of the two shift components, chosen per lane without divergence:
+// minus = false gives shift_plus, minus = true shift_minus, with the same
+// operations in the same order on selected operands (one exponential per lane).
+__device__ __forceinline__ float shift_comp(const EnsDev& E, bool minus, int N1, float q1, int N2, float q2,
+                                            const float4& a, const float4& b) {
+  const bool z1 = (q1 == 0.0f), z2 = (q2 == 0.0f);
+  const int i = (z1 ? 4 * N1 + (minus ? -1 : 1) : 2 * N1) + (z2 ? 4 * N2 + (minus ? 1 : -1) : 2 * N2);
+  const float u = minus ? q2 : q1, ux = minus ? b.x : a.x;
+  const float v = minus ? q1 : q2, vy = minus ? a.y : b.y;
+  const float arg = __fmaf_rn(u, ux, -__fmul_rn(v, vy));
+  const float pw = __fmul_rn(z1 ? 1.0f : (minus ? a.w : a.z), z2 ? 1.0f : (minus ? b.z : b.w));
+  const float w = __fmul_rn(__fmul_rn(__ldg(&E.FRIC[i]), pw), m_exp(arg));
+  return ((minus ? N1 : N2) > 1) ? w : 0.0f;
+}
+
 // status flags of a component: bit0 NaN, bit1 inf
 __device__ __forceinline__ int comp_bad(float x) {
   return (x != x) ? 1 : ((__float_as_uint(x) == 0x7f800000u) ? 2 : 0);
@@ -168,8 +236,9 @@ __device__ __forceinline__ int comp_bad(float x) {
 struct Corr0 {  // correlator level-0 counters of the resident chain
   int ins, navg;
   long long nins;
-  float a0, a1, a2;
-  int pad_;
+  float a0, a1, a2;  // block sum (stress) or first value of the block (MSD)
+  float r1x;         // MSD mode: first entanglement in the lab frame
+  float r1y, r1z;
   long long k_next, t_next;
 };
 
@@ -284,7 +353,7 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
     const int N2 = sl.N[p + 1];
     const float q1 = sl.Q[p].w, q2 = sl.Q[p + 1].w;
     const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
-    w = (lane & 1) ? shift_minus(E, N1, q1, N2, q2, a, b) : shift_plus(E, N1, q1, N2, q2, a, b);
+    w = shift_comp(E, (lane & 1) != 0, N1, q1, N2, q2, a, b);
   }
   const float wm = t.shfl_xor(w, 1);
   unsigned long long d = 0;
@@ -364,11 +433,15 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
 
 // ------------------------------------------------------------------ correlator
 // Levels >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
-// push the block average w into level 1 and cascade while blocks complete.
-template <int W>
+// push w into level 1 and cascade while blocks complete.  Stress (type 0):
+// the next level gets the block average, lag terms are products.  MSD (type
+// 1, :181-189,203,218): the next level gets the first value of each block (a
+// position is sampled, not averaged), lag terms are squared differences.
+template <int W, bool MSD>
 __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, float w1, float w2, const Tile<W> t) {
   const int lane = t.lane;
   const int L = E.corr_levels, p = E.corr_p, m = E.corr_m, dmin = p / m;
+  constexpr bool msd = MSD;
   for (int k = 1; k < L; ++k) {
     const size_t lk = (size_t)c * L + k;
     int4* cntp = &E.corr_cnt[lk];
@@ -378,7 +451,14 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
     double* acc = &E.corr_acc[lk * p];
     const int ins = cnt.x;
     const long long nins = (((long long)(unsigned)cnt.w) << 32 | (unsigned)cnt.z) + 1;
-    const float a0 = __fadd_rn(av[0], w0), a1 = __fadd_rn(av[1], w1), a2 = __fadd_rn(av[2], w2);
+    float a0, a1, a2;
+    if (!msd) {
+      a0 = __fadd_rn(av[0], w0); a1 = __fadd_rn(av[1], w1); a2 = __fadd_rn(av[2], w2);
+    } else if (cnt.y == 0) {
+      a0 = w0; a1 = w1; a2 = w2;
+    } else {
+      a0 = av[0]; a1 = av[1]; a2 = av[2];
+    }
     t.sync();
     if (lane == 0) { sh[ins * 3 + 0] = w0; sh[ins * 3 + 1] = w1; sh[ins * 3 + 2] = w2; }
     t.sync();
@@ -386,7 +466,13 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
       if ((long long)j >= nins) break;
       int i2 = ins - j;
       if (i2 < 0) i2 += p;
-      const float pv = __fmaf_rn(w2, sh[i2 * 3 + 2], __fmaf_rn(w1, sh[i2 * 3 + 1], __fmul_rn(w0, sh[i2 * 3 + 0])));
+      float pv;
+      if (msd) {
+        const float d0 = __fsub_rn(w0, sh[i2 * 3 + 0]), d1 = __fsub_rn(w1, sh[i2 * 3 + 1]), d2 = __fsub_rn(w2, sh[i2 * 3 + 2]);
+        pv = __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
+      } else {
+        pv = __fmaf_rn(w2, sh[i2 * 3 + 2], __fmaf_rn(w1, sh[i2 * 3 + 1], __fmul_rn(w0, sh[i2 * 3 + 0])));
+      }
       acc[j] += (double)pv;
     }
     const int navg = cnt.y + 1;
@@ -400,47 +486,103 @@ __device__ __noinline__ void corr_push_levels(const EnsDev& E, int c, float w0, 
     }
     t.sync();
     if (!up) break;
-    const float rm = (float)m;
-    w0 = __fdiv_rn(a0, rm); w1 = __fdiv_rn(a1, rm); w2 = __fdiv_rn(a2, rm);
+    if (msd) {
+      w0 = a0; w1 = a1; w2 = a2;
+    } else {
+      const float rm = (float)m;
+      w0 = __fdiv_rn(a0, rm); w1 = __fdiv_rn(a1, rm); w2 = __fdiv_rn(a2, rm);
+    }
   }
 }
 
-// Take every stress sample due at chain time T (eq_ensemble_kernel.cu:281-331):
-// shear stresses (xy, yz, xz) of the current state into correlator level 0.
+// Centre of mass of the resident chain (eq_ensemble_kernel.cu:297-321): strand
+// s contributes N_s/N_K times its midpoint R1 + sum_{i<s} Q_i + Q_s/2.  The
+// prefix sums over strands run as tile scans, W strands at a time.
 template <int W>
+__device__ __forceinline__ void chain_com(const EnsDev& E, const Slot& sl, int Z, int c, const Tile<W>& t, float* v) {
+  const int lane = t.lane;
+  float cx = 0.f, cy = 0.f, cz = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+  for (int base = 0; base < Z; base += W) {
+    const int s = base + lane;
+    const bool in = s < Z;
+    const float4 q = in ? sl.Q[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float n = in ? (float)sl.N[s] : 0.f;
+    float ix = q.x, iy = q.y, iz = q.z;
+#pragma unroll
+    for (int o = 1; o < W; o <<= 1) {
+      const float ux = t.shfl_up(ix, o), uy = t.shfl_up(iy, o), uz = t.shfl_up(iz, o);
+      if (lane >= o) { ix = __fadd_rn(ix, ux); iy = __fadd_rn(iy, uy); iz = __fadd_rn(iz, uz); }
+    }
+    float ex = t.shfl_up(ix, 1), ey = t.shfl_up(iy, 1), ez = t.shfl_up(iz, 1);
+    if (lane == 0) { ex = 0.f; ey = 0.f; ez = 0.f; }
+    cx = __fmaf_rn(__fadd_rn(__fadd_rn(px, ex), __fmul_rn(0.5f, q.x)), n, cx);
+    cy = __fmaf_rn(__fadd_rn(__fadd_rn(py, ey), __fmul_rn(0.5f, q.y)), n, cy);
+    cz = __fmaf_rn(__fadd_rn(__fadd_rn(pz, ez), __fmul_rn(0.5f, q.z)), n, cz);
+    px = __fadd_rn(px, t.shfl(ix, W - 1)); py = __fadd_rn(py, t.shfl(iy, W - 1)); pz = __fadd_rn(pz, t.shfl(iz, W - 1));
+  }
+  const float nk = (float)(E.poly ? __ldg(&E.nk_chain[c]) : E.nk);
+  const Corr0& k0 = *sl.k0;
+  v[0] = __fadd_rn(__fdiv_rn(t.sum(cx), nk), k0.r1x);
+  v[1] = __fadd_rn(__fdiv_rn(t.sum(cy), nk), k0.r1y);
+  v[2] = __fadd_rn(__fdiv_rn(t.sum(cz), nk), k0.r1z);
+}
+
+// Take every sample due at chain time T (eq_ensemble_kernel.cu:281-331): the
+// shear stresses (xy, yz, xz) or the centre of mass into correlator level 0.
+template <int W, bool MSD>
 __device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int c, long long T, const Tile<W> t) {
   const int lane = t.lane;
   Corr0& k0 = *sl.k0;
   const int p = E.corr_p, m = E.corr_m;
+  constexpr bool msd = MSD;
   while (k0.k_next < E.nsamples && T > k0.t_next) {
-    float sxy = 0.f, syz = 0.f, sxz = 0.f;
-    for (int s = lane; s < Z; s += W) {
-      const float4 q = sl.Q[s];
-      const float w = __ldg(&E.INV3N[sl.N[s]]);
-      sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
-      syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
-      sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
+    float v[3];
+    if (msd) {
+      chain_com<W>(E, sl, Z, c, t, v);
+    } else {
+      float sxy = 0.f, syz = 0.f, sxz = 0.f;
+      for (int s = lane; s < Z; s += W) {
+        const float4 q = sl.Q[s];
+        const float w = __ldg(&E.INV3N[sl.N[s]]);
+        sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
+        syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
+        sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
+      }
+      v[0] = t.sum(sxy); v[1] = t.sum(syz); v[2] = t.sum(sxz);
     }
-    sxy = t.sum(sxy); syz = t.sum(syz); sxz = t.sum(sxz);
     const int ins = k0.ins;
     const long long n0 = k0.nins + 1;
     t.sync();
-    if (lane == 0) { sl.Csh[ins * 3 + 0] = sxy; sl.Csh[ins * 3 + 1] = syz; sl.Csh[ins * 3 + 2] = sxz; }
+    if (lane == 0) { sl.Csh[ins * 3 + 0] = v[0]; sl.Csh[ins * 3 + 1] = v[1]; sl.Csh[ins * 3 + 2] = v[2]; }
     t.sync();
     for (int j = lane; j < p; j += W) {
       if ((long long)j >= n0) break;
       int i2 = ins - j;
       if (i2 < 0) i2 += p;
-      const float pv = __fmaf_rn(sxz, sl.Csh[i2 * 3 + 2], __fmaf_rn(syz, sl.Csh[i2 * 3 + 1], __fmul_rn(sxy, sl.Csh[i2 * 3 + 0])));
+      float pv;
+      if (msd) {
+        const float d0 = __fsub_rn(v[0], sl.Csh[i2 * 3 + 0]), d1 = __fsub_rn(v[1], sl.Csh[i2 * 3 + 1]);
+        const float d2 = __fsub_rn(v[2], sl.Csh[i2 * 3 + 2]);
+        pv = __fmaf_rn(d2, d2, __fmaf_rn(d1, d1, __fmul_rn(d0, d0)));
+      } else {
+        pv = __fmaf_rn(v[2], sl.Csh[i2 * 3 + 2], __fmaf_rn(v[1], sl.Csh[i2 * 3 + 1], __fmul_rn(v[0], sl.Csh[i2 * 3 + 0])));
+      }
       // Kahan-compensated FP32 accumulation
       float2 a = sl.Cacc[j];
       const float y = __fsub_rn(pv, a.y);
-      const float t = __fadd_rn(a.x, y);
-      a.y = __fsub_rn(__fsub_rn(t, a.x), y);
-      a.x = t;
+      const float tt = __fadd_rn(a.x, y);
+      a.y = __fsub_rn(__fsub_rn(tt, a.x), y);
+      a.x = tt;
       sl.Cacc[j] = a;
     }
-    const float a0 = __fadd_rn(k0.a0, sxy), a1 = __fadd_rn(k0.a1, syz), a2 = __fadd_rn(k0.a2, sxz);
+    float a0, a1, a2;
+    if (!msd) {
+      a0 = __fadd_rn(k0.a0, v[0]); a1 = __fadd_rn(k0.a1, v[1]); a2 = __fadd_rn(k0.a2, v[2]);
+    } else if (k0.navg == 0) {
+      a0 = v[0]; a1 = v[1]; a2 = v[2];
+    } else {
+      a0 = k0.a0; a1 = k0.a1; a2 = k0.a2;
+    }
     const int navg = k0.navg + 1;
     t.sync();
     if (lane == 0) {
@@ -453,8 +595,12 @@ __device__ __noinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, int 
     }
     t.sync();
     if (navg == m && E.corr_levels > 1) {
-      const float rm = (float)m;
-      corr_push_levels(E, c, __fdiv_rn(a0, rm), __fdiv_rn(a1, rm), __fdiv_rn(a2, rm), t);
+      if (msd) {
+        corr_push_levels<W, MSD>(E, c, a0, a1, a2, t);
+      } else {
+        const float rm = (float)m;
+        corr_push_levels<W, MSD>(E, c, __fdiv_rn(a0, rm), __fdiv_rn(a1, rm), __fdiv_rn(a2, rm), t);
+      }
     }
   }
 }
@@ -479,7 +625,7 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
   float g0, g1, g2, g3;
   m_gauss2(gr.x, gr.y, &g0, &g1);
   m_gauss2(gr.z, gr.w, &g2, &g3);
-  const PcdDev pp = partner_pcd(E, w3);
+  const PcdDev pp = partner_pcd(E, w3, evn == CDC_MID || evn == CDC_TAIL);
   const float u = u01(w2);
   const float trate = E.cd_flag ? ((evn == CDC_MID || evn == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
   if (evn == CDC_MID && j > 0) {
@@ -513,6 +659,10 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
       sl.N[0] = nd; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
       sl.N[1] = nn; sl.Q[1] = make_float4(x, y, z, m_q2(x, y, z));
       sl.T[0] = trate;
+      if (E.corr_type == 1) {  // MSD: the new first entanglement (eq_ensemble_kernel.cu:531-539,606-614)
+        Corr0& k0 = *sl.k0;
+        k0.r1x = __fsub_rn(k0.r1x, x); k0.r1y = __fsub_rn(k0.r1y, y); k0.r1z = __fsub_rn(k0.r1z, z);
+      }
     }
     *up0_out = 0; *upn_out = 2;
   } else {  // CDC_TAIL, SDC_TAIL
@@ -535,8 +685,10 @@ __device__ __noinline__ int apply_create(const EnsDev& E, Slot& sl, int evn, int
 
 // Apply a destruction (CD of pair j, SD at head or tail): sets the pairs to
 // recompute (up0, upn).
-template <int W>
-__device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, const Tile<W> t, int* up0_out, int* upn_out) {
+template <int W, bool MSD>
+__device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, const Tile<W> t, int* up0_out,
+                                          int* upn_out) {
+  constexpr bool msd = MSD;
   const int lane = t.lane;
   if (evn == CDD) {  // ensemble_kernel.cu:312-323
     const int n = sl.N[j] + sl.N[j + 1];
@@ -550,14 +702,25 @@ __device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, cons
       const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
       const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
       sl.N[j] = n; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+      if (msd && j == 0) {  // the first entanglement is now the old second one (eq_ensemble_kernel.cu:447-455)
+        Corr0& k0 = *sl.k0;
+        k0.r1x = __fadd_rn(k0.r1x, b.x); k0.r1y = __fadd_rn(k0.r1y, b.y); k0.r1z = __fadd_rn(k0.r1z, b.z);
+      }
     }
     *up0_out = j - 1; *upn_out = 2;
   } else if (evn == SDD_HEAD) {  // ensemble_kernel.cu:492-494
     const int n = sl.N[1] + 1;
+    const float4 b = sl.Q[1];
     t.sync();
     move_down(sl.Q, 1, Z, t); move_down(sl.N, 1, Z, t);
     move_down(sl.T, 1, Z - 1, t); move_down(sl.R, 1, Z - 1, t); move_down(sl.P, 1, Z - 1, t);
-    if (lane == 0) { sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    if (lane == 0) {
+      sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (msd) {  // eq_ensemble_kernel.cu:645-653
+        Corr0& k0 = *sl.k0;
+        k0.r1x = __fadd_rn(k0.r1x, b.x); k0.r1y = __fadd_rn(k0.r1y, b.y); k0.r1z = __fadd_rn(k0.r1z, b.z);
+      }
+    }
     *up0_out = 0; *upn_out = 1;
   } else {  // SDD_TAIL, ensemble_kernel.cu:495-498
     t.sync();
@@ -568,11 +731,14 @@ __device__ __noinline__ void apply_destroy(Slot& sl, int evn, int j, int Z, cons
 }
 
 // ------------------------------------------------------------------ step kernel
-template <bool FLOW, bool CORR, int W>
+// CK: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD (compile
+// time, so that the stress kernel carries no MSD code)
+template <bool FLOW, int CK, int W>
 __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict__ ens, int n_ens,
                                                  const long long* __restrict__ prefix, long long total,
                                                  unsigned int* work, int slot_cap, int pmax,
                                                  const volatile int* abort_flag, int* status, StepList lst) {
+  constexpr bool CORR = CK != 0, MSD = CK == 2;
   extern __shared__ __align__(16) unsigned char smem[];
   const Tile<W> t;
   const int lane = t.lane;
@@ -634,6 +800,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       k0.a0 = E.corr_avg[l0 * 3 + 0]; k0.a1 = E.corr_avg[l0 * 3 + 1]; k0.a2 = E.corr_avg[l0 * 3 + 2];
       k0.k_next = st.k_next;
       k0.t_next = st.k_next * E.dt_sample_ticks;
+      if (MSD) { k0.r1x = st.r1[0]; k0.r1y = st.r1[1]; k0.r1z = st.r1[2]; }
     }
     if (CORR) {
       const int p = E.corr_p;
@@ -683,7 +850,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         t.sync();
       }
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
-      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W>(E, sl, Z, c, T, t);
+      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W, MSD>(E, sl, Z, c, T, t);
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207); a full
       // slot (a creation could need strand Z+1) ends the launch for this chain
       // at this step boundary, exactly like a window end
@@ -795,7 +962,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
         ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
         slide = !ends_dirty;
       } else if (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) {
-        apply_destroy<W>(sl, evn, j, Z, t, &up0, &upn);
+        apply_destroy<W, MSD>(sl, evn, j, Z, t, &up0, &upn);
         Z -= 1;
         ends_dirty = true;
       } else if (Z >= cap) {
@@ -898,6 +1065,10 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       cs->Z = Z; cs->stall = stall; cs->dt_prev = dt_prev;
       cs->T = T; cs->step = step; cs->hash = hash;
       if (k_next >= 0) cs->k_next = k_next;
+      if (MSD) {
+        const Corr0& q = *sl.k0;
+        cs->r1[0] = q.r1x; cs->r1[1] = q.r1y; cs->r1[2] = q.r1z;
+      }
       atomicAdd(&E.counters[0], done);
       if (deferred) {
         lst.defer[atomicAdd(lst.n_defer, 1u)] = (int)(prefix[e] + c);
@@ -1001,7 +1172,7 @@ __global__ void __launch_bounds__(128) k_init(const EnsDev* __restrict__ ensp, i
     float tr = 0.0f;
     if (i < Z - 1) {
       const U4 r = rng_at(E, P_TAUINIT, (uint64_t)i, 0, (uint32_t)c);
-      const PcdDev pp = partner_pcd(E, r.y);
+      const PcdDev pp = partner_pcd(E, r.y, false);
       tr = E.cd_flag ? rate_f_t(pp, u01(r.x)) : 0.0f;
     }
     gt[i] = tr;
@@ -1027,7 +1198,7 @@ __global__ void __launch_bounds__(128) k_init(const EnsDev* __restrict__ ensp, i
     ChainState st;
     st.Z = Z; st.stall = 0; st.S = min(E.s0, LIMIT_E - emax); st.dt_prev = 0.f;
     st.T = 0; st.step = 0; st.hash = 0xCBF29CE484222325ull; st.k_next = 0;
-    st.nk = nk; st.pad_[0] = st.pad_[1] = st.pad_[2] = 0;
+    st.nk = nk; st.r1[0] = st.r1[1] = st.r1[2] = 0.f;
     E.cs[c] = st;
   }
 }
@@ -1097,16 +1268,16 @@ __global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win,
 }
 
 // ------------------------------------------------------------------ launchers
-template <bool FLOW, bool CORR, int W>
-static void* step_fn() { return (void*)k_step<FLOW, CORR, W>; }
+template <bool FLOW, int CK, int W>
+static void* step_fn() { return (void*)k_step<FLOW, CK, W>; }
 
 template <int W>
-static void* pick_step_w(bool flow, bool corr) {
-  if (flow) return step_fn<true, false, W>();
-  return corr ? step_fn<false, true, W>() : step_fn<false, false, W>();
+static void* pick_step_w(bool flow, int ck) {
+  if (flow) return step_fn<true, 0, W>();
+  return ck == 2 ? step_fn<false, 2, W>() : ck == 1 ? step_fn<false, 1, W>() : step_fn<false, 0, W>();
 }
-static void* pick_step(bool flow, bool corr, int lanes) {
-  return lanes == 16 ? pick_step_w<16>(flow, corr) : pick_step_w<32>(flow, corr);
+static void* pick_step(bool flow, int ck, int lanes) {
+  return lanes == 16 ? pick_step_w<16>(flow, ck) : pick_step_w<32>(flow, ck);
 }
 
 static int tile_lanes(const LaunchCfg& cfg) { return cfg.lanes == 16 ? 16 : 32; }
@@ -1115,14 +1286,34 @@ static size_t step_smem(const LaunchCfg& cfg) {
   return step_slot_bytes(cfg.slot_cap, cfg.pmax) * tiles;
 }
 
+// Function attributes are process-wide: one thread setting a smaller
+// dynamic shared-memory limit between another thread's set and launch would
+// make that launch fail.  Each step kernel is therefore prepared once per
+// device with the device's opt-in maximum (an upper bound only: occupancy
+// follows the size given at launch) and the largest carveout (the slots are
+// the working set), and never changed afterwards.
 static cudaError_t prep_step(void* fn, size_t sm) {
-  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  static std::mutex mu;
+  static std::vector<std::pair<void*, int>> done;  // (kernel, device)
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
-  // the slots are the working set: ask for the largest shared-memory carveout
-  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  std::lock_guard<std::mutex> lk(mu);
+  for (const auto& d : done)
+    if (d.first == fn && d.second == dev) return cudaSuccess;
+  int optin = 0;
+  err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (err != cudaSuccess) return err;
+  if (sm > (size_t)optin) return cudaErrorInvalidValue;
+  err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (err != cudaSuccess) return err;
+  done.push_back({fn, dev});
+  return cudaSuccess;
 }
 
-int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg) {
+int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg) {
   const size_t sm = step_smem(cfg);
   void* fn = pick_step(flow, corr, tile_lanes(cfg));
   if (prep_step(fn, sm) != cudaSuccess) return 0;
@@ -1134,7 +1325,7 @@ int step_max_blocks_per_sm(bool flow, bool corr, const LaunchCfg& cfg) {
 size_t step_block_smem(const LaunchCfg& cfg) { return step_smem(cfg); }
 
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
-                        unsigned int* d_work, bool flow, bool corr, const LaunchCfg& cfg,
+                        unsigned int* d_work, bool flow, int corr, const LaunchCfg& cfg,
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
                         const StepList& lst) {
   const size_t sm = step_smem(cfg);
@@ -1150,7 +1341,7 @@ cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefi
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st) {
   const int wpb = 4;
   const size_t sm = (size_t)(slot_cap + 1) * 8 * wpb;
-  cudaError_t err = cudaFuncSetAttribute((void*)k_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t err = prep_step((void*)k_init, sm);  // one-time attribute setup, as for the step kernels
   if (err != cudaSuccess) return err;
   const int grid = (h_ens.n_chains + wpb - 1) / wpb;
   k_init<<<grid, wpb * 32, sm, st>>>(d_ens, slot_cap);

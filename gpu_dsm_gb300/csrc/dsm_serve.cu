@@ -59,6 +59,9 @@ struct Req {
   int64_t n_outputs = 0;  // flow: outputs at min(t_end, k * sync_dt), k = 1..n_outputs
   bool inflight = false;
   double target = 0.0;    // end time of the chunk in flight
+  double eps = 0.0;       // kMC events per second of its last chunk (wall clock)
+  double occupancy = 1.0; // share of the GPU's chain slots its step launch fills
+  clk::time_point t_chunk;
   std::vector<double> ends;
   std::vector<dsm_stress_plus> sbuf;
   std::vector<double> out_t;
@@ -95,7 +98,9 @@ struct dsm_server {
   int max_active = 0;
   double chunk_s = 0.05;     // target duration of one chunk; < 0: whole-request windows
   double rate_est = 1.0e9;   // aggregate kMC events/s while work is in flight
+  int policy = 0;            // 0 first come first served with backfill, 1 equal pace per chain
   int prio_least = 0, prio_greatest = 0;  // CUDA stream priority range
+  int sm_slots = 4864;       // chains resident on the GPU at full occupancy (152 SMs x 32)
   std::mutex mu;
   std::condition_variable cv;       // request state changes (waiters)
   std::condition_variable cv_work;  // work for the loader / finisher threads
@@ -118,7 +123,7 @@ struct dsm_server {
   void load_loop();
   void finish_loop();
   void admit();
-  int start_chunk(Req* r, double chains_total);
+  int start_chunk(Req* r, double chains_total, int rank);
   void fail_req(Req* r, const std::string& why);
 };
 
@@ -157,8 +162,17 @@ void dsm_server::load_loop() {
     }
     const auto t0 = clk::now();
     dsm_sim* sim = nullptr;
-    int rc = dsm_create(&r->P, &sim);
+    // create and initialise on a highest-priority stream: the initialiser then
+    // gets SMs as soon as running blocks retire, not after whole chunks
+    dsm_params P = r->P;
+    P.stream_priority = prio_greatest;
+    int rc = dsm_create(&P, &sim);
     if (rc == DSM_OK) rc = dsm_init_equilibrium(sim);
+    if (rc == DSM_OK) {
+      int32_t grid = 0, bps = 0;
+      dsm_last_window(sim, nullptr, nullptr, &grid, &bps);
+      if (grid > 0 && bps > 0) r->occupancy = std::min(1.0, (double)grid / ((double)bps * (double)(sm_slots / 32)));
+    }
     std::string why;
     if (rc != DSM_OK) {
       why = sim ? dsm_last_error(sim) : "dsm_create failed";
@@ -198,6 +212,7 @@ void dsm_server::finish_loop() {
       to_finish.pop_front();
     }
     const auto t0 = clk::now();
+    dsm_set_priority(r->sim, prio_greatest);  // the G(t) reduction should not wait for whole chunks
     if (r->corr) {
       int32_t n = 8192;
       r->gt_t.assign(n, 0.f);
@@ -223,16 +238,32 @@ void dsm_server::finish_loop() {
   }
 }
 
-// Next chunk of r on its own stream.  Each resident chain advances by about
-// the same number of events per chunk: the chunk's share of rate_est * chunk_s
-// is the request's share of the resident chains (at least 64 events per chain).
-int dsm_server::start_chunk(Req* r, double chains_total) {
+// Next chunk of r on its own stream, about chunk_s seconds of work.
+//  * policy 0 (first come, first served with backfill): the request's stream
+//    priority follows its age rank (the oldest gets the highest), so when SMs
+//    free up the block scheduler serves older requests first and younger ones
+//    fill what is left; a chunk is chunk_s times the request's own measured
+//    events per second (first chunk: its share of the GPU's chain slots).
+//  * policy 1 (equal pace): every resident chain advances by the same number of
+//    events per chunk (the request's share of rate_est * chunk_s is its share
+//    of the resident chains), at the default priority.
+// Both give at least 64 events per chain per chunk.
+int dsm_server::start_chunk(Req* r, double chains_total, int rank) {
   const double n = (double)r->P.n_chains;
   double dtau = std::numeric_limits<double>::infinity();
   if (chunk_s > 0.0) {
-    const double ev = std::max(rate_est * chunk_s * n / std::max(chains_total, 1.0), 64.0 * n);
+    double ev;
+    if (policy == 0) {
+      const double slots = (double)sm_slots;
+      const double eps = r->eps > 0.0 ? r->eps : rate_est * std::min(1.0, n / slots);
+      ev = std::max(eps * chunk_s, 64.0 * n);
+    } else {
+      ev = std::max(rate_est * chunk_s * n / std::max(chains_total, 1.0), 64.0 * n);
+    }
     dtau = ev / std::max(r->rate, 1.0);
   }
+  if (policy == 0) dsm_set_priority(r->sim, prio_greatest + std::min(rank, prio_least - prio_greatest));
+  r->t_chunk = clk::now();
   if (r->flow) {
     const int64_t left = r->n_outputs - r->k_out;
     int64_t k = 1;
@@ -296,21 +327,29 @@ void dsm_server::run() {
         changed = true;
       }
     }
-    // older requests on higher-priority streams: when SMs free up, the block
-    // scheduler places the oldest requests' blocks first, the younger ones
-    // fill what is left (first come, first served with backfill)
-    const int levels = prio_least - prio_greatest;
+    (void)changed;
     double chains_total = 0.0;
-    for (size_t i = 0; i < active.size(); ++i) {
-      Req* r = active[i];
-      chains_total += r->P.n_chains;
-      if (changed && !r->inflight) dsm_set_priority(r->sim, prio_greatest + std::min<int>((int)i, levels));
-    }
+    for (Req* r : active) chains_total += r->P.n_chains;
     std::vector<Req*> still;
     bool progressed = false;
+    int rank = 0;  // age rank among the running requests (active is in arrival order)
+    // First come, first served with backfill: in arrival order, a request
+    // gets chunks while the older running ones leave part of the GPU's chain
+    // slots free (the oldest always runs); a request whose remaining work
+    // is below one chunk of the whole GPU runs at once.  Equal pace runs all.
+    double occ = 0.0;
+    const double short_work = rate_est * std::max(chunk_s, 0.0);
     for (Req* r : active) {
+      const int my_rank = rank++;
+      bool may_run = true;
+      if (policy == 0 && chunk_s > 0.0) {
+        const double rem = (r->P.t_end - r->t_cur) * r->rate;
+        may_run = r->inflight || occ < 1.0 || rem < short_work;
+        occ += r->occupancy;
+      }
+      if (!may_run) { still.push_back(r); continue; }
       if (!r->inflight) {
-        const int rc = start_chunk(r, chains_total);
+        const int rc = start_chunk(r, chains_total, my_rank);
         if (rc != DSM_OK) { fail_req(r, dsm_last_error(r->sim)); progressed = true; continue; }
         r->inflight = true;
         ++ticks;
@@ -324,6 +363,8 @@ void dsm_server::run() {
       if (rc != DSM_OK) { fail_req(r, dsm_last_error(r->sim)); continue; }
       const double dtau = r->target - r->t_cur;
       if (dtau > 0 && ev > 0) r->rate = (double)ev / dtau;
+      const double wall = std::chrono::duration<double>(clk::now() - r->t_chunk).count();
+      if (wall > 0 && ev > 0) r->eps = (double)ev / wall;
       r->t_cur = r->target;
       r->events += ev;
       events += ev;
@@ -342,14 +383,7 @@ void dsm_server::run() {
         still.push_back(r);
       }
     }
-    if (still.size() != active.size()) {
-      // a request left: re-rank the others' priorities before their next chunks
-      active.swap(still);
-      for (size_t i = 0; i < active.size(); ++i)
-        if (!active[i]->inflight) dsm_set_priority(active[i]->sim, prio_greatest + std::min<int>((int)i, levels));
-    } else {
-      active.swap(still);
-    }
+    active.swap(still);
     // aggregate rate over the last >= 20 ms with work in flight
     const auto now = clk::now();
     const double el = std::chrono::duration<double>(now - t_mark).count();
@@ -385,10 +419,20 @@ extern "C" int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t
   s->max_active = max_active;
   s->chunk_s = chunk_s != 0.0 ? chunk_s : 0.05;
   cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0)
+    s->sm_slots = sms * 32;
   s->th = std::thread([s] { s->run(); });
   s->loader = std::thread([s] { s->load_loop(); });
   s->finisher = std::thread([s] { s->finish_loop(); });
   *out = s;
+  return DSM_OK;
+}
+
+extern "C" int dsm_serve_set_policy(dsm_server* s, int32_t policy) {
+  if (!s || (policy != 0 && policy != 1)) return DSM_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->policy = policy;
   return DSM_OK;
 }
 
@@ -447,6 +491,14 @@ extern "C" int dsm_serve_wait_all(dsm_server* s, double timeout_s) {
     if (all) return DSM_OK;
     if (s->cv.wait_until(lk, dl) == std::cv_status::timeout) return DSM_ERR_WATCHDOG;
   }
+}
+
+extern "C" const char* dsm_serve_error(dsm_server* s, uint64_t id) {
+  if (!s) return "null server";
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return "unknown request";
+  return it->second->err.c_str();
 }
 
 extern "C" int dsm_serve_result_gt(dsm_server* s, uint64_t id, float* t, float* G, int32_t* n) {

@@ -59,8 +59,8 @@ typedef struct dsm_params {
   int32_t n_chains;        /* input.dat 3 */
   float kappa[9];          /* input.dat 4: transpose of the velocity gradient, row-major */
   int32_t cd_flag;         /* input.dat 5: 0 SD only, 1 SD+CD */
-  int32_t pd_flag;         /* input.dat 6: GEX background polydispersity (must be 0) */
-  int32_t eq_type;         /* input.dat 7: 1 G(t); other values: no correlator */
+  int32_t pd_flag;         /* input.dat 6: 1 = GEX background polydispersity (gex_* below) */
+  int32_t eq_type;         /* input.dat 7: 1 G(t), 2 MSD(t); other values: no correlator */
   double sync_dt;          /* input.dat 8: sync / sample interval (tau_K) */
   double t_end;            /* input.dat 9: total simulation time (tau_K) */
   uint64_t seed;           /* job_ID: Philox key */
@@ -76,6 +76,8 @@ typedef struct dsm_params {
   int32_t lanes_per_chain; /* 32: one chain per warp, 16: two chains per warp; 0 = auto */
   int32_t stream_priority; /* CUDA priority of the handle's streams (0 = default; lower
                               values are scheduled first, clamped to the device's range) */
+  float gex_a, gex_b;      /* pd_flag = 1: polydisp.dat a, b of the GEX background law */
+  float gex_mp, gex_mk;    /* polydisp.dat mp (mass scale) and Mk (Kuhn-step mass) */
 } dsm_params;
 
 typedef struct dsm_sim dsm_sim;
@@ -166,6 +168,12 @@ int dsm_stress(dsm_sim* sim, dsm_stress_plus* out, int32_t* chain_count);
  * units, G averaged over xy/yz/xz and chains.  n: in = capacity, out = points. */
 int dsm_gt(dsm_sim* sim, float* t, float* G, int32_t* n);
 /* Raw correlator sums: gsum[k*p+j] = sum over chains of C/count, count of chain 0 */
+/* eq_type = 2 (MSD mode, main_cuda.cu:79-82): dsm_gt returns MSD(t), the
+ * centre-of-mass mean-square displacement, written to MSD[_id].dat by
+ * main_cuda.  dsm_get_r1: position of every chain's first entanglement in the
+ * lab frame (n_chains x 3 floats), the MSD reference point
+ * (eq_ensemble_kernel.cu:275-277,447-653). */
+int dsm_get_r1(dsm_sim* sim, float* r1);
 int dsm_gt_raw(dsm_sim* sim, double* gsum, int64_t* count);
 
 /* Device time (CUDA events on the launching stream) and kMC events of the
@@ -213,8 +221,24 @@ int dsm_autotune(dsm_sim* sim, double window, int32_t* best, float* best_ms);
  * in their first slot, chains moved to a larger slot on the way. */
 int dsm_window_stats(const dsm_sim* sim, uint64_t* events, uint64_t* chains_done, uint64_t* deferred);
 
+/* GEX background molecular-weight tables of a polydisperse melt
+ * (polydisp.dat "a b mp Mk", common/gamma.cpp:174-263): m[0..n) = M/mp at
+ * cumulative probabilities j*step, md[0..n_d) the same for the law weighted by
+ * the partner's mean CD destruction rate; info = {step, step_d, CD creation
+ * prefactor}.  n, n_d: in = capacities, out = sizes.  Host only. */
+int dsm_gex_table(float a, float b, float mp, float mk, double beta, float* m, int32_t* n, float* md,
+                  int32_t* n_d, double* info);
+
 /* Correlator geometry of a simulation: levels, p, m */
 int dsm_corr_shape(const dsm_sim* sim, int32_t* levels, int32_t* p, int32_t* m);
+
+/* Conformation statistics of the -distr files, computed on the device
+ * (ensemble.cu:356-484 does them on the host): z_counts[Z] chains with Z
+ * strands (z_bins >= z_max + 1), n_counts[N] strands with N Kuhn steps
+ * (n_bins >= max N_K + 1); dsm_q_sorted: |Q| of every internal strand in
+ * ascending order (q NULL: *n receives the count; else *n in = capacity). */
+int dsm_zn_hist(dsm_sim* sim, uint64_t* z_counts, int32_t z_bins, uint64_t* n_counts, int32_t n_bins);
+int dsm_q_sorted(dsm_sim* sim, float* q, int64_t* n);
 
 /* Reference-format checkpoint (common/ensemble.cu:342-354,486-504):
  * int N_cha, then per chain chain_head, Z float4 QN, Z float tau. */
@@ -286,12 +310,20 @@ enum { DSM_REQ_QUEUED = 0, DSM_REQ_ACTIVE = 1, DSM_REQ_DONE = 2, DSM_REQ_FAILED 
 
 int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t max_active, double chunk_s,
                    dsm_server** out);
+/* Scheduling policy (default 0): 0 first come, first served with backfill (stream
+ * priority by age; chunks of chunk_s of each request's own measured speed),
+ * 1 equal pace for every resident chain at the default priority. */
+#define DSM_SERVE_FCFS 0
+#define DSM_SERVE_EQUAL_PACE 1
+int dsm_serve_set_policy(dsm_server* srv, int32_t policy);
 /* Queue a request; *id identifies it.  DSM_ERR_MEMORY if it can never fit. */
 int dsm_serve_submit(dsm_server* srv, const dsm_params* params, uint64_t* id);
 /* State, latency (arrival to completion, s; -1 while unfinished), queueing
  * delay (arrival to admission, s; -1 while queued), kMC events so far. */
 int dsm_serve_status(dsm_server* srv, uint64_t id, int32_t* state, double* latency_s, double* queue_s,
                      uint64_t* events);
+/* Message of a failed request ("" otherwise); valid until the server closes */
+const char* dsm_serve_error(dsm_server* srv, uint64_t id);
 /* Wait until every submitted request finished; DSM_ERR_WATCHDOG on timeout. */
 int dsm_serve_wait_all(dsm_server* srv, double timeout_s);
 /* Results of a finished request (n: in = capacity, out = points) */

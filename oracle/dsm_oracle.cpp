@@ -63,13 +63,19 @@ typedef struct orc_params {
   int32_t mode;          // 0 FP32 mirror, 1 FP64 transcription
   uint32_t stream;       // Philox counter word 3 (ensemble id)
   uint64_t seed;         // Philox key (job_ID)
-  int32_t corr_type;     // -1 none, 0 stress G(t)
+  int32_t corr_type;     // -1 none, 0 stress G(t), 1 centre-of-mass MSD(t)
   int32_t corr_p, corr_m, corr_levels;
   double corr_dt;        // sample interval
   int64_t corr_nsamples; // samples per chain over the run
   const int32_t* nk_chain;  // per-chain Kuhn steps (NULL: all nk)
   int32_t s0;            // initial fixed-point scale exponent (0 -> 40)
-  int32_t pad_;
+  int32_t gex;           // 1: GEX background partner law from the tables below
+  const float* gex_M;    // M/mp at probabilities j*gex_step (common/gamma.cpp:174-263)
+  const float* gex_Md;   // the CD-weighted counterpart, step gex_step_d
+  int32_t gex_n, gex_nd;
+  float gex_step, gex_step_d, gex_scale;  // scale = mp/Mk
+  int32_t pad2_;
+  double gex_prefact;    // CD creation prefactor of the background law (ensemble.cu:137-146)
 } orc_params;
 }
 
@@ -237,6 +243,7 @@ struct Chain {
   uint64_t step = 0, hash = 0xCBF29CE484222325ull;
   R dt_prev = 0;
   int64_t k_next = 0;     // next sample index
+  R r1[3] = {0, 0, 0};    // MSD mode: first entanglement in the lab frame (eq_ensemble_kernel.cu:275-277)
   std::vector<int32_t> N;
   std::vector<R> Qx, Qy, Qz, q2, tau;
   // multi-tau correlator (FP64), common/eq_ensemble_kernel.cu:133-227
@@ -269,10 +276,65 @@ static inline U4 rng_step(const Ensemble& E, uint32_t purpose, uint64_t step, ui
   return rng(E, purpose, step, (uint32_t)(step >> 32), chain);
 }
 
+// p_cd constants of a partner of N_K = nk, in float (the FP32 mirror of the
+// kernel's GEX partner law; common/pcd_tau.h:32-66 evaluated per sample as
+// gpu_random.cu:212-228 does)
+static PCD pcd_from_nk_f(float be, float nk) {
+  const float z = (nk + be) / (be + 1.0f);
+  const float g = 0.667f;
+  float alpha, tau0, tau_max, tau_d;
+  if (be != 1.0f) {
+    const float lb = m_log(be);
+    alpha = (0.053f * lb + 0.31f) * m_pow(z, -0.012f * lb - 0.024f);
+    tau0 = 0.285f * m_pow(be + 2.0f, 0.515f);
+    tau_max = (nk < 2.0f) ? tau0 : 0.025f * m_pow(be + 2.0f, 2.6f) * m_pow(z, 2.83f);
+    tau_d = (nk < 2.0f) ? tau0 : 0.036f * m_pow(be + 2.0f, 3.07f) * m_pow(z - 1.0f, 3.02f);
+  } else {
+    alpha = 0.267096f - 0.375571f * m_exp(-0.0838237f * nk);
+    tau0 = 0.460277f + 0.298913f * m_exp(-0.0705314f * nk);
+    tau_max = (nk < 4.0f) ? tau0 : 0.0156137f * m_pow(nk, 3.18849f);
+    tau_d = (nk < 4.0f) ? tau0 : 0.0740131f * m_pow(nk, 3.18363f);
+  }
+  const float pa = m_pow(tau_max, alpha), p0 = m_pow(tau0, alpha);
+  const float pam1 = m_pow(tau_max, alpha - 1.0f), p0m1 = m_pow(tau0, alpha - 1.0f);
+  const float c1 = pa - p0, cm1 = pam1 - p0m1;
+  const float rcm1c1 = (c1 == 0.0f) ? (alpha - 1.0f) / alpha / tau0 : cm1 / c1;
+  const float At = 1.0f - g;
+  const float Adt = At * alpha / (alpha - 1.0f);
+  const float Bdt = Adt * rcm1c1;
+  const float normdt = Bdt + g / tau_d;
+  PCD d{};
+  d.At_ = c1 / At; d.Dt_ = p0; d.Ct_ = -1.0f / alpha;
+  d.Adt_ = normdt * c1 / Adt; d.Bdt_ = Bdt / normdt; d.Cdt_ = -1.0f / (alpha - 1.0f); d.Ddt_ = p0m1;
+  d.tau_d_inv = 1.0f / tau_d; d.one_minus_g = 1.0f - g; d.normdt = normdt;
+  return d;
+}
+
 // Partner law for a new entanglement: monodisperse -> the ensemble's p_cd;
-// polydisperse -> p_cd of a partner chain drawn uniformly from the ensemble
-// (role of the GEX background draw, common/chain.cu:209-217).
-static inline const PCD& partner_pcd(const Ensemble& E, uint32_t w) {
+// per-chain N_K -> p_cd of a partner chain drawn uniformly from the ensemble;
+// GEX background -> partner mass from the inverse tables (the CD-weighted one
+// for CD-created entanglements), linear interpolation at u/step
+// (common/chain.cu:141-149, gpu_random.cu:212-228).
+static inline PCD partner_pcd(const Ensemble& E, uint32_t w, bool cd_created) {
+  if (E.P.gex) {
+    const float* T = cd_created ? E.P.gex_Md : E.P.gex_M;
+    const int n = cd_created ? E.P.gex_nd : E.P.gex_n;
+    const float st = cd_created ? E.P.gex_step_d : E.P.gex_step;
+    if (E.P.mode == 0) {
+      const float x = u01(w) / st;
+      int i = (int)std::floor(x);
+      float di = x - (float)i;
+      if (i > n - 2) { i = n - 2; di = 1.0f; }
+      const float mw = T[i] * (1.0f - di) + T[i + 1] * di;
+      return pcd_from_nk_f((float)E.P.beta, mw * E.P.gex_scale);
+    }
+    const double x = ((w >> 8) + 1u) * (1.0 / 16777216.0) / (double)st;
+    int i = (int)std::floor(x);
+    double di = x - (double)i;
+    if (i > n - 2) { i = n - 2; di = 1.0; }
+    const double mw = (double)T[i] * (1.0 - di) + (double)T[i + 1] * di;
+    return make_pcd(E.P.beta, mw * (double)E.P.gex_scale);
+  }
   if (!E.poly) return E.pcd;
   const uint32_t idx = (uint32_t)(((uint64_t)w * (uint64_t)E.P.n_chains) >> 32);
   return E.pcd_by_nk[E.nk_chain[idx]];
@@ -290,19 +352,27 @@ void corr_alloc(const Ensemble& E, Chain<R>& c) {
   c.cnavg.assign(L, 0);
 }
 
-// common/eq_ensemble_kernel.cu:133-227 (type 0: stress autocorrelation)
+// common/eq_ensemble_kernel.cu:133-227.  Type 0 (stress): level k+1 gets the
+// block average of m values of level k, lag products v(t)·v(t-j).  Type 1 (MSD,
+// :181-189,203,218): level k+1 gets the first value of each block of m (a
+// position must not be averaged), lag terms |v(t) - v(t-j)|^2.
 template <class R>
 void corr_add(const Ensemble& E, Chain<R>& c, const double v[3], int k) {
   const int L = E.P.corr_levels, p = E.P.corr_p, m = E.P.corr_m, dmin = p / m;
+  const bool msd = E.P.corr_type == 1;
   if (k >= L) return;
   const int ins = c.cins[k];
   double* sh = &c.cshift[((size_t)k * p) * 3];
   sh[ins * 3 + 0] = v[0]; sh[ins * 3 + 1] = v[1]; sh[ins * 3 + 2] = v[2];
   double* av = &c.cavg[(size_t)k * 3];
-  av[0] += v[0]; av[1] += v[1]; av[2] += v[2];
+  if (!msd) {
+    av[0] += v[0]; av[1] += v[1]; av[2] += v[2];
+  } else if (c.cnavg[k] == 0) {
+    av[0] = v[0]; av[1] = v[1]; av[2] = v[2];
+  }
   c.cnavg[k]++;
   if (c.cnavg[k] == m) {
-    const double w[3] = {av[0] / m, av[1] / m, av[2] / m};
+    const double w[3] = {msd ? av[0] : av[0] / m, msd ? av[1] : av[1] / m, msd ? av[2] : av[2] / m};
     av[0] = av[1] = av[2] = 0.0;
     c.cnavg[k] = 0;
     corr_add(E, c, w, k + 1);
@@ -313,7 +383,12 @@ void corr_add(const Ensemble& E, Chain<R>& c, const double v[3], int k) {
     if ((int64_t)j >= c.cnins[k]) break;
     int i2 = ins - j;
     if (i2 < 0) i2 += p;
-    acc[j] += v[0] * sh[i2 * 3 + 0] + v[1] * sh[i2 * 3 + 1] + v[2] * sh[i2 * 3 + 2];
+    if (msd) {
+      const double dx = v[0] - sh[i2 * 3 + 0], dy = v[1] - sh[i2 * 3 + 1], dz = v[2] - sh[i2 * 3 + 2];
+      acc[j] += dx * dx + dy * dy + dz * dz;
+    } else {
+      acc[j] += v[0] * sh[i2 * 3 + 0] + v[1] * sh[i2 * 3 + 1] + v[2] * sh[i2 * 3 + 2];
+    }
   }
   c.cins[k] = (ins + 1 == p) ? 0 : ins + 1;
 }
@@ -329,6 +404,23 @@ void stress_sample(const Chain<R>& c, double v[3]) {
     sxz -= 3.0 * x * z / n;
   }
   v[0] = sxy; v[1] = syz; v[2] = sxz;
+}
+
+// Centre of mass of the chain (eq_ensemble_kernel.cu:297-321): strand j
+// contributes N_j/N_K times the position of its midpoint, R1 + sum_{i<j} Q_i
+// + Q_j/2 (the dangling head strand has Q = 0, so R1 is where strand 1 starts).
+template <class R>
+void com_sample(const Chain<R>& c, double v[3]) {
+  double px = 0, py = 0, pz = 0, cx = 0, cy = 0, cz = 0;
+  const double nk = (double)c.nk;
+  for (int i = 0; i < c.Z; ++i) {
+    const double x = c.Qx[i], y = c.Qy[i], z = c.Qz[i], n = c.N[i];
+    cx += (px + 0.5 * x) * n / nk;
+    cy += (py + 0.5 * y) * n / nk;
+    cz += (pz + 0.5 * z) * n / nk;
+    px += x; py += y; pz += z;
+  }
+  v[0] = cx + (double)c.r1[0]; v[1] = cy + (double)c.r1[1]; v[2] = cz + (double)c.r1[2];
 }
 
 // ------------------------------------------------------------------ initialiser
@@ -388,12 +480,13 @@ void init_chain(const Ensemble& E, Chain<R>& c, uint32_t ci) {
   }
   for (int k = 0; k < c.Z - 1; ++k) {
     const U4 r = rng(E, P_TAUINIT, (uint64_t)k, 0, ci);
-    const PCD& pp = partner_pcd(E, r.y);
+    const PCD pp = partner_pcd(E, r.y, false);
     if (!E.P.cd_flag) { c.tau[k] = 0; continue; }
     if (E.P.mode == 0) c.tau[k] = (R)rate_f_t(pp, u01(r.x));
     else c.tau[k] = (R)rate_f_t_d(pp, ((r.x >> 8) + 1u) * (1.0 / 16777216.0));
   }
   c.T = 0; c.Td = 0; c.step = 0; c.dt_prev = 0; c.stall = 0; c.k_next = 0;
+  c.r1[0] = c.r1[1] = c.r1[2] = 0;
   c.hash = 0xCBF29CE484222325ull;
   c.S = E.s0;
   corr_alloc(E, c);
@@ -426,8 +519,12 @@ static inline double q2f(double x, double y, double z) { return x * x + y * y + 
 // g[3]: normals for a new strand; trate: lifetime rate of a new entanglement;
 // newn: Kuhn steps of the new strand for a CD creation.
 template <class R>
-void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
+void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate, bool track_r1) {
   const int Z = c.Z;
+  // MSD mode: the first entanglement moves when the head changes
+  // (eq_ensemble_kernel.cu:447-455,531-539,606-614,645-653)
+  auto r1_add = [&](R x, R y, R z) { c.r1[0] = c.r1[0] + x; c.r1[1] = c.r1[1] + y; c.r1[2] = c.r1[2] + z; };
+  auto r1_sub = [&](R x, R y, R z) { c.r1[0] = c.r1[0] - x; c.r1[1] = c.r1[1] - y; c.r1[2] = c.r1[2] - z; };
   auto setQ = [&](int i, R x, R y, R z) {
     c.Qx[i] = x; c.Qy[i] = y; c.Qz[i] = z; c.q2[i] = q2f(x, y, z);
   };
@@ -436,6 +533,7 @@ void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
       const int n = c.N[j] + c.N[j + 1];
       R x = c.Qx[j] + c.Qx[j + 1], y = c.Qy[j] + c.Qy[j + 1], z = c.Qz[j] + c.Qz[j + 1];
       if (j == Z - 2 || j == 0) { x = 0; y = 0; z = 0; }
+      if (track_r1 && j == 0) r1_add(c.Qx[1], c.Qy[1], c.Qz[1]);
       remove_strand(c, j + 1);  // strands > j+1 move down one slot
       remove_tau(c, j);         // entanglement j disappears
       c.N[j] = n; setQ(j, x, y, z);
@@ -453,6 +551,7 @@ void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
         c.N[0] = newn; setQ(0, 0, 0, 0);
         c.N[1] = nn; setQ(1, g[0] * sg, g[1] * sg, g[2] * sg);
         c.tau[0] = trate;
+        if (track_r1) r1_sub(c.Qx[1], c.Qy[1], c.Qz[1]);
       } else {
         const R sg = (R)std::sqrt((R)(newn * (N1 - newn)) / (R)(3 * N1));
         const R ra = (R)newn / (R)N1;
@@ -487,6 +586,7 @@ void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
       c.N[0] = 1; setQ(0, 0, 0, 0);
       c.N[1] = n0; setQ(1, g[0] * sg, g[1] * sg, g[2] * sg);
       c.tau[0] = trate;
+      if (track_r1) r1_sub(c.Qx[1], c.Qy[1], c.Qz[1]);
       c.Z = Z + 1;
       break;
     }
@@ -501,6 +601,7 @@ void apply_event(Chain<R>& c, int ev, int j, int newn, const R g[3], R trate) {
     }
     case SDD_HEAD: {  // ensemble_kernel.cu:492-494
       const int n = c.N[1] + 1;
+      if (track_r1) r1_add(c.Qx[1], c.Qy[1], c.Qz[1]);
       remove_strand(c, 0);
       remove_tau(c, 0);
       c.N[0] = n; setQ(0, 0, 0, 0);
@@ -642,13 +743,13 @@ bool step_mirror(const Ensemble& E, Chain<float>& c, uint32_t ci) {
     float g[3], g3;
     m_gauss2(gr.x, gr.y, &g[0], &g[1]);
     m_gauss2(gr.z, gr.w, &g[2], &g3);
-    const PCD& pp = partner_pcd(E, r.w);
+    const PCD pp = partner_pcd(E, r.w, ev == CDC_MID || ev == CDC_TAIL);
     const float u = u01(r.z);
     const float trate = cd ? ((ev == CDC_MID || ev == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
-    apply_event<float>(c, ev, j, newn, g, trate);
+    apply_event<float>(c, ev, j, newn, g, trate, E.P.corr_type == 1);
     code |= (uint32_t)newn << 8;
   } else {
-    apply_event<float>(c, ev, j, 0, nullptr, 0.0f);
+    apply_event<float>(c, ev, j, 0, nullptr, 0.0f, E.P.corr_type == 1);
   }
   c.hash = hash_step(c.hash, code);
   c.step++;
@@ -731,12 +832,12 @@ bool step_fp64(const Ensemble& E, Chain<double>& c, uint32_t ci) {
       const double u1b = ((gr.z >> 8) + 1u) * (1.0 / 16777216.0), u2b = (gr.w >> 8) * (1.0 / 16777216.0);
       const double ra = std::sqrt(-2.0 * std::log(u1a)), rb = std::sqrt(-2.0 * std::log(u1b));
       const double g[3] = {ra * std::cos(2 * M_PI * u2a), ra * std::sin(2 * M_PI * u2a), rb * std::cos(2 * M_PI * u2b)};
-      const PCD& pp = partner_pcd(E, r.w);
+      const PCD pp = partner_pcd(E, r.w, ev == CDC_MID || ev == CDC_TAIL);
       const double u = ((r.z >> 8) + 1u) * (1.0 / 16777216.0);
       const double trate = cd ? ((ev == CDC_MID || ev == CDC_TAIL) ? rate_f_dt_d(pp, u) : rate_f_t_d(pp, u)) : 0.0;
-      apply_event<double>(c, ev, j, newn, g, trate);
+      apply_event<double>(c, ev, j, newn, g, trate, E.P.corr_type == 1);
     } else {
-      apply_event<double>(c, ev, j, 0, nullptr, 0.0);
+      apply_event<double>(c, ev, j, 0, nullptr, 0.0, E.P.corr_type == 1);
     }
   }
   c.step++;
@@ -796,7 +897,7 @@ int64_t run_chain(const Ensemble& E, Chain<R>& c, uint32_t ci, double t_end, int
         else due = c.Td > (double)c.k_next * E.P.corr_dt;
         if (!due) break;
         double v[3];
-        stress_sample(c, v);
+        if (E.P.corr_type == 1) com_sample(c, v); else stress_sample(c, v);
         corr_add(E, c, v, 0);
         c.k_next++;
       }
@@ -847,7 +948,7 @@ void* orc_create(const orc_params* p) {
     E->pcd = make_pcd(E->P.beta, p->nk);
   } else {
     E->pcd = make_pcd(E->P.beta, p->nk);
-    E->prefact = (float)(E->pcd.normdt / E->P.beta);
+    E->prefact = p->gex ? (float)p->gex_prefact : (float)(E->pcd.normdt / E->P.beta);
   }
   E->prefact_d = E->prefact;
   E->tab = make_tables(nkmax, E->P.beta, E->prefact);
@@ -1069,14 +1170,28 @@ void orc_tau_sample(double beta, double nk, int kind, int mode, const float* u, 
 
 // Multi-tau correlator alone on a series of n 3-vectors (unit test of the
 // correlator semantics of eq_ensemble_kernel.cu:133-227).
-int orc_corr_series(int p, int m, int levels, int64_t n, const double* series, double* acc, int64_t* nins) {
+int orc_corr_series(int type, int p, int m, int levels, int64_t n, const double* series, double* acc,
+                    int64_t* nins) {
   Ensemble E;
-  E.P.corr_type = 0; E.P.corr_p = p; E.P.corr_m = m; E.P.corr_levels = levels;
+  E.P.corr_type = type; E.P.corr_p = p; E.P.corr_m = m; E.P.corr_levels = levels;
   Chain<double> c;
   corr_alloc(E, c);
   for (int64_t t = 0; t < n; ++t) corr_add(E, c, &series[3 * t], 0);
   for (int q = 0; q < levels * p; ++q) acc[q] = c.cacc[q];
   for (int k = 0; k < levels; ++k) nins[k] = c.cnins[k];
+  return 0;
+}
+
+// MSD mode: position of every chain's first entanglement (n_chains x 3)
+int orc_get_r1(void* h, double* r1) {
+  Ensemble* E = (Ensemble*)h;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    if (E->P.mode == 0) {
+      for (int q = 0; q < 3; ++q) r1[3 * i + q] = E->cf[i].r1[q];
+    } else {
+      for (int q = 0; q < 3; ++q) r1[3 * i + q] = E->cd[i].r1[q];
+    }
+  }
   return 0;
 }
 

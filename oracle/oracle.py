@@ -28,7 +28,10 @@ class OrcParams(C.Structure):
         ("cd_flag", C.c_int32), ("kappa", C.c_float * 9), ("mode", C.c_int32), ("stream", C.c_uint32),
         ("seed", C.c_uint64), ("corr_type", C.c_int32), ("corr_p", C.c_int32), ("corr_m", C.c_int32),
         ("corr_levels", C.c_int32), ("corr_dt", C.c_double), ("corr_nsamples", C.c_int64),
-        ("nk_chain", C.c_void_p), ("s0", C.c_int32), ("pad_", C.c_int32),
+        ("nk_chain", C.c_void_p), ("s0", C.c_int32), ("gex", C.c_int32),
+        ("gex_M", C.c_void_p), ("gex_Md", C.c_void_p), ("gex_n", C.c_int32), ("gex_nd", C.c_int32),
+        ("gex_step", C.c_float), ("gex_step_d", C.c_float), ("gex_scale", C.c_float), ("pad2_", C.c_int32),
+        ("gex_prefact", C.c_double),
     ]
 
 
@@ -64,7 +67,8 @@ def lib() -> C.CDLL:
         L.orc_math.argtypes = [C.c_int, vp, vp, vp, C.c_int]
         L.orc_tau_sample.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, vp, vp, C.c_int]
         L.orc_num_threads.restype = C.c_int
-        L.orc_corr_series.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp]
+        L.orc_corr_series.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp]
+        L.orc_get_r1.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -85,7 +89,7 @@ class Oracle:
 
     def __init__(self, *, beta=1.0, nk, n_chains, z_max=0, cd_flag=1, kappa=(0.0,) * 9, mode=0, seed=1,
                  stream=0, corr=False, corr_p=64, corr_m=8, corr_levels=0, sync_dt=1.0, t_end=0.0,
-                 nk_chain: Optional[np.ndarray] = None, s0=0, threads=0):
+                 nk_chain: Optional[np.ndarray] = None, s0=0, threads=0, msd=False, gex_tables=None):
         L = lib()
         p = OrcParams()
         p.beta = float(np.float32(beta))
@@ -99,7 +103,8 @@ class Oracle:
         p.stream = stream
         p.seed = seed
         flow = any(k != 0 for k in kappa)
-        p.corr_type = 0 if (corr and not flow) else -1
+        corr = corr or msd
+        p.corr_type = (1 if msd else 0) if (corr and not flow) else -1
         p.corr_p, p.corr_m = corr_p, corr_m
         p.corr_levels = corr_levels if corr_levels > 0 else (corr_levels_for(t_end, sync_dt, corr_p, corr_m) if corr else 1)
         p.corr_dt = sync_dt
@@ -108,6 +113,16 @@ class Oracle:
         self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
         p.s0 = s0
+        if gex_tables is not None:
+            # GEX background: inverse tables and prefactor as the product builds them
+            self._gex_M = np.ascontiguousarray(gex_tables["M"], np.float32)
+            self._gex_Md = np.ascontiguousarray(gex_tables["Md"], np.float32)
+            p.gex = 1
+            p.gex_M, p.gex_Md = self._gex_M.ctypes.data, self._gex_Md.ctypes.data
+            p.gex_n, p.gex_nd = len(self._gex_M), len(self._gex_Md)
+            p.gex_step, p.gex_step_d = gex_tables["step"], gex_tables["step_d"]
+            p.gex_scale = gex_tables["scale"]
+            p.gex_prefact = gex_tables["prefact"]
         self.p = p
         self.n = n_chains
         self.cap = p.z_max
@@ -152,6 +167,12 @@ class Oracle:
         cnt = np.zeros(1, np.int32)
         lib().orc_stress(self._h, _p(out), _p(cnt))
         return out, int(cnt[0])
+
+    def r1(self):
+        """MSD mode: first-entanglement position of every chain (n, 3)."""
+        out = np.zeros((self.n, 3), np.float64)
+        lib().orc_get_r1(self._h, _p(out))
+        return out
 
     def gt_raw(self):
         L, p = self.p.corr_levels, self.p.corr_p
@@ -213,10 +234,11 @@ def ref_lib() -> Optional[C.CDLL]:
     return _ref
 
 
-def corr_series(series: np.ndarray, p: int, m: int, levels: int):
-    """Run the oracle's multi-tau correlator on one series of 3-vectors."""
+def corr_series(series: np.ndarray, p: int, m: int, levels: int, kind: int = 0):
+    """Run the oracle's multi-tau correlator (kind 0 products, 1 squared
+    differences) on one series of 3-vectors."""
     x = np.ascontiguousarray(series, np.float64)
     acc = np.zeros(levels * p, np.float64)
     nins = np.zeros(levels, np.int64)
-    lib().orc_corr_series(p, m, levels, len(x), _p(x), _p(acc), _p(nins))
+    lib().orc_corr_series(kind, p, m, levels, len(x), _p(x), _p(acc), _p(nins))
     return acc.reshape(levels, p), nins

@@ -5,6 +5,7 @@
 // and to generate the golden fixtures under tests/golden/.  Never shipped.
 #include <cstring>
 #include "chain.h"
+#include "gamma.h"
 
 // globals the reference host code expects (defined in its ensemble.cu /
 // gpu_random.cu / main_cuda.cu, which are not compiled here)
@@ -13,6 +14,12 @@ float step = 0.0f;
 float mp = 0.0f, Mk = 0.0f;
 float* GEX_table = 0;
 double universal_time = 0.0;
+// GEX background tables of common/gamma.cpp
+float a = 0.0f, b = 0.0f;
+float step_d = 0.0f;
+int table_size = 0, table_size_d = 0;
+float gamma_table_cutoff = 0.0f;
+float* GEXd_table = 0;
 
 extern "C" {
 
@@ -54,6 +61,29 @@ int ref_tau_samples(float beta, float nk, int kind, int seed, int n, float* out)
   Ran eran(seed);
   p_cd p(beta, nk, &eran);
   for (int i = 0; i < n; ++i) out[i] = kind == 0 ? p.tau_CD_f_t() : p.tau_CD_f_d_t();
+  return 0;
+}
+
+// GEX background molecular-weight tables built by the reference's own
+// make_gamma_table (gamma.cpp:174-263): the M/mp table and its CD-weighted
+// counterpart, their probability steps and the table cutoff.  The caller's
+// arrays hold up to cap entries; sizes are returned.
+int ref_gex_table(float ga, float gb, float gmp, float gmk, float beta, int cap, float* tab_m, int* n_m,
+                  float* tab_md, int* n_md, float* steps_out) {
+  Be = beta; a = ga; b = gb; mp = gmp; Mk = gmk;
+  step = 0.0f; step_d = 0.0f;
+  make_gamma_table(ga, gb);
+  *n_m = table_size;
+  *n_md = table_size_d;
+  for (int i = 0; i < table_size && i < cap; ++i) tab_m[i] = GEX_table[i];
+  for (int i = 0; i < table_size_d && i < cap; ++i) tab_md[i] = GEXd_table[i];
+  steps_out[0] = step;
+  steps_out[1] = step_d;
+  steps_out[2] = gamma_table_cutoff;
+  delete[] GEX_table;
+  delete[] GEXd_table;
+  GEX_table = 0;
+  GEXd_table = 0;
   return 0;
 }
 

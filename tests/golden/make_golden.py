@@ -12,6 +12,11 @@ Outputs (small JSON files, committed):
                         lifetime-rate quantiles
   tau_reference.json    quantiles of the reference lifetime samplers
                         (pcd_tau.h:67-82)
+  gex_reference.json    GEX background-MW tables of the reference's
+                        make_gamma_table (gamma.cpp:174-263), every 100th entry,
+                        from oracle/_ref/ref_gex (a separate process: the
+                        reference reads uninitialised memory at the end of the
+                        CD-weighted inversion, see oracle/ref_gex_main.cpp)
 """
 from __future__ import annotations
 
@@ -84,6 +89,21 @@ def main():
             R.ref_tau_samples(C.c_float(beta), C.c_float(nk), kind, 12345, n, out.ctypes.data_as(C.c_void_p))
             tq.append({"beta": beta, "nk": nk, "kind": ["f_t", "f_d_t"][kind], "n": n,
                        "tau_quantiles": {str(q): float(np.quantile(out, q)) for q in QUANTS}})
+    # ---- GEX tables (separate process per parameter set)
+    import subprocess
+    exe = HERE.parent.parent / "oracle" / "_ref" / "ref_gex"
+    gex = []
+    for (a, b, mp, mk, be) in [(1.0, 1.0, 1000.0, 100.0, 1.0), (2.0, 1.0, 1000.0, 100.0, 1.0),
+                               (3.0, 2.0, 2000.0, 100.0, 1.0), (1.5, 1.2, 5000.0, 150.0, 2.0)]:
+        r = subprocess.run([str(exe), str(a), str(b), str(mp), str(mk), str(be), "100"], capture_output=True,
+                           text=True, timeout=600)
+        if r.returncode != 0:
+            continue
+        d = json.loads(r.stdout)
+        d.update(a=a, b=b, mp=mp, mk=mk, beta=be)
+        gex.append(d)
+    (HERE / "gex_reference.json").write_text(json.dumps({"source": "common/gamma.cpp:174-263 (compiled)",
+                                                         "rows": gex}))
     (HERE / "tau_reference.json").write_text(json.dumps({"source": "common/pcd_tau.h:67-82 (compiled)", "rows": tq}, indent=1))
     print("golden fixtures written to", HERE)
 

@@ -42,11 +42,11 @@ def assert_bitexact(g: dict, o: dict, keys=STATE_KEYS, what=""):
 
 
 def pair(dsm, orc, *, nk, n, seed=1, beta=1.0, z_max=0, cd=1, kappa=(0.0,) * 9, corr=False, sync_dt=1.0,
-         t_end=0.0, corr_p=16, corr_m=2, nk_chain=None, stream=0, lanes=0):
+         t_end=0.0, corr_p=16, corr_m=2, nk_chain=None, stream=0, lanes=0, msd=False):
     g = dsm.Ensemble(beta=beta, nk=nk, n_chains=n, z_max=z_max, cd_flag=cd, kappa=kappa,
-                     eq_type=1 if corr else 0, sync_dt=sync_dt, t_end=t_end, seed=seed, corr_p=corr_p,
-                     corr_m=corr_m, nk_chain=nk_chain, stream=stream, lanes_per_chain=lanes)
+                     eq_type=2 if msd else (1 if corr else 0), sync_dt=sync_dt, t_end=t_end, seed=seed,
+                     corr_p=corr_p, corr_m=corr_m, nk_chain=nk_chain, stream=stream, lanes_per_chain=lanes)
     o = orc.Oracle(beta=beta, nk=nk, n_chains=n, z_max=z_max, cd_flag=cd, kappa=kappa, seed=seed,
                    corr=corr, sync_dt=sync_dt, t_end=t_end, corr_p=corr_p, corr_m=corr_m, nk_chain=nk_chain,
-                   stream=stream)
+                   stream=stream, msd=msd)
     return g, o

@@ -262,3 +262,65 @@ def test_graph_series_size_classes(dsm_mod, oracle_mod):
     ev, _ = g.advance_series(1.5, 4)
     assert ev == o.run(6.0)
     assert_bitexact(gpu_state(g), o.get_state(), what="series with size classes")
+
+
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_msd_mode(dsm_mod, oracle_mod, lanes):
+    """MSD mode (eq_type=2): chain state and the first-entanglement positions
+    R1 bit for bit, MSD(t) sums within 1e-4 of the FP64 oracle (FP32 centre of
+    mass from tile scans on the GPU)."""
+    g, o = pair(dsm_mod, oracle_mod, nk=30, n=512, seed=8, msd=True, sync_dt=1.0, t_end=300.0, corr_p=16, corr_m=2,
+                lanes=lanes)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    for t in (70.0, 300.0):
+        g.advance(t)
+    o.run(300.0)
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash"), what="msd")
+    r1g, r1o = g.r1(), o.r1()
+    assert np.array_equal(r1g, r1o.astype(np.float32)) and np.abs(r1o).max() > 0
+    gs, gc = g.gt_raw()
+    os_, oc = o.gt_raw()
+    assert np.array_equal(gc, oc)
+    mask = oc > 0
+    assert (np.abs(gs[mask] - os_[mask]) / np.abs(os_[mask]).max()).max() < 1e-4
+    t, msd = g.gt()
+    assert msd[0] == 0.0 and np.all(np.diff(msd[1:12]) > 0)
+
+
+def test_device_distributions(dsm_mod):
+    """-distr statistics computed on the device equal the host computation from
+    the downloaded conformations (ensemble.cu:356-484)."""
+    nkc = _lognormal_nk(500, 3, 60, 0.5, 10, 300)
+    g = dsm_mod.Ensemble(nk=int(nkc.max()), n_chains=500, seed=3, nk_chain=nkc)
+    g.init_equilibrium()
+    g.advance(20.0)
+    hz, hn, q = g.distributions()
+    heads, qn, _ = g.get_chains()
+    Z = heads["Z"]
+    assert np.array_equal(hz, np.bincount(Z, minlength=len(hz)).astype(np.uint64))
+    ns = np.concatenate([qn[i, :Z[i], 3] for i in range(len(Z))]).astype(np.int64)
+    assert np.array_equal(hn, np.bincount(ns, minlength=len(hn)).astype(np.uint64))
+    inner = np.concatenate([qn[i, 1:Z[i] - 1, :3] for i in range(len(Z)) if Z[i] > 2])
+    ql = np.sort(np.sqrt((inner.astype(np.float64) ** 2).sum(axis=1)))
+    assert len(q) == len(ql) and np.all(np.diff(q) >= 0)
+    assert np.allclose(q, ql, rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("beta,kappa", [(1.0, (0.0,) * 9), (2.0, (0.0,) * 9),
+                                        (1.0, (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0))])
+def test_gex_background_bitexact(dsm_mod, oracle_mod, beta, kappa):
+    """GEX background polydispersity (pd_flag = 1, polydisp.dat a b mp Mk):
+    partner masses from the inverse tables, p_cd evaluated per new
+    entanglement on the device; bit for bit against the oracle fed the same
+    tables."""
+    gex = (1.0, 1.0, 1000.0, 100.0)
+    tabs = dsm_mod.gex_tables(*gex, beta)
+    g = dsm_mod.Ensemble(nk=40, n_chains=384, beta=beta, kappa=kappa, seed=19, gex=gex)
+    o = oracle_mod.Oracle(nk=40, n_chains=384, beta=beta, kappa=kappa, seed=19, gex_tables=tabs)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    for t in (10.0, 30.0):
+        g.advance(t)
+        o.run(t)
+    assert_bitexact(gpu_state(g), o.get_state(), what=f"gex beta={beta}")

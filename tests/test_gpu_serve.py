@@ -48,9 +48,10 @@ def _check(srv, ids, dsm):
             assert np.all(np.abs(g - gr) <= 1e-5 * np.abs(gr).max())
 
 
-@pytest.mark.parametrize("max_active,chunk_s", [(0, 0.002), (1, -1.0)])
-def test_serve_matches_alone(dsm_mod, max_active, chunk_s):
-    with dsm_mod.Server(max_active=max_active, chunk_s=chunk_s) as srv:
+@pytest.mark.parametrize("max_active,chunk_s,policy", [(0, 0.002, "fcfs"), (0, 0.002, "equal_pace"),
+                                                        (1, -1.0, "fcfs")])
+def test_serve_matches_alone(dsm_mod, max_active, chunk_s, policy):
+    with dsm_mod.Server(max_active=max_active, chunk_s=chunk_s, policy=policy) as srv:
         ids = [srv.submit(**r) for r in REQS]
         srv.wait_all(600.0)
         _check(srv, ids, dsm_mod)

@@ -223,3 +223,56 @@ def test_correlator_matches_bruteforce(oracle_mod, p, m, levels, n):
                 continue
             brute = np.sum(y[j:] * y[: nb - j])
             assert acc[k, j] == pytest.approx(brute, rel=1e-9, abs=1e-9), (k, j)
+
+
+@pytest.mark.parametrize("p,m,levels,n", [(16, 2, 4, 300), (8, 4, 3, 500)])
+def test_msd_correlator_matches_bruteforce(oracle_mod, p, m, levels, n):
+    """MSD correlator (type 1, eq_ensemble_kernel.cu:181-189,203,218): level k
+    holds every m^k-th position (the first of each block, not an average); lag j
+    accumulates sum_i |y_k(i) - y_k(i-j)|^2."""
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((n, 3)).cumsum(axis=0)
+    acc, nins = oracle_mod.corr_series(x, p, m, levels, kind=1)
+    dmin = p // m
+    for k in range(levels):
+        y = x[:: m ** k][: n // m ** k]
+        nb = len(y)
+        assert nins[k] == nb
+        for j in range(0 if k == 0 else dmin, p):
+            if j >= nb:
+                continue
+            brute = np.sum((y[j:] - y[: nb - j]) ** 2)
+            assert acc[k, j] == pytest.approx(brute, rel=1e-9, abs=1e-9), (k, j)
+
+
+def test_msd_mode_is_diffusive(oracle_mod):
+    """Centre-of-mass MSD of an equilibrium melt: zero at lag 0, growing with
+    the lag, and the first-entanglement positions move (R1 tracking)."""
+    o = oracle_mod.Oracle(nk=20, n_chains=64, seed=5, msd=True, sync_dt=1.0, t_end=200.0, corr_p=16, corr_m=2)
+    o.init_equilibrium()
+    o.run(200.0)
+    g, c = o.gt_raw()
+    msd = g.ravel()[c.ravel() > 0] / 64.0
+    assert msd[0] == 0.0
+    lag = msd[1:12]
+    assert np.all(np.diff(lag) > 0), lag
+    assert np.abs(o.r1()).max() > 0.0
+
+
+def test_gex_background_oracle_runs(oracle_mod, dsm_mod):
+    """The oracle's GEX partner law: lifetimes of the initial entanglements
+    follow the background mixture (a broader law than the monodisperse one:
+    partners shorter than N_K renew faster), and the run stays finite."""
+    tabs = dsm_mod.gex_tables(1.0, 1.0, 1000.0, 100.0, 1.0)
+    assert tabs["step"] > 0 and len(tabs["M"]) > 1000 and tabs["prefact"] > 0
+    o = oracle_mod.Oracle(nk=40, n_chains=256, seed=3, gex_tables=tabs)
+    m = oracle_mod.Oracle(nk=40, n_chains=256, seed=3)
+    o.init_equilibrium()
+    m.init_equilibrium()
+    so, sm = o.get_state(), m.get_state()
+    to = np.concatenate([so["tau"][i, : so["Z"][i] - 1] for i in range(256)])
+    tm = np.concatenate([sm["tau"][i, : sm["Z"][i] - 1] for i in range(256)])
+    assert np.all(np.isfinite(to)) and np.all(to > 0)
+    assert not np.array_equal(np.sort(to), np.sort(tm))
+    o.run(20.0)
+    assert np.all(o.get_state()["stall"] == 0)
