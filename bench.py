@@ -395,10 +395,11 @@ def prior_events(r) -> float:
     return (0.2 * r["nk"] + 2.0) * r["n_chains"] * r["t_end"]
 
 
-def serve_once(reqs, arrivals, *, max_active, chunk_s, device, policy="fcfs"):
+def serve_once(reqs, arrivals, *, max_active, chunk_s, device, policy="fcfs", overlap=1.5, bypass=0.2):
     import gpu_dsm_gb300 as dsm
 
-    srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s, policy=policy)
+    srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s, policy=policy, overlap=overlap,
+                     bypass=bypass)
     ids = []
     t0 = time.perf_counter()
     for r, a in zip(reqs, arrivals):
@@ -446,19 +447,27 @@ def run_serve(args, device: int = 0) -> dict:
     arrivals -= arrivals[0]
     served, out_s = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device, policy="fcfs")
     plain, out_p = serve_once(reqs, arrivals, max_active=1, chunk_s=-1.0, device=device)
-    equal = None
-    if args.serve_equal_pace:
-        equal, _ = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device,
-                              policy="equal_pace")
+    others = {}
+    for spec in args.serve_policies.split(","):
+        # policy[:overlap[:bypass]]
+        if not spec:
+            continue
+        f = spec.split(":")
+        pol = f[0]
+        ov = float(f[1]) if len(f) > 1 else 1.5
+        bp = float(f[2]) if len(f) > 2 else 0.2
+        others[spec], _ = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device,
+                                     policy=pol, overlap=ov, bypass=bp)
     err = 0.0
     for r, a, b in zip(reqs, out_s, out_p):
         if r.get("eq_type") == 1 and len(a) and len(b):
             err = max(err, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)))
     return {"requests": len(reqs), "t_end_scale": args.serve_scale, "arrival_rate_per_s": lam,
             "offered_load_vs_plain": 1.2, "chunk_s": args.serve_chunk, "served": served, "plain": plain,
-            "served_equal_pace": equal,
-            "policies": "served: first come first served with backfill (stream priority by age); "
-                        "plain: one request at a time, one launch per request / flow output",
+            "other_policies": others,
+            "policies": "served: first come first served with backfill (stream priority by age, running "
+                        "requests up to 1.5 GPUs of chain slots, requests under 0.2 chunk of the GPU start at "
+                        "once); plain: one request at a time, one launch per request / flow output",
             "p99_speedup": plain["p99_s"] / served["p99_s"], "p50_speedup": plain["p50_s"] / served["p50_s"],
             "throughput_ratio": served["events_per_s"] / plain["events_per_s"],
             "gt_max_rel_diff_served_vs_plain": err,
@@ -487,7 +496,7 @@ def main():
     ap.add_argument("--serve-cal", type=int, default=16)
     ap.add_argument("--serve-scale", type=float, default=1.0e-3, help="t_end multiplier of the request stream")
     ap.add_argument("--serve-chunk", type=float, default=0.05, help="target chunk duration of the served form (s)")
-    ap.add_argument("--serve-equal-pace", action="store_true", help="also run the equal-pace serving policy")
+    ap.add_argument("--serve-policies", default="", help="other serving policies to run too (equal_pace,fcfs_strict)")
     args = ap.parse_args()
     global N_CHAINS
     N_CHAINS = args.chains

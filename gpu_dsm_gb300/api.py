@@ -152,6 +152,8 @@ def load_library() -> C.CDLL:
     lib.dsm_serve_stats.argtypes = [vp, C.POINTER(ServeTotals)]
     lib.dsm_serve_set_policy.argtypes = [vp, i32]
     lib.dsm_serve_set_policy.restype = C.c_int
+    lib.dsm_serve_tune.argtypes = [vp, C.c_double, C.c_double]
+    lib.dsm_serve_tune.restype = C.c_int
     lib.dsm_serve_error.argtypes = [vp, u64]
     lib.dsm_serve_error.restype = C.c_char_p
     lib.dsm_serve_close.argtypes = [vp]
@@ -479,10 +481,10 @@ class Server:
     time, one launch per request (equilibrium) or per output (flow).
     """
 
-    POLICIES = {"fcfs": 0, "equal_pace": 1}
+    POLICIES = {"fcfs": 0, "equal_pace": 1, "fcfs_strict": 2}
 
     def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_s: float = 0.0,
-                 policy: str = "fcfs"):
+                 policy: str = "fcfs", overlap: float = 1.5, bypass: float = 0.2):
         self._lib = load_library()
         h = C.c_void_p()
         rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, chunk_s, C.byref(h))
@@ -490,6 +492,8 @@ class Server:
             raise DSMError(rc, "dsm_serve_open")
         self._h = h
         rc = self._lib.dsm_serve_set_policy(h, self.POLICIES[policy])
+        if rc == DSM_OK:
+            rc = self._lib.dsm_serve_tune(h, overlap, bypass)
         if rc != DSM_OK:
             raise DSMError(rc, "dsm_serve_set_policy")
         self.device = device

@@ -491,14 +491,15 @@ extern "C" void dsm_destroy(dsm_sim* s) {
 
 extern "C" const char* dsm_last_error(const dsm_sim* s) { return s ? s->err.c_str() : "null handle"; }
 
-// Default launch schedule of a monodisperse ensemble.  Equilibrium chains run
-// two per warp (16 lanes each) with slots of the size that keeps 4 blocks of 4
-// warps per SM, when the chains' strand count (mean + 5 sd of its equilibrium
-// law) fits such a slot: 32 chains per SM instead of 16 (measured +14 % at
-// N_K = 200).  A chain that still outgrows the slot finishes in the overflow
-// launch.  Otherwise, and for flow, one warp per chain with full-capacity slots.
+// Default launch schedule of a monodisperse ensemble.  Chains run two per warp
+// (16 lanes each) with slots of the size that keeps 4 blocks of 4 warps per
+// SM, when the chains' strand count (mean + 5 sd of its equilibrium law) fits
+// such a slot: 32 chains per SM instead of 16 (measured +14 % at N_K = 200
+// with G(t), +24 % for shear at N_K = 100).  A chain that still outgrows the
+// slot finishes in the overflow launch.  Otherwise one warp per chain with
+// full-capacity slots.
 static int default_schedule(dsm_sim* s) {
-  if (s->flow || s->P.lanes_per_chain != 0) return plan_single(s);
+  if (s->P.lanes_per_chain != 0) return plan_single(s);
   LaunchCfg c = s->cfg;
   c.lanes = 16;
   c.warps_per_block = 4;

@@ -382,8 +382,8 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
 // overflow; flow raises again once 2^16 of headroom is free) and requantise if S
 // changes.  Returns the new S; *flags_out gets NaN/inf bits (S kept then).
 template <bool FLOW, int W>
-__device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, const Tile<W> t,
-                                       int* flags_out) {
+__device__ __forceinline__ int full_rates_body(const EnsDev& E, Slot& sl, int Z, int S, float wz1, const Tile<W>& t,
+                                               int* flags_out) {
   const int lane = t.lane;
   const int np = Z - 1;
   int emax = -200, flags = 0;
@@ -429,6 +429,15 @@ __device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, 
   t.sync();
   *flags_out = flags;
   return Snew;
+}
+
+// Equilibrium ensembles run the full pass only at window starts and after
+// scale changes: out of line.  Flow runs it every event: inlined (no call,
+// no register save and restore around it).
+template <bool FLOW, int W>
+__device__ __noinline__ int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, const Tile<W> t,
+                                       int* flags_out) {
+  return full_rates_body<FLOW, W>(E, sl, Z, S, wz1, t, flags_out);
 }
 
 // ------------------------------------------------------------------ correlator
@@ -868,7 +877,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (4) rates: flow recomputes everything; equilibrium refreshes the chain
       // ends when a strand next to an end changed
       if (FLOW) {
-        S = full_rates<true, W>(E, sl, Z, S, wz1, t, &pend);
+        S = full_rates_body<true, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
       } else if (ends_dirty) {
         int over = 0;

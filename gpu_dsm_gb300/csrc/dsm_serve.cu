@@ -99,6 +99,8 @@ struct dsm_server {
   double chunk_s = 0.05;     // target duration of one chunk; < 0: whole-request windows
   double rate_est = 1.0e9;   // aggregate kMC events/s while work is in flight
   int policy = 0;            // 0 first come first served with backfill, 1 equal pace per chain
+  double overlap = 1.5;      // running requests may fill up to this many GPUs' worth of chain slots
+  double bypass = 0.2;       // requests shorter than bypass * chunk_s of the whole GPU run at once
   int prio_least = 0, prio_greatest = 0;  // CUDA stream priority range
   int sm_slots = 4864;       // chains resident on the GPU at full occupancy (152 SMs x 32)
   std::mutex mu;
@@ -253,7 +255,7 @@ int dsm_server::start_chunk(Req* r, double chains_total, int rank) {
   double dtau = std::numeric_limits<double>::infinity();
   if (chunk_s > 0.0) {
     double ev;
-    if (policy == 0) {
+    if (policy != 1) {
       const double slots = (double)sm_slots;
       const double eps = r->eps > 0.0 ? r->eps : rate_est * std::min(1.0, n / slots);
       ev = std::max(eps * chunk_s, 64.0 * n);
@@ -262,7 +264,7 @@ int dsm_server::start_chunk(Req* r, double chains_total, int rank) {
     }
     dtau = ev / std::max(r->rate, 1.0);
   }
-  if (policy == 0) dsm_set_priority(r->sim, prio_greatest + std::min(rank, prio_least - prio_greatest));
+  if (policy != 1) dsm_set_priority(r->sim, prio_greatest + std::min(rank, prio_least - prio_greatest));
   r->t_chunk = clk::now();
   if (r->flow) {
     const int64_t left = r->n_outputs - r->k_out;
@@ -338,13 +340,13 @@ void dsm_server::run() {
     // slots free (the oldest always runs); a request whose remaining work
     // is below one chunk of the whole GPU runs at once.  Equal pace runs all.
     double occ = 0.0;
-    const double short_work = rate_est * std::max(chunk_s, 0.0);
+    const double short_work = rate_est * std::max(chunk_s, 0.0) * bypass;
     for (Req* r : active) {
       const int my_rank = rank++;
       bool may_run = true;
-      if (policy == 0 && chunk_s > 0.0) {
+      if ((policy == 0 || policy == 2) && chunk_s > 0.0) {
         const double rem = (r->P.t_end - r->t_cur) * r->rate;
-        may_run = r->inflight || occ < 1.0 || rem < short_work;
+        may_run = r->inflight || occ < overlap || (policy == 0 && rem < short_work);
         occ += r->occupancy;
       }
       if (!may_run) { still.push_back(r); continue; }
@@ -430,9 +432,17 @@ extern "C" int dsm_serve_open(int32_t device, uint64_t hbm_budget_bytes, int32_t
 }
 
 extern "C" int dsm_serve_set_policy(dsm_server* s, int32_t policy) {
-  if (!s || (policy != 0 && policy != 1)) return DSM_ERR_INVALID;
+  if (!s || policy < 0 || policy > 2) return DSM_ERR_INVALID;
   std::lock_guard<std::mutex> lk(s->mu);
   s->policy = policy;
+  return DSM_OK;
+}
+
+extern "C" int dsm_serve_tune(dsm_server* s, double overlap, double bypass) {
+  if (!s || !(overlap >= 1.0) || !(bypass >= 0.0)) return DSM_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->overlap = overlap;
+  s->bypass = bypass;
   return DSM_OK;
 }
 
