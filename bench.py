@@ -46,7 +46,8 @@ def config(window: float, n_gpus: int) -> dict:
     return {"workload": f"equilibrium monodisperse melt: {N_CHAINS} chains x N_K={NK}, beta={BETA}, CD on, "
                         f"G(t) multi-tau p={CORR_P} m={CORR_M} over xy/yz/xz (levels for t_end=1e7, dt=1)",
             "n_chains_per_gpu": N_CHAINS, "nk": NK, "beta": BETA, "window_tau_per_step": window,
-            "l2": "inputs larger than L2 (state ~0.85 GB per GPU); no flush", "parallelism": f"chains x{n_gpus} (replicas)"}
+            "l2": "inputs larger than L2 (state ~0.85 GB per GPU); no flush",
+            "parallelism": f"chains sharded over {n_gpus} GPU(s), G(t) sums all-reduced at output"}
 
 
 # ---------------------------------------------------------------- clocks
@@ -190,9 +191,12 @@ def run_gpu(args):
         torch.distributed.barrier()
     torch.cuda.set_device(local)
 
+    # one ensemble of world x N_CHAINS chains sharded over the ranks (weak
+    # scaling): rank r holds chains [r*N_CHAINS, (r+1)*N_CHAINS), random streams
+    # keyed by global chain id
     ens = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT, t_end=T_END_RUN,
-                       seed=1, stream=rank, device=local, corr_p=CORR_P, corr_m=CORR_M,
-                       lanes_per_chain=args.lanes)
+                       seed=1, device=local, corr_p=CORR_P, corr_m=CORR_M, lanes_per_chain=args.lanes,
+                       chain_offset=rank * N_CHAINS)
     ens.init_equilibrium()
     t = 0.0
     for _ in range(args.warmup):
@@ -217,8 +221,14 @@ def run_gpu(args):
     launches_per_step = max(1, len(sched))  # size classes + overflow launch, or one launch
     heads, qn, tau = ens.get_chains()
     zmean = float(heads["Z"].mean())
+    gt_points = None
     if world > 1:
         import torch.distributed as dist
+        from gpu_dsm_gb300 import sharded
+        # the exchange step: global G(t) from the per-rank correlator sums
+        _, g_all = sharded.sharded_gt(ens, n_total=world * N_CHAINS, p=CORR_P, m=CORR_M, sync_dt=SAMPLE_DT,
+                                      t_end=T_END_RUN)
+        gt_points = int(len(g_all))
         tt = torch.tensor([kms, float(events)], dtype=torch.float64, device="cuda")
         mx = tt.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
@@ -319,6 +329,7 @@ def run_gpu(args):
             "config": config(args.window, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clocks, "gpu_launches": args.steps * launches_per_step, "shear": shear, "serve": serve,
             "detail": {"events": events_all, "wall_s": wall, "kernel_ms_total": kms, "mean_Z": zmean,
+                       "sharded_gt_points": gt_points,
                        "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"], "schedule": sched}}
     print(json.dumps(line))
     ens.close()

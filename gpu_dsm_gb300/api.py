@@ -55,6 +55,8 @@ class DsmParams(C.Structure):
         ("gex_b", C.c_float),
         ("gex_mp", C.c_float),
         ("gex_mk", C.c_float),
+        ("chain_offset", C.c_uint32),
+        ("pad2_", C.c_int32),
     ]
 
 
@@ -200,7 +202,7 @@ def make_params(*, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[fl
                 cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
                 device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
                 stream: int = 0, warps_per_block: int = 0, s0: int = 0, lanes_per_chain: int = 0,
-                gex: Optional[Sequence[float]] = None) -> DsmParams:
+                gex: Optional[Sequence[float]] = None, chain_offset: int = 0) -> DsmParams:
     """dsm_params of an ensemble (input.dat fields, common/main_cuda.cu:55-68).
     gex = (a, b, mp, Mk) of polydisp.dat switches on the GEX background (pd_flag 1)."""
     p = DsmParams()
@@ -227,6 +229,7 @@ def make_params(*, beta: float = 1.0, nk: int, n_chains: int, kappa: Sequence[fl
     p.warps_per_block = warps_per_block
     p.s0 = s0
     p.lanes_per_chain = lanes_per_chain
+    p.chain_offset = chain_offset
     return p
 
 
@@ -243,13 +246,13 @@ class Ensemble:
                  cd_flag: int = 1, eq_type: int = 0, sync_dt: float = 1.0, t_end: float = 0.0, seed: int = 1,
                  device: int = 0, z_max: int = 0, corr_p: int = 0, corr_m: int = 0, corr_levels: int = 0,
                  stream: int = 0, nk_chain: Optional[np.ndarray] = None, warps_per_block: int = 0, s0: int = 0,
-                 lanes_per_chain: int = 0, gex: Optional[Sequence[float]] = None):
+                 lanes_per_chain: int = 0, gex: Optional[Sequence[float]] = None, chain_offset: int = 0):
         self._lib = load_library()
         self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
         p = make_params(beta=beta, nk=nk, n_chains=n_chains, kappa=kappa, cd_flag=cd_flag, eq_type=eq_type,
                         sync_dt=sync_dt, t_end=t_end, seed=seed, device=device, z_max=z_max, corr_p=corr_p,
                         corr_m=corr_m, corr_levels=corr_levels, stream=stream, warps_per_block=warps_per_block,
-                        s0=s0, lanes_per_chain=lanes_per_chain, gex=gex)
+                        s0=s0, lanes_per_chain=lanes_per_chain, gex=gex, chain_offset=chain_offset)
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
         self.params = p
         self.n_chains = n_chains

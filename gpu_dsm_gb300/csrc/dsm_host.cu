@@ -324,6 +324,7 @@ int dsm::sim_setup(dsm_sim* s) {
   E.beta = P.beta; E.prefact = s->prefact; E.beta_d = (double)P.beta;
   for (int q = 0; q < 9; ++q) E.kap[q] = P.kappa[q];
   E.seed_lo = (uint32_t)P.seed; E.seed_hi = (uint32_t)(P.seed >> 32); E.stream = P.stream;
+  E.chain_offset = P.chain_offset;
   E.dt_sample_ticks = s->corr ? (int64_t)std::llrint(P.sync_dt * TICKS) : 0;
   E.nsamples = s->nsamples;
   E.t_end_ticks = 0; E.step_limit = INT64_MAX; E.watchdog_events = INT64_MAX;

@@ -48,6 +48,8 @@ struct EnsDev {
   double beta_d;
   float kap[9];
   uint32_t seed_lo, seed_hi, stream;
+  uint32_t chain_offset;     // global id of local chain 0 (chains sharded over GPUs)
+  uint32_t pad_off_;
   int64_t dt_sample_ticks, nsamples;
   // window of the current launch
   int64_t t_end_ticks;       // chains stop when T >= t_end_ticks

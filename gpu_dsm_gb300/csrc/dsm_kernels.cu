@@ -123,7 +123,10 @@ __device__ __forceinline__ unsigned long long quant(float x, float sf) {
 // Philox words (counter layout shared with the oracle)
 __device__ __forceinline__ U4 rng_at(const EnsDev& E, uint32_t purpose, uint64_t ctr, uint32_t hi24,
                                      uint32_t chain) {
-  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain, E.stream, E.seed_lo, E.seed_hi);
+  // keyed by the global chain id: a chain's stream does not depend on how the
+  // chains are sharded over GPUs
+  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain + E.chain_offset, E.stream, E.seed_lo,
+                E.seed_hi);
 }
 
 // Lifetime samplers returning rates (gpu_random.cu:143-148, pcd_tau.h:67-82)

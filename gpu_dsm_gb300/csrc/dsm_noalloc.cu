@@ -140,6 +140,7 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   E.beta = p->beta; E.prefact = prefact; E.beta_d = be;
   for (int q = 0; q < 9; ++q) E.kap[q] = p->kappa[q];
   E.seed_lo = (uint32_t)p->seed; E.seed_hi = (uint32_t)(p->seed >> 32); E.stream = p->stream;
+  E.chain_offset = p->chain_offset;
   E.t_end_ticks = (int64_t)std::llrint(t_end * dsm::TICKS);
   E.step_limit = step_limit < 0 ? INT64_MAX : step_limit;
   // a chain that does 100x the expected events of the window (at least 2^24)

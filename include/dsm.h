@@ -78,6 +78,9 @@ typedef struct dsm_params {
                               values are scheduled first, clamped to the device's range) */
   float gex_a, gex_b;      /* pd_flag = 1: polydisp.dat a, b of the GEX background law */
   float gex_mp, gex_mk;    /* polydisp.dat mp (mass scale) and Mk (Kuhn-step mass) */
+  uint32_t chain_offset;   /* global id of chain 0 when an ensemble is sharded over GPUs:
+                              random streams are keyed by global chain id */
+  int32_t pad2_;
 } dsm_params;
 
 typedef struct dsm_sim dsm_sim;

@@ -76,6 +76,8 @@ typedef struct orc_params {
   float gex_step, gex_step_d, gex_scale;  // scale = mp/Mk
   int32_t pad2_;
   double gex_prefact;    // CD creation prefactor of the background law (ensemble.cu:137-146)
+  uint32_t chain_offset; // global id of chain 0 (Philox keyed by global chain id)
+  int32_t pad3_;
 } orc_params;
 }
 
@@ -269,7 +271,7 @@ struct Ensemble {
 };
 
 static inline U4 rng(const Ensemble& E, uint32_t purpose, uint64_t ctr, uint32_t hi24, uint32_t chain) {
-  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain, E.P.stream,
+  return philox((uint32_t)ctr, (purpose << 24) | (hi24 & 0xffffffu), chain + E.P.chain_offset, E.P.stream,
                 (uint32_t)E.P.seed, (uint32_t)(E.P.seed >> 32));
 }
 static inline U4 rng_step(const Ensemble& E, uint32_t purpose, uint64_t step, uint32_t chain) {

@@ -31,7 +31,7 @@ class OrcParams(C.Structure):
         ("nk_chain", C.c_void_p), ("s0", C.c_int32), ("gex", C.c_int32),
         ("gex_M", C.c_void_p), ("gex_Md", C.c_void_p), ("gex_n", C.c_int32), ("gex_nd", C.c_int32),
         ("gex_step", C.c_float), ("gex_step_d", C.c_float), ("gex_scale", C.c_float), ("pad2_", C.c_int32),
-        ("gex_prefact", C.c_double),
+        ("gex_prefact", C.c_double), ("chain_offset", C.c_uint32), ("pad3_", C.c_int32),
     ]
 
 
@@ -89,7 +89,8 @@ class Oracle:
 
     def __init__(self, *, beta=1.0, nk, n_chains, z_max=0, cd_flag=1, kappa=(0.0,) * 9, mode=0, seed=1,
                  stream=0, corr=False, corr_p=64, corr_m=8, corr_levels=0, sync_dt=1.0, t_end=0.0,
-                 nk_chain: Optional[np.ndarray] = None, s0=0, threads=0, msd=False, gex_tables=None):
+                 nk_chain: Optional[np.ndarray] = None, s0=0, threads=0, msd=False, gex_tables=None,
+                 chain_offset=0):
         L = lib()
         p = OrcParams()
         p.beta = float(np.float32(beta))
@@ -113,6 +114,7 @@ class Oracle:
         self._nk_chain = None if nk_chain is None else np.ascontiguousarray(nk_chain, dtype=np.int32)
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
         p.s0 = s0
+        p.chain_offset = chain_offset
         if gex_tables is not None:
             # GEX background: inverse tables and prefactor as the product builds them
             self._gex_M = np.ascontiguousarray(gex_tables["M"], np.float32)

@@ -324,3 +324,26 @@ def test_gex_background_bitexact(dsm_mod, oracle_mod, beta, kappa):
         g.advance(t)
         o.run(t)
     assert_bitexact(gpu_state(g), o.get_state(), what=f"gex beta={beta}")
+
+
+def test_chain_offset_shards_equal_one_ensemble(dsm_mod):
+    """Two handles holding chains [0, n/2) and [n/2, n) of one ensemble
+    (chain_offset) reproduce the single handle's chains bit for bit: random
+    streams are keyed by global chain id, so sharding over GPUs changes
+    nothing."""
+    n = 512
+    spec = dict(nk=40, seed=31, eq_type=1, sync_dt=1.0, t_end=50.0, corr_p=16, corr_m=2)
+    whole = dsm_mod.Ensemble(n_chains=n, **spec)
+    parts = [dsm_mod.Ensemble(n_chains=n // 2, chain_offset=k * (n // 2), **spec) for k in range(2)]
+    for e in [whole] + parts:
+        e.init_equilibrium()
+        e.advance(50.0)
+    sw = gpu_state(whole)
+    for k, e in enumerate(parts):
+        sp = gpu_state(e)
+        sl = slice(k * n // 2, (k + 1) * n // 2)
+        assert_bitexact(sp, {key: sw[key][sl] for key in sw}, keys=("Z", "QN", "tau", "T", "step", "hash"),
+                        what=f"shard {k}")
+    gw, _ = whole.gt_raw()
+    gp = sum(e.gt_raw()[0] for e in parts)
+    assert np.allclose(gp, gw, rtol=1e-12, atol=0.0)
