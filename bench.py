@@ -304,9 +304,14 @@ def run_gpu(args):
 
     if rank != 0:
         return 0
-    serve = shear = None
+    serve = shear = poly = None
     if world == 1:
         ens.close()
+    if not args.no_poly and world == 1:
+        try:
+            poly = run_poly(args, local)
+        except Exception as e:  # reported, never silently replaced
+            poly = {"failed": repr(e)}
     if not args.no_shear and world == 1:
         try:
             shear = run_shear(args, local)
@@ -327,7 +332,8 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": kms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic equilibrium melt",
             "config": config(args.window, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clocks, "gpu_launches": args.steps * launches_per_step, "shear": shear, "serve": serve,
+            "clocks": clocks, "gpu_launches": args.steps * launches_per_step, "shear": shear, "poly": poly,
+            "serve": serve,
             "detail": {"events": events_all, "wall_s": wall, "kernel_ms_total": kms, "mean_Z": zmean,
                        "sharded_gt_points": gt_points,
                        "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"], "schedule": sched}}
@@ -347,8 +353,8 @@ def run_shear(args, device: int = 0) -> dict:
     --shear-windows output windows after equilibrium start."""
     import gpu_dsm_gb300 as dsm
 
-    nk, n, t_end = 100, 32768, 5.0e5
-    dt_out = t_end / 1000.0
+    nk, n, t_end = 100, args.shear_chains, 5.0e5
+    dt_out = args.shear_window if args.shear_window > 0 else t_end / 1000.0
     tau_d = dsm.pcd(1.0, nk)["tau_d"]
     ens = [dsm.Ensemble(nk=nk, n_chains=n, beta=1.0, kappa=(0.0, wi / tau_d, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),
                         sync_dt=dt_out, t_end=t_end, seed=4, stream=k, device=device)
@@ -366,11 +372,41 @@ def run_shear(args, device: int = 0) -> dict:
         series.append([float(e.stress()[0][3]) for e in ens])
     for e in ens:
         e.close()
-    return {"workload": "4 x 32768 chains, N_K=100, beta=1, shear Wi {0.1,1,10,100}, kappa_xy=Wi/tau_d, "
+    return {"workload": f"4 x {n} chains, N_K=100, beta=1, shear Wi {{0.1,1,10,100}}, kappa_xy=Wi/tau_d, "
                         f"tau_d={tau_d:.4g}, output every {dt_out:g} tau_K",
             "windows": args.shear_windows, "events": ev_tot, "events_per_s": ev_tot / secs, "wall_s": secs,
             "sigma_xy_per_window": series,
             "timing": "host wall clock around dsm_advance_batch (launch + window + stress readback)"}
+
+
+# ---------------------------------------------------------------- polydisperse melt
+def run_poly(args, device: int = 0) -> dict:
+    """Batched polydisperse melt: 262144 chains, N_K log-normal (mean 150,
+    PDI 1.5 = exp(sigma^2), clipped to [10, 2000], seed 7), beta=1, G(t)
+    p=64 m=8 (levels for t_end=1e6).  One persistent launch per size class,
+    the schedule chosen by the online autotuner, then timed windows replayed
+    as one CUDA graph (dsm_advance_series)."""
+    import gpu_dsm_gb300 as dsm
+
+    n = args.poly_chains
+    rng = np.random.default_rng(7)
+    s2 = math.log(1.5)
+    nkc = np.clip(np.round(np.exp(rng.normal(math.log(150.0) - s2 / 2, math.sqrt(s2), size=n))), 10, 2000)
+    nkc = nkc.astype(np.int32)
+    e = dsm.Ensemble(nk=int(nkc.max()), n_chains=n, nk_chain=nkc, eq_type=1, sync_dt=1.0, t_end=1.0e6, corr_p=64,
+                     corr_m=8, seed=7, device=device)
+    e.init_equilibrium()
+    e.advance(args.poly_window)
+    best = e.autotune(args.poly_window)
+    ev, _ = e.advance_series(args.poly_window, args.poly_windows)
+    ms = e.last_window()["kernel_ms"]
+    sched = e.schedule()
+    e.close()
+    return {"workload": f"{n} chains, N_K log-normal mean 150 PDI 1.5 in [10, 2000] (mean {nkc.mean():.1f}, "
+                        f"max {int(nkc.max())}), beta=1, G(t) p=64 m=8",
+            "events_per_s": ev / (ms / 1e3), "events": int(ev), "kernel_ms": ms,
+            "windows": args.poly_windows, "window_tau": args.poly_window, "autotune": best, "schedule": sched,
+            "timing": "CUDA events around one graph replay of the windows (size-class launches + overflow launch)"}
 
 
 # ---------------------------------------------------------------- serving
@@ -502,6 +538,13 @@ def main():
     ap.add_argument("--no-shear", action="store_true", help="skip the shear start-up leg")
     ap.add_argument("--shear-only", action="store_true", help="run only the shear start-up leg")
     ap.add_argument("--shear-windows", type=int, default=2)
+    ap.add_argument("--no-poly", action="store_true", help="skip the polydisperse leg")
+    ap.add_argument("--poly-only", action="store_true", help="run only the polydisperse leg")
+    ap.add_argument("--poly-chains", type=int, default=262144)
+    ap.add_argument("--poly-window", type=float, default=2.0)
+    ap.add_argument("--poly-windows", type=int, default=4)
+    ap.add_argument("--shear-chains", type=int, default=32768, help="chains per shear ensemble")
+    ap.add_argument("--shear-window", type=float, default=0.0, help="tau_K per output window (0: t_end/1000)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-cal", type=int, default=16)
@@ -515,6 +558,11 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.poly_only:
+        from gpu_dsm_gb300 import build as native
+        native.build()
+        print(json.dumps({"poly": run_poly(args)}))
+        return 0
     if args.shear_only:
         from gpu_dsm_gb300 import build as native
         native.build()
