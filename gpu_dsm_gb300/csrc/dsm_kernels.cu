@@ -453,8 +453,8 @@ __device__ __forceinline__ int full_rates_body(const EnsDev& E, Slot& sl, int Z,
 }
 
 // Equilibrium ensembles run the full pass only at window starts and after
-// scale changes: out of line by default.  Flow runs its own fused pass every
-// event (flow_rates below), inlined.
+// scale changes: out of line by default.  Flow runs the body every event,
+// inlined (no call, no register save and restore around it).
 template <bool FLOW, int W>
 __device__ DSM_RATES_ATTR int full_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, const Tile<W> t,
                                        int* flags_out) {
@@ -476,98 +476,6 @@ __device__ __forceinline__ void flow_deform(const EnsDev& E, Slot& sl, int Z, fl
     sl.Q[s] = make_float4(nx, ny, nz, m_q2(nx, ny, nz));
   }
   t.sync();
-}
-
-// Flow step: the deformation by the pending dt and the full rate pass in one
-// sweep over the strands, W at a time.  The lane holding strand s deforms it,
-// keeps Q^2 and N in registers and evaluates pair (s-1, s) with its left
-// neighbour's values from the lane below (or, for the first lane, from the
-// last lane of the previous sweep), so no lane reads another lane's strand
-// from shared memory.  Same float operations in the same order as
-// flow_deform followed by full_rates_body<true>.
-template <int W>
-__device__ __forceinline__ int flow_rates(const EnsDev& E, Slot& sl, int Z, int S, float wz1, float dt_prev,
-                                          const Tile<W>& t, int* flags_out) {
-  const int lane = t.lane;
-  const int np = Z - 1;
-  const bool deform = dt_prev != 0.0f;
-  float a[9];
-#pragma unroll
-  for (int q = 0; q < 9; ++q) a[q] = __fmul_rn(dt_prev, E.kap[q]);
-  int emax = -200, flags = 0;
-  const float sf = pow2f(S);
-  float cq2 = 0.0f;  // Q^2 and N of the last strand of the previous sweep
-  int cn = 1;
-  for (int base = 0; base < Z; base += W) {
-    const int s = base + lane;
-    const bool in = s < Z;
-    float q2 = 0.0f;
-    int N = 1;
-    if (in) {
-      float4 q = sl.Q[s];
-      N = sl.N[s];
-      if (deform) {
-        const float nx = __fmaf_rn(a[2], q.z, __fmaf_rn(a[1], q.y, __fmaf_rn(a[0], q.x, q.x)));
-        const float ny = __fmaf_rn(a[5], q.z, __fmaf_rn(a[4], q.y, __fmaf_rn(a[3], q.x, q.y)));
-        const float nz = __fmaf_rn(a[8], q.z, __fmaf_rn(a[7], q.y, __fmaf_rn(a[6], q.x, q.z)));
-        q = make_float4(nx, ny, nz, m_q2(nx, ny, nz));
-        sl.Q[s] = q;
-      }
-      q2 = q.w;
-    }
-    float q2L = t.shfl_up(q2, 1);
-    int NL = t.shfl_up(N, 1);
-    if (lane == 0) { q2L = cq2; NL = cn; }
-    if (in && s >= 1) {
-      const int p = s - 1;
-      const float4 na = __ldg(&E.NT[NL]), nb = __ldg(&E.NT[N]);
-      float o[4];
-      o[0] = E.cd_flag ? sl.T[p] : 0.0f;
-      o[1] = shift_plus(E, NL, q2L, N, q2, na, nb);
-      o[2] = shift_minus(E, NL, q2L, N, q2, na, nb);
-      o[3] = E.cd_flag ? __ldg(&E.NE[NL]).w : 0.0f;
-      unsigned long long tot = 0;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int b = comp_bad(o[q]);
-        flags |= b;
-        if (!b) emax = max(emax, fexp(o[q]));
-        tot += quant(o[q], sf);
-      }
-      sl.R[p] = tot;
-      sl.P[p] = quant(o[1], sf);
-    }
-    cq2 = t.shfl(q2, W - 1);
-    cn = t.shfl(N, W - 1);
-  }
-  float ev = 0.0f;
-  if (lane < NEND) {
-    ev = end_comp(E, lane, Z, sl.N, wz1);
-    emax = max(emax, fexp(ev));
-    sl.R[np + lane] = quant(ev, sf);
-  }
-  emax = t.maxi(emax);
-  flags = t.or_(flags);
-  int Snew = S;
-  if (flags == 0) {
-    if (emax + S > LIMIT_E) Snew = LIMIT_E - emax;
-    else if (S < E.s0 && emax + S < LIMIT_E - S_HYST) Snew = min(E.s0, LIMIT_E - emax);
-  }
-  if (Snew != S) {
-    t.sync();  // Q, R and P written by the other lanes of the tile
-    const float sf2 = pow2f(Snew);
-    for (int p = lane; p < np; p += W) {
-      float o[4];
-      pair_floats(E, sl, p, o);
-      const unsigned long long qp = quant(o[1], sf2);
-      sl.R[p] = quant(o[0], sf2) + qp + quant(o[2], sf2) + quant(o[3], sf2);
-      sl.P[p] = qp;
-    }
-    if (lane < NEND) sl.R[np + lane] = quant(ev, sf2);
-  }
-  t.sync();
-  *flags_out = flags;
-  return Snew;
 }
 
 // ------------------------------------------------------------------ correlator
@@ -974,23 +882,19 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     bool words = false;  // Philox words of the current batch of W events loaded
 
     for (;;) {
+      // (1) flow: deformation by the previous dt (ensemble_kernel.cu:135-146)
+      if (FLOW && dt_prev != 0.0f) flow_deform<W>(E, sl, Z, dt_prev, t);
+      // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
+      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W, MSD>(E, sl, Z, c, T, t);
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207); a full
       // slot (a creation could need strand Z+1) ends the launch for this chain
       // at this step boundary, exactly like a window end
-      const bool stop = stall != 0 || T >= t_end || (long long)step >= step_lim || Z >= zlim;
-      const bool abort_now = !stop && abort_flag != nullptr && (step & 4095) == 4095 && *abort_flag != 0;
-      // (1) flow: the deformation by the previous dt comes first in every
-      // iteration (ensemble_kernel.cu:135-146); for a step that is taken it is
-      // done inside the fused pass of (4), for one that is not, here
-      if (FLOW && dt_prev != 0.0f && (stop || abort_now)) flow_deform<W>(E, sl, Z, dt_prev, t);
-      // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
-      if (CORR && T > sl.k0->t_next && sl.k0->k_next < E.nsamples) corr_samples<W, MSD>(E, sl, Z, c, T, t);
-      if (stop) {
+      if (stall != 0 || T >= t_end || (long long)step >= step_lim || Z >= zlim) {
         if (stall == 0 && T < t_end && (long long)step >= step_lim && step_lim != E.step_limit) stall = ST_WATCHDOG;
         dt_prev = 0.0f;
         break;
       }
-      if (abort_now) {
+      if (abort_flag != nullptr && (step & 4095) == 4095 && *abort_flag != 0) {
         if (lane == 0) atomicOr(status, 1);
         dt_prev = 0.0f;
         break;
@@ -999,7 +903,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // (4) rates: flow recomputes everything; equilibrium refreshes the chain
       // ends when a strand next to an end changed
       if (FLOW) {
-        S = flow_rates<W>(E, sl, Z, S, wz1, dt_prev, t, &pend);
+        S = full_rates_body<true, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
       } else if (ends_dirty) {
         int over = 0;
