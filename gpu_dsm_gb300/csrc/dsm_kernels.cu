@@ -254,6 +254,13 @@ __device__ __forceinline__ int comp_bad(float x) {
 }
 
 // ------------------------------------------------------------------ SMEM slot
+// Per-chain value that the event loop updates off its critical path: lane 0
+// keeps it in shared memory, so it holds no registers of the tile.
+struct ChainHdr {
+  uint64_t hash;  // FNV-1a hash of the event codes
+  long long pad_;
+};
+
 struct Corr0 {  // correlator level-0 counters of the resident chain
   int ins, navg;
   long long nins;
@@ -269,6 +276,7 @@ struct Slot {
   unsigned long long* P;    // quantised shift +1 component per pair
   int* N;                   // Kuhn steps per strand
   float* T;                 // CD lifetime rates per entanglement
+  ChainHdr* h;              // event hash of the resident chain
   Corr0* k0;                // correlator level-0 counters
   float* Csh;               // correlator level-0 shift register [p][3]
   float2* Cacc;             // correlator level-0 compensated sums [p]
@@ -279,7 +287,7 @@ __host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a -
 __host__ __device__ size_t step_slot_bytes(int slot_cap, int pmax) {
   const size_t n = (size_t)slot_cap + 1, nr = (size_t)slot_cap + NEND + 1;
   size_t b = n * 16 + nr * 8 + n * 8 + n * 4 + n * 4;
-  b = align_up(b, 16) + sizeof(Corr0);
+  b = align_up(b, 16) + sizeof(ChainHdr) + sizeof(Corr0);
   b = align_up(b, 8) + (size_t)pmax * 12;
   b = align_up(b, 8) + (size_t)pmax * 8;
   return align_up(b, 16);
@@ -294,8 +302,9 @@ __device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int
   s.N = (int*)(base + n * 24 + nr * 8);
   s.T = (float*)(base + n * 28 + nr * 8);
   size_t off = align_up(n * 32 + nr * 8, 16);
-  s.k0 = (Corr0*)(base + off);
-  off = align_up(off + sizeof(Corr0), 8);
+  s.h = (ChainHdr*)(base + off);
+  s.k0 = (Corr0*)(base + off + sizeof(ChainHdr));
+  off = align_up(off + sizeof(ChainHdr) + sizeof(Corr0), 8);
   s.Csh = (float*)(base + off);
   off = align_up(off + (size_t)pmax * 12, 8);
   s.Cacc = (float2*)(base + off);
@@ -822,7 +831,8 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     }
     int Z = st.Z, S = st.S, stall = st.stall;
     long long T = st.T;
-    uint64_t step = st.step, hash = st.hash;
+    uint64_t step = st.step;
+    if (lane == 0) sl.h->hash = st.hash;
     float dt_prev = st.dt_prev;
     // stop at step_lim; if the watchdog cap is the tighter one, stopping there
     // is a stall (step_lim then differs from E.step_limit)
@@ -1033,7 +1043,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       } else if (upn > 0 || ends_dirty) {
         rescan = true;
       }
-      hash = (hash ^ (uint64_t)code) * 0x100000001B3ull;
+      if (lane == 0) sl.h->hash = (sl.h->hash ^ (uint64_t)code) * 0x100000001B3ull;
       ++step;
       dt_prev = dt;
     }
@@ -1098,7 +1108,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       // a rescale at load is kept only if an event followed (as in the oracle)
       if (done > 0) cs->S = S;
       cs->Z = Z; cs->stall = stall; cs->dt_prev = dt_prev;
-      cs->T = T; cs->step = step; cs->hash = hash;
+      cs->T = T; cs->step = step; cs->hash = sl.h->hash;
       if (k_next >= 0) cs->k_next = k_next;
       if (MSD) {
         const Corr0& q = *sl.k0;
