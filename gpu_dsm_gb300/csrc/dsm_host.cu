@@ -814,16 +814,28 @@ int dsm::sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit) {
 }
 
 // ------------------------------------------------------------------ graph series
-// n windows as one CUDA graph: per window a one-thread kernel sets the end
-// time and event cap from a device array, then the step launch(es), then
-// (flow) the stress sums of the window into their own slot; at the end the
-// sums and counters go to pinned host memory.  One graph is captured per
-// (n, launch schedule) and replayed with new end times.
+// n windows as one CUDA graph, replayed with new end times; one graph is
+// captured per (n, launch schedule).  Equilibrium: per window a one-thread
+// kernel sets the end time and event cap from a device array, then the step
+// launch(es).  Flow: groups of up to kSeriesGroup windows run inside one step
+// launch (each chain records its stress at every window end it crosses and
+// keeps its state resident), followed by the stress sums of each window of
+// the group.  At the end the sums and counters go to pinned host memory.
+static constexpr int kSeriesGroup = 16;
+
+// bytes of the series buffer: window ends and caps, stress sums, and (flow)
+// the per-chain stress of one group of windows
+static size_t series_bytes(const dsm_sim* s, int cap) {
+  size_t b = (size_t)cap * (2 * sizeof(long long) + 9 * sizeof(double));
+  if (s->flow) b = (b + 255) / 256 * 256 + (size_t)std::min(cap, kSeriesGroup) * s->P.n_chains * 8 * sizeof(float);
+  return b;
+}
 static void series_free(dsm_sim* s) {
   for (auto& g : s->ser_graphs) cudaGraphExecDestroy(g.second);
   s->ser_graphs.clear();
   if (s->ser_d) cudaFreeAsync(s->ser_d, s->st);
   if (s->ser_h) cudaFreeHost(s->ser_h);
+  s->h.win_stress = nullptr;
   s->ser_d = nullptr;
   s->ser_h = nullptr;
   s->ser_cap = 0;
@@ -848,10 +860,18 @@ static int series_capture(dsm_sim* s, int n, cudaGraphExec_t* exec) {
   // timing events must be real event-record nodes (a plain record inside a
   // capture only orders streams)
   cap(cudaEventRecordWithFlags(s->ev0, s->st, cudaEventRecordExternal), "event");
-  for (int w = 0; w < n && rc == DSM_OK; ++w) {
-    cap(launch_window_begin(s->d_ens, d_win, s->ser_cap, w, s->st), "window begin");
-    if (rc == DSM_OK) rc = enqueue_step(s);
-    if (s->flow && rc == DSM_OK) cap(launch_stress_reduce_dev(s->d_ens, d_out + 9 * w, s->st), "stress");
+  if (s->flow) {
+    for (int w0 = 0; w0 < n && rc == DSM_OK; w0 += kSeriesGroup) {
+      const int k = std::min(kSeriesGroup, n - w0);
+      cap(launch_series_begin(s->d_ens, d_win + w0, s->ser_cap, k, s->P.n_chains, s->d_cs, s->st), "series begin");
+      if (rc == DSM_OK) rc = enqueue_step(s);
+      if (rc == DSM_OK) cap(launch_series_reduce(s->d_ens, d_out + 9 * w0, k, s->st), "stress");
+    }
+  } else {
+    for (int w = 0; w < n && rc == DSM_OK; ++w) {
+      cap(launch_window_begin(s->d_ens, d_win, s->ser_cap, w, s->st), "window begin");
+      if (rc == DSM_OK) rc = enqueue_step(s);
+    }
   }
   cap(cudaEventRecordWithFlags(s->ev1, s->st, cudaEventRecordExternal), "event");
   cap(cudaMemcpyAsync(ser_out_h(s), d_out, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st), "copy");
@@ -874,10 +894,11 @@ static int series_prepare(dsm_sim* s, int n, cudaGraphExec_t* exec) {
     int cap = std::max(n, s->ser_cap);
     if (s->ser_version == s->sched_version || cap < 16) cap = std::max(cap, 16);
     series_free(s);
-    const size_t bytes = (size_t)cap * (2 * sizeof(long long) + 9 * sizeof(double));
-    CK(cudaMallocAsync(&s->ser_d, bytes, s->st));
-    CK(cudaHostAlloc(&s->ser_h, bytes, cudaHostAllocDefault));
+    const size_t hbytes = (size_t)cap * (2 * sizeof(long long) + 9 * sizeof(double));
+    CK(cudaMallocAsync(&s->ser_d, series_bytes(s, cap), s->st));
+    CK(cudaHostAlloc(&s->ser_h, hbytes, cudaHostAllocDefault));
     s->ser_cap = cap;
+    if (s->flow) s->h.win_stress = (float*)((char*)s->ser_d + (hbytes + 255) / 256 * 256);
     s->ser_version = s->sched_version;
   }
   for (auto& g : s->ser_graphs)

@@ -86,6 +86,13 @@ struct EnsDev {
   int4* corr_cnt;
   float* out_stress;               // [chain][8] stress at the end of the launch (flow)
   unsigned long long* counters;    // [0] events this launch, [1] chains done
+  // flow output series inside one launch (n_win > 0): window w ends at
+  // win[w] ticks with event cap win[win_stride + w]; a chain records its stress
+  // at each window end in win_stress[w][chain][8] and keeps running; its next
+  // window is ChainState::k_next (reset to 0 before the launch)
+  const long long* win;
+  float* win_stress;
+  int32_t n_win, win_stride;
 };
 
 struct LaunchCfg {
@@ -112,6 +119,12 @@ struct StepList {
 
 // kernels (dsm_kernels.cu)
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
+// flow output series: point the descriptor at windows d_win[0 .. n) (event
+// caps at d_win[stride + w]) and reset every chain's window index
+cudaError_t launch_series_begin(EnsDev* d_ens, const long long* d_win, int stride, int n, int n_chains,
+                                ChainState* d_cs, cudaStream_t st);
+// stress sums of windows 0 .. n of a flow series into out[9 w .. 9 w + 9)
+cudaError_t launch_series_reduce(const EnsDev* d_ens, double* out, int n, cudaStream_t st);
 cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefix, long long total,
                         unsigned int* d_work, bool flow, int corr, const LaunchCfg& cfg,
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,

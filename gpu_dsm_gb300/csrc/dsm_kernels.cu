@@ -487,6 +487,31 @@ __device__ __forceinline__ void flow_deform(const EnsDev& E, Slot& sl, int Z, fl
   t.sync();
 }
 
+// Stress of the resident chain, sigma_ab = -sum 3 Q_a Q_b / N, Lpp = sum |Q|,
+// and Z (ensemble_kernel.cu:504-538); lane 0 writes the 8 floats to o
+template <int W>
+__device__ __forceinline__ void flow_stress(const EnsDev& E, const Slot& sl, int Z, const Tile<W>& t, float* o) {
+  float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = t.lane; i < Z; i += W) {
+    const float4 q = sl.Q[i];
+    const float w = __ldg(&E.INV3N[sl.N[i]]);
+    s[0] = __fmaf_rn(-__fmul_rn(q.x, q.x), w, s[0]);
+    s[1] = __fmaf_rn(-__fmul_rn(q.y, q.y), w, s[1]);
+    s[2] = __fmaf_rn(-__fmul_rn(q.z, q.z), w, s[2]);
+    s[3] = __fmaf_rn(-__fmul_rn(q.x, q.y), w, s[3]);
+    s[4] = __fmaf_rn(-__fmul_rn(q.y, q.z), w, s[4]);
+    s[5] = __fmaf_rn(-__fmul_rn(q.x, q.z), w, s[5]);
+    s[6] = __fadd_rn(s[6], __fsqrt_rn(q.w));
+  }
+#pragma unroll
+  for (int q = 0; q < 7; ++q) s[q] = t.sum(s[q]);
+  if (t.lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 7; ++q) o[q] = s[q];
+    o[7] = (float)Z;
+  }
+}
+
 // ------------------------------------------------------------------ correlator
 // Levels >= 1 of the multi-tau correlator in HBM (eq_ensemble_kernel.cu:133-227):
 // push w into level 1 and cascade while blocks complete.  Stress (type 0):
@@ -836,9 +861,18 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     float dt_prev = st.dt_prev;
     // stop at step_lim; if the watchdog cap is the tighter one, stopping there
     // is a stall (step_lim then differs from E.step_limit)
-    const long long step_lim = (E.watchdog_events < E.step_limit - (long long)step)
-                                   ? (long long)step + E.watchdog_events : E.step_limit;
-    const long long t_end = E.t_end_ticks;
+    long long t_end = E.t_end_ticks;
+    long long wd = E.watchdog_events;
+    // flow output series: the chain's next window of this launch
+    int win = 0;
+    const bool series = FLOW && E.n_win > 0;
+    if (series) {
+      win = (int)st.k_next;
+      t_end = win < E.n_win ? E.win[win] : INT64_MIN;
+      wd = win < E.n_win ? E.win[E.win_stride + win] : 0;
+    }
+    long long step_lim = (wd < E.step_limit - (long long)step) ? (long long)step + wd : E.step_limit;
+    bool aborted = false;
     const float4* gq = E.QN + (size_t)c * cap;
     const float* gt = E.tau + (size_t)c * cap;
     for (int s = lane; s < Z; s += W) {
@@ -902,11 +936,24 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       if (stall != 0 || T >= t_end || (long long)step >= step_lim || Z >= zlim) {
         if (stall == 0 && T < t_end && (long long)step >= step_lim && step_lim != E.step_limit) stall = ST_WATCHDOG;
         dt_prev = 0.0f;
+        // a window of a flow series ends: record the stress and go on with
+        // the next window, exactly as a new launch would (no deformation by
+        // the last dt, event cap counted from here)
+        if (series && stall == 0 && T >= t_end && win < E.n_win) {
+          flow_stress<W>(E, sl, Z, t, E.win_stress + ((size_t)win * E.n_chains + c) * 8);
+          if (++win < E.n_win) {
+            t_end = E.win[win];
+            wd = E.win[E.win_stride + win];
+            step_lim = (wd < E.step_limit - (long long)step) ? (long long)step + wd : E.step_limit;
+            continue;
+          }
+        }
         break;
       }
       if (abort_flag != nullptr && (step & 4095) == 4095 && *abort_flag != 0) {
         if (lane == 0) atomicOr(status, 1);
         dt_prev = 0.0f;
+        aborted = true;
         break;
       }
       const int np = Z - 1;
@@ -1051,28 +1098,12 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
     // stopped early because the slot is full (an abort ends the launch anyway)
     const bool deferred = E.cap > slot_cap && Z >= slot_cap && stall == 0 && T < t_end && (long long)step < step_lim;
     // ---- flow: stress at the end of the window (ensemble_kernel.cu:504-538)
-    if (FLOW && !deferred) {
-      float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      for (int i = lane; i < Z; i += W) {
-        const float4 q = sl.Q[i];
-        const float w = __ldg(&E.INV3N[sl.N[i]]);
-        s[0] = __fmaf_rn(-__fmul_rn(q.x, q.x), w, s[0]);
-        s[1] = __fmaf_rn(-__fmul_rn(q.y, q.y), w, s[1]);
-        s[2] = __fmaf_rn(-__fmul_rn(q.z, q.z), w, s[2]);
-        s[3] = __fmaf_rn(-__fmul_rn(q.x, q.y), w, s[3]);
-        s[4] = __fmaf_rn(-__fmul_rn(q.y, q.z), w, s[4]);
-        s[5] = __fmaf_rn(-__fmul_rn(q.x, q.z), w, s[5]);
-        s[6] = __fadd_rn(s[6], __fsqrt_rn(q.w));
-      }
-#pragma unroll
-      for (int q = 0; q < 7; ++q) s[q] = t.sum(s[q]);
-      if (lane == 0) {
-        float* o = E.out_stress + (size_t)c * 8;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) o[q] = s[q];
-        o[7] = (float)Z;
-      }
-    }
+    if (FLOW && !deferred && !series) flow_stress<W>(E, sl, Z, t, E.out_stress + (size_t)c * 8);
+    // a chain that stalled stands still for the remaining windows of a series
+    // and is left out of their sums (NaN marker, as a stalled chain is left
+    // out at the end of a launch)
+    if (series && !deferred && !aborted && lane == 0)
+      for (int w = win; w < E.n_win; ++w) E.win_stress[((size_t)w * E.n_chains + c) * 8] = __int_as_float(0x7fc00000);
     // ---- correlator level 0 back to HBM (compensated FP32 sums -> FP64)
     long long k_next = -1;  // -1: unchanged (no correlator)
     if (CORR) {
@@ -1110,6 +1141,7 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       cs->Z = Z; cs->stall = stall; cs->dt_prev = dt_prev;
       cs->T = T; cs->step = step; cs->hash = sl.h->hash;
       if (k_next >= 0) cs->k_next = k_next;
+      if (series) cs->k_next = win;
       if (MSD) {
         const Corr0& q = *sl.k0;
         cs->r1[0] = q.r1x; cs->r1[1] = q.r1y; cs->r1[2] = q.r1z;
@@ -1306,6 +1338,46 @@ __global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
   if (threadIdx.x < 9) out[threadIdx.x] = red[threadIdx.x][0];
 }
 
+// Flow series: windows d_win[0 .. n) with event caps at d_win[stride + w];
+// every chain starts at window 0
+__global__ void k_series_begin(EnsDev* ens, const long long* d_win, int stride, int n, ChainState* cs,
+                               int n_chains) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    ens->win = d_win;
+    ens->win_stride = stride;
+    ens->n_win = n;
+  }
+  if (i < n_chains) cs[i].k_next = 0;
+}
+
+// Stress sums of window blockIdx.x of a flow series, in the order of
+// k_stress_reduce (same per-thread strides, same tree)
+__global__ void k_series_reduce(const EnsDev* __restrict__ ensp, double* out) {
+  const EnsDev& E = *ensp;
+  __shared__ double red[9][256];
+  double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const float* base = E.win_stress + (size_t)blockIdx.x * E.n_chains * 8;
+  for (int c = threadIdx.x; c < E.n_chains; c += blockDim.x) {
+    const float* s = base + (size_t)c * 8;
+    if (s[0] != s[0]) continue;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] += (double)s[q];
+    a[8] += 1.0;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) red[q][threadIdx.x] = a[q];
+  __syncthreads();
+  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 9) out[(size_t)blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
+}
+
 // Window w of a captured series: end time d_win[w] and event cap d_win[n+w]
 __global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win, int n, int w) {
   ens->t_end_ticks = d_win[w];
@@ -1400,6 +1472,15 @@ cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double*
 }
 cudaError_t launch_window_begin(EnsDev* d_ens, const long long* d_win, int n, int w, cudaStream_t st) {
   k_window_begin<<<1, 1, 0, st>>>(d_ens, d_win, n, w);
+  return cudaGetLastError();
+}
+cudaError_t launch_series_begin(EnsDev* d_ens, const long long* d_win, int stride, int n, int n_chains,
+                                ChainState* d_cs, cudaStream_t st) {
+  k_series_begin<<<(n_chains + 255) / 256, 256, 0, st>>>(d_ens, d_win, stride, n, d_cs, n_chains);
+  return cudaGetLastError();
+}
+cudaError_t launch_series_reduce(const EnsDev* d_ens, double* out, int n, cudaStream_t st) {
+  k_series_reduce<<<n, 256, 0, st>>>(d_ens, out);
   return cudaGetLastError();
 }
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st) {

@@ -265,6 +265,76 @@ def test_graph_series_size_classes(dsm_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("lanes", [0, 32])
+def test_flow_series_groups(dsm_mod, oracle_mod, lanes):
+    """A flow series runs up to 16 output windows inside one step launch
+    (stress recorded at every window end): 40 short windows (about three
+    events per chain each, so some chains cross windows without an event)
+    equal 40 dsm_advance calls, stress after every window and state bit for
+    bit, with one chain stalled (NaN conformation) left out of every sum; the
+    state also equals the oracle's."""
+    kap = (0.0, 4.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    spec = dict(nk=40, n_chains=300, kappa=kap, seed=41, lanes_per_chain=lanes)
+    a = dsm_mod.Ensemble(**spec)
+    b = dsm_mod.Ensemble(**spec)
+    o = oracle_mod.Oracle(nk=40, n_chains=300, kappa=kap, seed=41)
+    for x in (a, b, o):
+        x.init_equilibrium()
+    ev_o = o.run(1.0)
+    for x in (a, b):
+        assert x.advance(1.0) == ev_o
+    assert_bitexact(gpu_state(a), o.get_state(), what="start")
+    dt, n = 0.3, 40
+    sa, ev_a = [], 0
+    for w in range(1, n + 1):
+        ev_a += a.advance(1.0 + dt * w)
+        sa.append(a.stress()[0])
+    ev_b, sb = b.advance_series(dt, n)
+    assert ev_b == ev_a
+    assert np.array_equal(np.array(sa, np.float32), sb)
+    assert_bitexact(gpu_state(b), gpu_state(a), what="flow series vs windows")
+    assert ev_a == o.run(1.0 + dt * n)
+    assert_bitexact(gpu_state(b), o.get_state(), what="flow series vs oracle")
+    # one chain stalls at its next event; it stays out of every window's sum
+    for x in (a, b):
+        heads, qn, tau = x.get_chains()
+        qn[7, 1, 0] = np.nan
+        x.set_chains(heads, qn, tau)
+    t0, sa = 1.0 + dt * n, []
+    for w in range(1, 21):
+        a.advance(t0 + dt * w)
+        sa.append(a.stress())
+    _, sb = b.advance_series(dt, 20)
+    assert all(c == 299 for _, c in sa)
+    assert np.array_equal(np.array([s for s, _ in sa], np.float32), sb)
+    assert_bitexact(gpu_state(b), gpu_state(a), what="flow series with a stalled chain")
+
+
+def test_flow_series_size_classes(dsm_mod, oracle_mod):
+    """Flow series of a polydisperse melt in size classes: a chain that
+    outgrows its small slot inside a window group finishes the remaining
+    windows of the group in the overflow launch, with the same stress and
+    state as separate windows and the oracle."""
+    nkc = _lognormal_nk(300, 43, 120, 0.6, 10, 700)
+    kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=300, seed=47, nk_chain=nkc, kappa=kap)
+    h = dsm_mod.Ensemble(nk=int(nkc.max()), n_chains=300, seed=47, nk_chain=nkc, kappa=kap)
+    for x in (g, h):
+        x.set_schedule(small_slot=40, z_margin_sd=0.01)
+        x.init_equilibrium()
+    o.init_equilibrium()
+    sh, ev_h = [], 0
+    for w in range(1, 25):
+        ev_h += h.advance(0.5 * w)
+        sh.append(h.stress()[0])
+    ev, sg = g.advance_series(0.5, 24)
+    assert ev == ev_h == o.run(12.0)
+    assert np.array_equal(np.array(sh, np.float32), sg)
+    assert_bitexact(gpu_state(g), gpu_state(h), what="flow series in size classes vs windows")
+    assert_bitexact(gpu_state(g), o.get_state(), what="flow series in size classes vs oracle")
+    assert g.window_stats()["deferred"] > 0
+
+
+@pytest.mark.parametrize("lanes", [0, 32])
 def test_msd_mode(dsm_mod, oracle_mod, lanes):
     """MSD mode (eq_type=2): chain state and the first-entanglement positions
     R1 bit for bit, MSD(t) sums within 1e-4 of the FP64 oracle (FP32 centre of
