@@ -384,8 +384,10 @@ def run_poly(args, device: int = 0) -> dict:
     """Batched polydisperse melt: 262144 chains, N_K log-normal (mean 150,
     PDI 1.5 = exp(sigma^2), clipped to [10, 2000], seed 7), beta=1, G(t)
     p=64 m=8 (levels for t_end=1e6).  One persistent launch per size class,
-    the schedule chosen by the online autotuner, then timed windows replayed
-    as one CUDA graph (dsm_advance_series)."""
+    the schedule chosen by the online autotuner on --poly-tune-window windows,
+    then --poly-windows timed windows of --poly-window tau_K (default 4 x 250,
+    1e3 tau_K as for the monodisperse workload) replayed as one CUDA graph
+    (dsm_advance_series)."""
     import gpu_dsm_gb300 as dsm
 
     n = args.poly_chains
@@ -396,8 +398,8 @@ def run_poly(args, device: int = 0) -> dict:
     e = dsm.Ensemble(nk=int(nkc.max()), n_chains=n, nk_chain=nkc, eq_type=1, sync_dt=1.0, t_end=1.0e6, corr_p=64,
                      corr_m=8, seed=7, device=device)
     e.init_equilibrium()
-    e.advance(args.poly_window)
-    best = e.autotune(args.poly_window)
+    e.advance(args.poly_tune_window)
+    best = e.autotune(args.poly_tune_window)
     ev, _ = e.advance_series(args.poly_window, args.poly_windows)
     ms = e.last_window()["kernel_ms"]
     sched = e.schedule()
@@ -541,8 +543,9 @@ def main():
     ap.add_argument("--no-poly", action="store_true", help="skip the polydisperse leg")
     ap.add_argument("--poly-only", action="store_true", help="run only the polydisperse leg")
     ap.add_argument("--poly-chains", type=int, default=262144)
-    ap.add_argument("--poly-window", type=float, default=2.0)
+    ap.add_argument("--poly-window", type=float, default=250.0, help="tau_K per timed polydisperse window")
     ap.add_argument("--poly-windows", type=int, default=4)
+    ap.add_argument("--poly-tune-window", type=float, default=5.0, help="tau_K per autotuner candidate window")
     ap.add_argument("--shear-chains", type=int, default=32768, help="chains per shear ensemble")
     ap.add_argument("--shear-window", type=float, default=0.0, help="tau_K per output window (0: t_end/1000)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")
