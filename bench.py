@@ -254,6 +254,12 @@ def run_gpu(args):
         tv[:] = tau
         ens2 = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT,
                             t_end=T_END_RUN, seed=2, device=local, corr_p=CORR_P, corr_m=CORR_M)
+        # results come back into pinned buffers of their own
+        o_heads = torch.empty(N_CHAINS * 16, dtype=torch.uint8, pin_memory=True)
+        o_qn = torch.empty(N_CHAINS * cap * 4, dtype=torch.float32, pin_memory=True)
+        o_tau = torch.empty(N_CHAINS * cap, dtype=torch.float32, pin_memory=True)
+        outs = (o_heads.numpy().view(dsm.api.HEAD_DTYPE), o_qn.numpy().reshape(N_CHAINS, cap, 4),
+                o_tau.numpy().reshape(N_CHAINS, cap))
         ev_e, t_e = 0, 0.0
         npts = 0
         for i in range(args.e2e_steps + 1):
@@ -261,7 +267,7 @@ def run_gpu(args):
             s0 = time.perf_counter()
             ens2.set_chains(hv, qv, tv)
             ev = ens2.advance(args.window)
-            h2, q2, t2 = ens2.get_chains()
+            ens2.get_chains(out=outs)
             tg, g = ens2.gt()
             torch.cuda.synchronize()
             s1 = time.perf_counter()

@@ -293,12 +293,19 @@ class Ensemble:
     def init_equilibrium(self) -> None:
         self._check(self._lib.dsm_init_equilibrium(self._h))
 
-    def get_chains(self):
-        """Returns (heads structured array, QN float32 [n, z_max, 4], tau float32 [n, z_max])."""
+    def get_chains(self, out=None):
+        """Returns (heads structured array, QN float32 [n, z_max, 4], tau float32 [n, z_max]),
+        written into ``out`` = (heads, qn, tau) when given (e.g. views of pinned host buffers)."""
         n, cap = self.n_chains, self.z_max
-        heads = np.zeros(n, dtype=HEAD_DTYPE)
-        qn = np.zeros((n, cap, 4), dtype=np.float32)
-        tau = np.zeros((n, cap), dtype=np.float32)
+        if out is not None:
+            heads, qn, tau = out
+            assert heads.dtype == HEAD_DTYPE and heads.shape == (n,) and heads.flags.c_contiguous
+            assert qn.dtype == np.float32 and qn.shape == (n, cap, 4) and qn.flags.c_contiguous
+            assert tau.dtype == np.float32 and tau.shape == (n, cap) and tau.flags.c_contiguous
+        else:
+            heads = np.zeros(n, dtype=HEAD_DTYPE)
+            qn = np.zeros((n, cap, 4), dtype=np.float32)
+            tau = np.zeros((n, cap), dtype=np.float32)
         self._check(self._lib.dsm_get_chains(self._h, _ptr(heads), _ptr(qn), _ptr(tau)))
         return heads, qn, tau
 

@@ -656,21 +656,41 @@ extern "C" int dsm_set_chains(dsm_sim* s, const dsm_chain_head* heads, const dsm
   if (!s || !s->ready || !heads || !QN || !tau) return DSM_ERR_INVALID;
   const size_t n = s->P.n_chains, cap = s->cap;
   std::vector<ChainState> cs(n);
-  for (size_t i = 0; i < n; ++i) {
-    const int Z = heads[i].Z;
-    if (Z < 1 || Z > (int)cap) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": Z out of [1, z_max]");
-    long long sumN = 0;
-    for (int k = 0; k < Z; ++k) {
-      const float w = QN[i * cap + k].w;
-      if (!(w >= 1.0f) || w != std::floor(w)) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": strand with N < 1 or fractional N");
-      sumN += (long long)w;
+  // validate and build the chain states in parallel over chain ranges; the
+  // first bad chain in chain order is reported, as a serial pass would
+  const size_t nt = std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency(), n / 4096 + 1}));
+  std::vector<size_t> bad(nt, n);
+  std::vector<int> why(nt, 0);
+  auto work = [&](size_t r) {
+    const size_t i0 = n * r / nt, i1 = n * (r + 1) / nt;
+    for (size_t i = i0; i < i1; ++i) {
+      const int Z = heads[i].Z;
+      int code = 0;
+      if (Z < 1 || Z > (int)cap) code = 1;
+      long long sumN = 0;
+      for (int k = 0; k < Z && code == 0; ++k) {
+        const float w = QN[i * cap + k].w;
+        if (!(w >= 1.0f) || w != std::floor(w)) code = 2;
+        sumN += (long long)w;
+      }
+      if (code == 0 && sumN != s->nk_chain[i]) code = 3;
+      if (code != 0) { bad[r] = i; why[r] = code; return; }
+      ChainState& c = cs[i];
+      std::memset(&c, 0, sizeof(c));
+      c.Z = Z; c.stall = heads[i].stall_flag; c.S = s->h.s0; c.dt_prev = 0.f;
+      c.T = (int64_t)std::llrint((double)heads[i].time * TICKS);
+      c.step = 0; c.hash = 0xCBF29CE484222325ull; c.k_next = 0; c.nk = s->nk_chain[i];
     }
-    if (sumN != s->nk_chain[i]) return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(i) + ": sum of N differs from N_K");
-    ChainState& c = cs[i];
-    std::memset(&c, 0, sizeof(c));
-    c.Z = Z; c.stall = heads[i].stall_flag; c.S = s->h.s0; c.dt_prev = 0.f;
-    c.T = (int64_t)std::llrint((double)heads[i].time * TICKS);
-    c.step = 0; c.hash = 0xCBF29CE484222325ull; c.k_next = 0; c.nk = s->nk_chain[i];
+  };
+  std::vector<std::thread> pool;
+  for (size_t r = 1; r < nt; ++r) pool.emplace_back(work, r);
+  work(0);
+  for (auto& th : pool) th.join();
+  for (size_t r = 0; r < nt; ++r) {
+    if (bad[r] == n) continue;
+    static const char* const msg[] = {"", ": Z out of [1, z_max]", ": strand with N < 1 or fractional N",
+                                      ": sum of N differs from N_K"};
+    return fail(s, DSM_ERR_INVALID, "chain " + std::to_string(bad[r]) + msg[why[r]]);
   }
   CK(cudaMemcpyAsync(s->d_QN, QN, n * cap * sizeof(float4), cudaMemcpyHostToDevice, s->st));
   CK(cudaMemcpyAsync(s->d_tau, tau, n * cap * sizeof(float), cudaMemcpyHostToDevice, s->st));
@@ -684,6 +704,9 @@ extern "C" int dsm_set_chains(dsm_sim* s, const dsm_chain_head* heads, const dsm
 extern "C" int dsm_get_chains(dsm_sim* s, dsm_chain_head* heads, dsm_float4* QN, float* tau) {
   if (!s || !s->ready) return DSM_ERR_INVALID;
   const size_t n = s->P.n_chains, cap = s->cap;
+  // slots beyond Z are not maintained on the device: zero them there, so the
+  // copies come back in the reference layout without a host pass
+  if (QN || tau) CK(launch_clear_tail(s->d_QN, s->d_tau, s->d_cs, (int)n, (int)cap, s->st));
   if (QN) CK(cudaMemcpyAsync(QN, s->d_QN, n * cap * sizeof(float4), cudaMemcpyDeviceToHost, s->st));
   if (tau) CK(cudaMemcpyAsync(tau, s->d_tau, n * cap * sizeof(float), cudaMemcpyDeviceToHost, s->st));
   std::vector<ChainState> cs(heads ? n : 0);
@@ -696,22 +719,6 @@ extern "C" int dsm_get_chains(dsm_sim* s, dsm_chain_head* heads, dsm_float4* QN,
       heads[i].dummy = 0.f;
       heads[i].stall_flag = cs[i].stall;
     }
-  // slots beyond Z are not maintained on the device; clear them in the copy
-  if (QN || tau) {
-    std::vector<ChainState> zs(n);
-    if (heads) for (size_t i = 0; i < n; ++i) zs[i].Z = heads[i].Z;
-    else {
-      CK(cudaMemcpy(zs.data(), s->d_cs, n * sizeof(ChainState), cudaMemcpyDeviceToHost));
-    }
-    for (size_t i = 0; i < n; ++i) {
-      const int Z = zs[i].Z;
-      for (size_t k = (size_t)std::max(Z, 0); k < cap; ++k) {
-        if (QN) QN[i * cap + k] = dsm_float4{0.f, 0.f, 0.f, 0.f};
-        if (tau) tau[i * cap + k] = 0.f;
-      }
-      if (tau && Z >= 1) tau[i * cap + Z - 1] = 0.f;
-    }
-  }
   return DSM_OK;
 }
 

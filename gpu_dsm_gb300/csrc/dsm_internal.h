@@ -119,6 +119,9 @@ struct StepList {
 
 // kernels (dsm_kernels.cu)
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
+// zero the slots a chain does not use (strands >= Z, entanglements >= Z-1)
+cudaError_t launch_clear_tail(float4* d_QN, float* d_tau, const ChainState* d_cs, int n_chains, int cap,
+                              cudaStream_t st);
 // flow output series: point the descriptor at windows d_win[0 .. n) (event
 // caps at d_win[stride + w]) and reset every chain's window index
 cudaError_t launch_series_begin(EnsDev* d_ens, const long long* d_win, int stride, int n, int n_chains,

@@ -1338,6 +1338,17 @@ __global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
   if (threadIdx.x < 9) out[threadIdx.x] = red[threadIdx.x][0];
 }
 
+// Slots beyond a chain's strands are not maintained by the step kernel; the
+// reference layout has them zero.  One thread per (chain, slot).
+__global__ void k_clear_tail(float4* QN, float* tau, const ChainState* __restrict__ cs, int n_chains, int cap) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)n_chains * cap) return;
+  const int c = (int)(i / cap), k = (int)(i - (long long)c * cap);
+  const int Z = cs[c].Z;
+  if (k >= Z) QN[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (k >= Z - 1) tau[i] = 0.f;
+}
+
 // Flow series: windows d_win[0 .. n) with event caps at d_win[stride + w];
 // every chain starts at window 0
 __global__ void k_series_begin(EnsDev* ens, const long long* d_win, int stride, int n, ChainState* cs,
@@ -1472,6 +1483,13 @@ cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double*
 }
 cudaError_t launch_window_begin(EnsDev* d_ens, const long long* d_win, int n, int w, cudaStream_t st) {
   k_window_begin<<<1, 1, 0, st>>>(d_ens, d_win, n, w);
+  return cudaGetLastError();
+}
+cudaError_t launch_clear_tail(float4* d_QN, float* d_tau, const ChainState* d_cs, int n_chains, int cap,
+                              cudaStream_t st) {
+  const long long n = (long long)n_chains * cap;
+  if (n == 0) return cudaSuccess;
+  k_clear_tail<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_QN, d_tau, d_cs, n_chains, cap);
   return cudaGetLastError();
 }
 cudaError_t launch_series_begin(EnsDev* d_ens, const long long* d_win, int stride, int n, int n_chains,

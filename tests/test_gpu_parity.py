@@ -133,6 +133,39 @@ def test_set_get_roundtrip(dsm_mod, oracle_mod, tmp_path):
                     what="loaded")
 
 
+def test_chain_transfer_layout_and_validation(dsm_mod):
+    """dsm_get_chains returns the reference layout (slots beyond Z zero, the
+    entanglement slot of the last strand zero), also into caller buffers;
+    dsm_set_chains rejects the first bad chain in chain order and accepts the
+    state it returned."""
+    g = dsm_mod.Ensemble(nk=60, n_chains=9000, seed=5)
+    g.init_equilibrium()
+    g.advance(30.0)
+    heads, qn, tau = g.get_chains()
+    Z = heads["Z"].astype(np.int64)
+    idx = np.arange(g.z_max)[None, :]
+    assert np.all(qn[idx >= Z[:, None]] == 0.0)
+    assert np.all(tau[idx >= (Z - 1)[:, None]] == 0.0)
+    assert np.all(qn[idx < Z[:, None]][:, 3] >= 1.0)
+    out = (np.empty_like(heads), np.full_like(qn, 7.0), np.full_like(tau, 7.0))
+    g.get_chains(out=out)
+    assert np.array_equal(out[0], heads) and np.array_equal(out[1], qn) and np.array_equal(out[2], tau)
+    ok = gpu_state(g)
+    bad_q = qn.copy()
+    bad_q[8000, 0, 3] += 0.5          # fractional N, later in chain order
+    bad_q[6500, 0, 3] += 1.0          # sum of N off by one: the first bad chain
+    with pytest.raises(dsm_mod.api.DSMError, match="chain 6500: sum of N"):
+        g.set_chains(heads, bad_q, tau)
+    bad_h = heads.copy()
+    bad_h["Z"][100] = 0
+    with pytest.raises(dsm_mod.api.DSMError, match="chain 100: Z out of"):
+        g.set_chains(bad_h, qn, tau)
+    g.set_chains(heads, qn, tau)
+    h2, q2, t2 = g.get_chains()
+    assert np.array_equal(q2, qn) and np.array_equal(t2, tau) and np.array_equal(h2["Z"], heads["Z"])
+    assert np.array_equal(gpu_state(g)["Z"], ok["Z"])
+
+
 @pytest.mark.parametrize("nk,n,kappa,z_max", [(25, 1024, (0.0,) * 9, 0), (200, 256, (0.0,) * 9, 0),
                                               (50, 256, (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 0),
                                               (30, 256, (0.0,) * 9, 14)])
