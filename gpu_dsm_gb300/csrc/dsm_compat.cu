@@ -13,6 +13,7 @@
 #include <fstream>
 #include <iostream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/dsm.h"
@@ -179,19 +180,38 @@ extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadf
     std::cout << "output file: " << filename_ID("tau", job_ID) << '\n';
     std::cout << "performing time evolution for the ensemble..\n";
     std::cout << "time\tstress tensor(xx yy zz xy yz xz)\t<Lpp>\t<Z>\n";
-    for (double t_step = 0; t_step < in.t_end; t_step += in.sync_dt) {
+    // output times of the reference loop (main_cuda.cu:117-133): t_step += sync_dt
+    std::vector<double> ends;
+    for (double t_step = 0; t_step < in.t_end; t_step += in.sync_dt) ends.push_back(t_step + in.sync_dt);
+    // up to 64 outputs per graph replay; the chains run through 16 of them per
+    // step launch, recording the stress at each output time
+    constexpr size_t kOutGroup = 64;
+    std::vector<dsm_stress_plus> sp(kOutGroup);
+    for (size_t g0 = 0; g0 < ends.size(); g0 += kOutGroup) {
+      const int32_t k = (int32_t)std::min(kOutGroup, ends.size() - g0);
       poll();
-      rc = dsm_advance(sim, t_step + in.sync_dt, -1, &abort_word, nullptr);
+      if (abort_word) { dsm_destroy(sim); return -1; }
+      rc = dsm_series_start(sim, ends.data() + g0, k);
+      int32_t n_out = 0;
+      while (rc == DSM_OK) {
+        rc = dsm_poll(sim, nullptr, sp.data(), &n_out);
+        if (rc != DSM_PENDING) break;
+        rc = DSM_OK;
+        poll();
+        if (abort_word) dsm_abort(sim);
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+      }
       if (rc == DSM_ABORTED) { dsm_destroy(sim); return -1; }
       if (rc != DSM_OK) { std::cout << dsm_last_error(sim) << "\n"; dsm_destroy(sim); return rc; }
-      dsm_stress_plus sp;
-      dsm_stress(sim, &sp, nullptr);
-      std::cout << t_step + in.sync_dt << '\t' << sp.xx << ' ' << sp.yy << ' ' << sp.zz << ' ' << sp.xy << ' '
-                << sp.yz << ' ' << sp.zx << ' ' << sp.Lpp << ' ' << sp.Z << '\n';
-      tau_file << t_step + in.sync_dt << '\t' << sp.xx << ' ' << sp.yy << ' ' << sp.zz << ' ' << sp.xy << ' '
-               << sp.yz << ' ' << sp.zx << ' ' << sp.Lpp << ' ' << sp.Z << '\n';
+      for (int32_t w = 0; w < k; ++w) {
+        const dsm_stress_plus& q = sp[w];
+        std::cout << ends[g0 + w] << '\t' << q.xx << ' ' << q.yy << ' ' << q.zz << ' ' << q.xy << ' ' << q.yz << ' '
+                  << q.zx << ' ' << q.Lpp << ' ' << q.Z << '\n';
+        tau_file << ends[g0 + w] << '\t' << q.xx << ' ' << q.yy << ' ' << q.zz << ' ' << q.xy << ' ' << q.yz << ' '
+                 << q.zx << ' ' << q.Lpp << ' ' << q.Z << '\n';
+      }
       tau_file.flush();
-      if (progress_bar) *progress_bar = (int)(100.0 * (t_step + in.sync_dt) / in.t_end);
+      if (progress_bar) *progress_bar = (int)(100.0 * ends[g0 + k - 1] / in.t_end);
     }
     std::cout << "time evolution done.\n";
   } else if (in.eq_type == 1 || in.eq_type == 2) {

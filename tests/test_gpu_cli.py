@@ -60,6 +60,28 @@ def test_cli_flow_and_load(dsm_mod, tmp_path):
     assert table(tmp_path / "tau_2.dat").shape[0] >= 10
 
 
+def test_cli_flow_outputs_match_library(dsm_mod, tmp_path):
+    """tau.dat of a flow run (100 outputs, so more than one series replay)
+    holds the stress of one dsm_advance + dsm_stress per output time, to the
+    6 significant digits the driver prints."""
+    kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    write_input(tmp_path, nk=30, n=256, kappa=kap, eq=0, sync=0.5, t_end=50.0)
+    run(tmp_path, 5)
+    tau = table(tmp_path / "tau_5.dat")
+    e = dsm_mod.Ensemble(nk=30, n_chains=256, kappa=kap, seed=5, sync_dt=0.5, t_end=50.0)
+    e.init_equilibrium()
+    times, rows = [], []
+    t = 0.0
+    while t < 50.0:
+        e.advance(t + 0.5)
+        times.append(t + 0.5)
+        rows.append(e.stress()[0])
+        t += 0.5
+    assert tau.shape == (100, 9)
+    assert np.allclose(tau[:, 0], times, rtol=1e-6, atol=0)
+    assert np.allclose(tau[:, 1:], np.array(rows, np.float64), rtol=1e-5, atol=0)
+
+
 def test_cli_gex_background(dsm_mod, tmp_path):
     """pd_flag = 1 reads polydisp.dat (a b mp Mk) like the reference driver."""
     write_input(tmp_path, pd=1, eq=1, t_end=100.0)
