@@ -418,20 +418,27 @@ __device__ __forceinline__ int full_rates_body(const EnsDev& E, Slot& sl, int Z,
   const int np = Z - 1;
   int emax = -200, flags = 0;
   const float sf = pow2f(S);
+  // per component: NaN -> bit0, +inf -> bit1, else its exponent counts
+  // towards emax; bad components need not be excluded from the exponent
+  // maximum (any flag keeps the scale), so the largest |bits| gives it, and
+  // a NaN is exactly an |bits| above the infinity pattern
+  unsigned mx = 0u;
   for (int p = lane; p < np; p += W) {
     float o[4];
     pair_floats(E, sl, p, o);
     unsigned long long tot = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int b = comp_bad(o[q]);
-      flags |= b;
-      if (!b) emax = max(emax, fexp(o[q]));
+      const unsigned b = __float_as_uint(o[q]);
+      mx = max(mx, b & 0x7fffffffu);
+      if (b == 0x7f800000u) flags |= 2;
       tot += quant(o[q], sf);
     }
     sl.R[p] = tot;
     sl.P[p] = quant(o[1], sf);
   }
+  if (mx > 0x7f800000u) flags |= 1;
+  if (mx >= 0x00800000u) emax = max(emax, (int)(mx >> 23) - 127);
   float ev = 0.0f;
   if (lane < NEND) {
     ev = end_comp(E, lane, Z, sl.N, wz1);
