@@ -403,13 +403,22 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   if (small_cap <= 0) small_cap = full_cap;
   // one slot size fits all chains at full occupancy (or no useful split)
   if (small_cap >= s->cap || small_cap < 8) return plan_single(s);
+  // with two chains per warp in the small class, chains that outgrow its slot
+  // but fit a one-chain-per-warp slot at full occupancy run in a middle class
+  int mid_cap = 0;
+  if (sc.lanes == 16) {
+    LaunchCfg mc = sc;
+    mc.lanes = 32;
+    mid_cap = largest_slot(s->flow, s->ck, mc, 4, s->cap);
+    if (mid_cap <= small_cap) mid_cap = 0;
+  }
   // chains whose strand count is expected to stay below the small slot
   // (mean + margin_sd sd of 1 + Binomial(N_K - 1, 1/(1+beta)), plus 2) go there
   const double pe = 1.0 / (1.0 + (double)P.beta);
   const double msd = margin_sd > 0.f ? (double)margin_sd : 5.0;
-  std::vector<int> big, small;
+  std::vector<int> big, mid, small;
   int nk_big = 0;
-  double w_big = 0.0, w_all = 0.0;
+  double w_big = 0.0, w_mid = 0.0, w_all = 0.0;
   for (int i = 0; i < n; ++i) {
     const int nk = s->nk_chain[i];
     const double m = 1.0 + (nk - 1) * pe, sd = std::sqrt(std::max(0.0, (nk - 1) * pe * (1.0 - pe)));
@@ -417,25 +426,32 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     // work per tau_K: events ~ N_K, cost per event ~ strands + fixed part
     const double w = (double)nk * (m + 40.0);
     w_all += w;
-    if (zb > small_cap) { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
-    else small.push_back(i);
+    if (zb <= small_cap) small.push_back(i);
+    else if (zb <= mid_cap) { mid.push_back(i); w_mid += w; }
+    else { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
   }
   auto by_nk = [&](int a, int b) { return s->nk_chain[a] != s->nk_chain[b] ? s->nk_chain[a] > s->nk_chain[b] : a < b; };
   std::sort(big.begin(), big.end(), by_nk);
+  std::sort(mid.begin(), mid.end(), by_nk);
   std::sort(small.begin(), small.end(), by_nk);
   std::vector<int> order(big);
+  order.insert(order.end(), mid.begin(), mid.end());
   order.insert(order.end(), small.begin(), small.end());
   if (!s->d_order) {
     CK(cudaMallocAsync((void**)&s->d_order, (size_t)n * sizeof(int), s->st));
     CK(cudaMallocAsync((void**)&s->d_defer, (size_t)n * sizeof(int), s->st));
-    CK(cudaMallocAsync((void**)&s->d_works, 4 * sizeof(unsigned int), s->st));
+    CK(cudaMallocAsync((void**)&s->d_works, 8 * sizeof(unsigned int), s->st));
     CK(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, s->prio));
+    CK(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, s->prio));
     CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&s->ev_join2, cudaEventDisableTiming));
   }
   CK(cudaMemcpyAsync(s->d_order, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s->st));
   const int tiles_per_sm_full = 16;
-  SizeClass B, Sm;
+  SizeClass B, M, Sm;
+  B.stream = 1;
+  M.stream = 2;
   if (!big.empty()) {
     B.cfg = LaunchCfg{1, std::min(s->cap, nk_big), s->cfg.pmax, 32};
     B.bps = step_max_blocks_per_sm(s->flow, s->ck, B.cfg);
@@ -447,10 +463,20 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     g = (int)std::max<long long>(1, std::min<long long>(g, std::min<long long>(B.count, (long long)B.bps * s->sm_count)));
     B.grid = g;
   }
+  if (!mid.empty()) {
+    // persistent blocks of 4 chains, as many as its share of the work
+    M.cfg = LaunchCfg{4, mid_cap, s->cfg.pmax, 32};
+    M.bps = step_max_blocks_per_sm(s->flow, s->ck, M.cfg);
+    if (M.bps < 1) return fail(s, DSM_ERR_INVALID, "middle slot does not fit shared memory");
+    M.first = B.count;
+    M.count = (long long)mid.size();
+    const long long g = (long long)std::ceil(w_mid / std::max(w_all, 1.0) * tiles_per_sm_full * s->sm_count / 4.0);
+    M.grid = (int)std::max<long long>(1, std::min<long long>({g, (M.count + 3) / 4, (long long)M.bps * s->sm_count}));
+  }
   Sm.cfg = LaunchCfg{4, small_cap, s->cfg.pmax, sc.lanes};
   Sm.bps = step_max_blocks_per_sm(s->flow, s->ck, Sm.cfg);
   if (Sm.bps < 1) return fail(s, DSM_ERR_INVALID, "small slot does not fit shared memory");
-  Sm.first = B.count;
+  Sm.first = B.count + M.count;
   Sm.count = (long long)small.size();
   {
     const int tiles = 4 * 32 / Sm.cfg.lanes;
@@ -463,6 +489,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   if (s->cleanup.bps < 1) return fail(s, DSM_ERR_INVALID, "chain capacity does not fit one shared-memory slot");
   s->cleanup.grid = s->cleanup.bps * s->sm_count;
   if (B.count > 0) s->classes.push_back(B);
+  if (M.count > 0) s->classes.push_back(M);
   s->classes.push_back(Sm);
   s->blocks_per_sm = Sm.bps;
   s->grid = Sm.grid;
@@ -474,6 +501,7 @@ extern "C" void dsm_destroy(dsm_sim* s) {
   if (s->st) cudaStreamSynchronize(s->st);
   if (s->st) series_free(s);
   if (s->side) cudaStreamSynchronize(s->side);
+  if (s->side2) cudaStreamSynchronize(s->side2);
   void* ptrs[] = {s->d_tables, s->d_QN, s->d_tau, s->d_cs, s->d_stress, s->d_cshift, s->d_cacc, s->d_cavg,
                   s->d_ccnt, s->d_gsum, s->d_gcnt, s->d_pcd_by_nk, s->d_nk_chain, s->d_ens, s->d_prefix,
                   s->d_work, s->d_status, s->d_counters, s->d_red, s->d_order, s->d_defer, s->d_works, s->d_gex};
@@ -481,7 +509,9 @@ extern "C" void dsm_destroy(dsm_sim* s) {
   for (void* p : ptrs) if (p) cudaFreeAsync(p, s->st);
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
   if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->ev_join2) cudaEventDestroy(s->ev_join2);
   if (s->side) cudaStreamDestroy(s->side);
+  if (s->side2) cudaStreamDestroy(s->side2);
   dsm::host_words_give(s->hw);
   if (s->ev_done) cudaEventDestroy(s->ev_done);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -559,7 +589,7 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
       }
       const int rc = plan_classes(s, sm, 0, lanes, 0.f);
       if (rc != DSM_OK) return rc;
-      const int g0 = s->classes.size() > 1 ? s->classes[0].grid : 0;
+      const int g0 = s->classes.size() > 1 && s->classes[0].stream == 1 ? s->classes[0].grid : 0;
       if (g0 == 0) { cands.push_back({sm, 0, lanes}); continue; }
       for (int g : {std::max(1, g0 / 2), g0, 2 * g0}) cands.push_back({sm, g, lanes});
     }
@@ -609,7 +639,7 @@ extern "C" int dsm_get_schedule(const dsm_sim* s, int32_t* n_classes, int32_t* i
   if (!s || !n_classes) return DSM_ERR_INVALID;
   *n_classes = (int32_t)s->classes.size();
   if (info) {
-    for (int i = 0; i < 15; ++i) info[i] = 0;
+    for (int i = 0; i < DSM_SCHEDULE_INFO; ++i) info[i] = 0;
     int i = 0;
     auto put = [&](const SizeClass& k, long long count) {
       info[5 * i + 0] = k.cfg.slot_cap; info[5 * i + 1] = k.cfg.warps_per_block; info[5 * i + 2] = k.cfg.lanes;
@@ -779,23 +809,28 @@ static int enqueue_step(dsm_sim* s) {
                    s->d_abort, s->d_status, s->grid, s->st));
     return DSM_OK;
   }
-  // size classes: large-slot chains on the side stream first (their blocks
-  // are placed first), small-slot chains on the main stream; then the chains
-  // that outgrew their slot, in slots of the ensemble's full capacity
-  CK(cudaMemsetAsync(s->d_works, 0, 4 * sizeof(unsigned int), s->st));
+  // size classes: large-slot chains on the side stream first, then the
+  // middle class on the second side stream (their blocks are placed first),
+  // small-slot chains on the main stream; then the chains that outgrew their
+  // slot, in slots of the ensemble's full capacity
+  CK(cudaMemsetAsync(s->d_works, 0, 8 * sizeof(unsigned int), s->st));
   CK(cudaEventRecord(s->ev_fork, s->st));
   CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+  CK(cudaStreamWaitEvent(s->side2, s->ev_fork, 0));
   for (const SizeClass& k : s->classes) {
-    const bool large = k.cfg.warps_per_block == 1;
     StepList l;
     l.order = s->d_order + k.first;
     l.defer = s->d_defer;
     l.n_defer = s->d_works + 3;
-    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, s->d_works + (large ? 1 : 0), s->flow, s->ck, k.cfg,
-                   s->d_abort, s->d_status, k.grid, large ? s->side : s->st, l));
+    cudaStream_t st = k.stream == 1 ? s->side : k.stream == 2 ? s->side2 : s->st;
+    unsigned int* work = s->d_works + (k.stream == 1 ? 1 : k.stream == 2 ? 4 : 0);
+    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, work, s->flow, s->ck, k.cfg, s->d_abort, s->d_status,
+                   k.grid, st, l));
   }
   CK(cudaEventRecord(s->ev_join, s->side));
+  CK(cudaEventRecord(s->ev_join2, s->side2));
   CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
+  CK(cudaStreamWaitEvent(s->st, s->ev_join2, 0));
   StepList l;
   l.order = s->d_defer;
   l.dyn_total = s->d_works + 3;
@@ -1047,12 +1082,15 @@ extern "C" int dsm_set_priority(dsm_sim* s, int32_t priority) {
   // before the new streams' work by the synchronisation below
   CK(cudaStreamSynchronize(s->st));
   if (s->side) CK(cudaStreamSynchronize(s->side));
-  cudaStream_t st = nullptr, side = nullptr;
+  if (s->side2) CK(cudaStreamSynchronize(s->side2));
+  cudaStream_t st = nullptr, side = nullptr, side2 = nullptr;
   CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, pr));
   if (s->side) CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, pr));
+  if (s->side2) CK(cudaStreamCreateWithPriority(&side2, cudaStreamNonBlocking, pr));
   cudaStreamDestroy(s->st);
   s->st = st;
   if (s->side) { cudaStreamDestroy(s->side); s->side = side; }
+  if (s->side2) { cudaStreamDestroy(s->side2); s->side2 = side2; }
   s->prio = pr;
   return DSM_OK;
 }

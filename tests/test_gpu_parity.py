@@ -201,22 +201,30 @@ def _lognormal_nk(n, seed, mean, sd, lo, hi):
     return np.clip(np.round(np.exp(rng.normal(np.log(mean), sd, size=n))), lo, hi).astype(np.int32)
 
 
-@pytest.mark.parametrize("small_slot,margin,kappa", [
-    (0, 0.0, (0.0,) * 9),
-    (40, 0.01, (0.0,) * 9),
-    (40, 0.01, (0.0, 1.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)),
+@pytest.mark.parametrize("small_slot,margin,kappa,lanes", [
+    (0, 0.0, (0.0,) * 9, 0),
+    (40, 0.01, (0.0,) * 9, 0),
+    (40, 0.01, (0.0, 1.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 0),
+    (40, 0.01, (0.0,) * 9, 16),
+    (40, 0.01, (0.0, 1.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 16),
 ])
-def test_size_classes_bitexact(dsm_mod, oracle_mod, small_slot, margin, kappa):
+def test_size_classes_bitexact(dsm_mod, oracle_mod, small_slot, margin, kappa, lanes):
     """Polydisperse chains up to N_K=1200 in size classes (large slots, small
-    slots, overflow launch for chains that outgrow theirs) give the oracle's
+    slots, with two chains per warp also a middle class of one chain per warp,
+    overflow launch for chains that outgrow theirs) give the oracle's
     trajectories exactly, whatever the schedule."""
     nkc = _lognormal_nk(400, 21, 120, 0.9, 10, 1200)
     g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=400, seed=17, nk_chain=nkc, kappa=kappa)
     if small_slot:
-        g.set_schedule(small_slot=small_slot, z_margin_sd=margin)
+        g.set_schedule(small_slot=small_slot, z_margin_sd=margin, lanes=lanes)
     sch = g.schedule()
-    assert len(sch) == 3 and sch[0]["warps_per_block"] == 1 and sch[1]["warps_per_block"] == 4
-    assert sch[0]["chains"] + sch[1]["chains"] == 400
+    if lanes == 16:
+        assert len(sch) == 4 and [k["warps_per_block"] for k in sch] == [1, 4, 4, 1]
+        assert [k["lanes"] for k in sch[:3]] == [32, 32, 16] and min(k["chains"] for k in sch[:3]) > 0
+        assert sum(k["chains"] for k in sch[:3]) == 400
+    else:
+        assert len(sch) == 3 and sch[0]["warps_per_block"] == 1 and sch[1]["warps_per_block"] == 4
+        assert sch[0]["chains"] + sch[1]["chains"] == 400
     g.init_equilibrium()
     o.init_equilibrium()
     deferred = 0
