@@ -367,7 +367,7 @@ def run_shear(args, device: int = 0) -> dict:
            for k, wi in enumerate((0.1, 1.0, 10.0, 100.0))]
     for e in ens:
         e.init_equilibrium()
-    ev_tot, secs, series = 0, 0.0, []
+    ev_tot, secs, series, zs = 0, 0.0, [], []
     t = 0.0
     for w in range(args.shear_windows):
         t += dt_out
@@ -375,13 +375,26 @@ def run_shear(args, device: int = 0) -> dict:
         ev = dsm.advance_batch(ens, t)
         secs += time.perf_counter() - t0
         ev_tot += int(np.sum(ev))
-        series.append([float(e.stress()[0][3]) for e in ens])
+        st = [e.stress()[0] for e in ens]
+        series.append([float(x[3]) for x in st])
+        zs.append(float(np.mean([x[7] for x in st])))
     for e in ens:
         e.close()
+    rate = ev_tot / secs
+    # flow roofline: every pair rate is recomputed after the deformation, so
+    # L_flow(Z) = L_eq(Z) + 9 Z (deformation) + 40 (Z - 1) (pair rates)
+    zmean = float(np.mean(zs))
+    l_flow = 2.0 * (zmean - 1.0) + 152.0 + 9.0 * zmean + 40.0 * (zmean - 1.0)
+    f_max = float(measured_peaks().get("sm_max_mhz", 2070.0)) * 1e6
+    peak_lane = 152 * 128 * f_max
+    roof = {"bound": "sm_issue", "achieved": rate * l_flow / 1e9, "peak": peak_lane / 1e9, "unit": "Glane-op/s",
+            "frac": rate * l_flow / peak_lane,
+            "per_unit": f"L_flow(Z)=2(Z-1)+152+9Z+40(Z-1) lane-ops per kMC event at <Z>={zmean:.1f}",
+            "peak_source": "152 SMs x 128 lanes x sm_max_mhz of MEASURED_PEAKS.json (of measured clock)"}
     return {"workload": f"4 x {n} chains, N_K=100, beta=1, shear Wi {{0.1,1,10,100}}, kappa_xy=Wi/tau_d, "
                         f"tau_d={tau_d:.4g}, output every {dt_out:g} tau_K",
-            "windows": args.shear_windows, "events": ev_tot, "events_per_s": ev_tot / secs, "wall_s": secs,
-            "sigma_xy_per_window": series,
+            "windows": args.shear_windows, "events": ev_tot, "events_per_s": rate, "wall_s": secs,
+            "sigma_xy_per_window": series, "roofline": roof,
             "timing": "host wall clock around dsm_advance_batch (launch + window + stress readback)"}
 
 
