@@ -118,6 +118,8 @@ def load_library() -> C.CDLL:
     lib.dsm_advance_batch.restype = C.c_int
     lib.dsm_save_file.argtypes = [vp, C.c_char_p]
     lib.dsm_load_file.argtypes = [vp, C.c_char_p]
+    lib.dsm_checkpoint_save.argtypes = [vp, C.c_char_p]
+    lib.dsm_checkpoint_load.argtypes = [vp, C.c_char_p]
     lib.dsm_advance_series.argtypes = [vp, C.c_double, i32, vp, vp, C.POINTER(u64)]
     lib.dsm_advance_series.restype = C.c_int
     lib.dsm_advance_start.argtypes = [vp, C.c_double, i64]
@@ -461,6 +463,15 @@ class Ensemble:
 
     def load(self, path: str) -> None:
         self._check(self._lib.dsm_load_file(self._h, os.fsencode(path)))
+
+    def checkpoint(self, path: str) -> None:
+        """Full-state checkpoint for an exact resume (dsm_checkpoint_save)."""
+        self._check(self._lib.dsm_checkpoint_save(self._h, os.fsencode(path)))
+
+    def restore(self, path: str) -> None:
+        """Restore a full-state checkpoint written by an ensemble of the same shape and
+        random streams (dsm_checkpoint_load); the ensemble is unchanged on failure."""
+        self._check(self._lib.dsm_checkpoint_load(self._h, os.fsencode(path)))
 
 
 def advance_batch(ensembles, t_end, step_limit=None):

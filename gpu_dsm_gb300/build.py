@@ -26,7 +26,8 @@ CLI = PKG / "gpu_DSM"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-I", str(ROOT / "include")]
-SOURCES = ["dsm_kernels.cu", "dsm_host.cu", "dsm_compat.cu", "dsm_noalloc.cu", "dsm_serve.cu", "dsm_distr.cu", "dsm_gex.cpp"]
+SOURCES = ["dsm_kernels.cu", "dsm_host.cu", "dsm_compat.cu", "dsm_noalloc.cu", "dsm_serve.cu", "dsm_distr.cu", "dsm_gex.cpp",
+           "dsm_checkpoint.cu"]
 
 
 def nvcc() -> str:

@@ -566,6 +566,7 @@ extern "C" int dsm_set_schedule(dsm_sim* s, int32_t small_slot, int32_t large_gr
 // trial is wasted) and the one with the most events per kernel millisecond is
 // kept.
 extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* best_ms) {
+  const dsm::NvtxRange nvtx_range("dsm_autotune");
   if (!s || !s->ready || !(window > 0.0) || s->pending) return DSM_ERR_INVALID;
   struct Cand { int small, grid, lanes; };
   std::vector<Cand> cands;
@@ -671,6 +672,7 @@ static int reset_corr(dsm_sim* s) {
 }
 
 extern "C" int dsm_init_equilibrium(dsm_sim* s) {
+  const dsm::NvtxRange nvtx_range("dsm_init_equilibrium");
   if (!s || !s->ready) return DSM_ERR_INVALID;
   CK(cudaMemsetAsync(s->d_QN, 0, (size_t)s->P.n_chains * s->cap * sizeof(float4), s->st));
   CK(cudaMemsetAsync(s->d_tau, 0, (size_t)s->P.n_chains * s->cap * sizeof(float), s->st));
@@ -683,6 +685,7 @@ extern "C" int dsm_init_equilibrium(dsm_sim* s) {
 
 // ------------------------------------------------------------------ state transfer
 extern "C" int dsm_set_chains(dsm_sim* s, const dsm_chain_head* heads, const dsm_float4* QN, const float* tau) {
+  const dsm::NvtxRange nvtx_range("dsm_set_chains");
   if (!s || !s->ready || !heads || !QN || !tau) return DSM_ERR_INVALID;
   const size_t n = s->P.n_chains, cap = s->cap;
   std::vector<ChainState> cs(n);
@@ -732,6 +735,7 @@ extern "C" int dsm_set_chains(dsm_sim* s, const dsm_chain_head* heads, const dsm
 }
 
 extern "C" int dsm_get_chains(dsm_sim* s, dsm_chain_head* heads, dsm_float4* QN, float* tau) {
+  const dsm::NvtxRange nvtx_range("dsm_get_chains");
   if (!s || !s->ready) return DSM_ERR_INVALID;
   const size_t n = s->P.n_chains, cap = s->cap;
   // slots beyond Z are not maintained on the device: zero them there, so the
@@ -1026,6 +1030,7 @@ static std::vector<double> series_ends(const dsm_sim* s, double dt, int n) {
 
 extern "C" int dsm_advance_series(dsm_sim* s, double dt, int32_t n, const volatile int32_t* abort_flag,
                                   dsm_stress_plus* out, uint64_t* events) {
+  const dsm::NvtxRange nvtx_range("dsm_advance_series");
   if (!s || !s->ready || n < 1 || !(dt > 0.0) || s->pending) return DSM_ERR_INVALID;
   *s->h_abort = (abort_flag && *abort_flag) ? 1 : 0;
   const std::vector<double> e = series_ends(s, dt, n);
@@ -1038,6 +1043,7 @@ extern "C" int dsm_advance_series(dsm_sim* s, double dt, int32_t n, const volati
 
 // ------------------------------------------------------------------ asynchronous form
 extern "C" int dsm_advance_start(dsm_sim* s, double t_end, int64_t step_limit) {
+  const dsm::NvtxRange nvtx_range("dsm_advance_start");
   if (!s || !s->ready || s->pending) return DSM_ERR_INVALID;
   if (!(t_end >= 0.0) || t_end * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
   *s->h_abort = 0;
@@ -1048,6 +1054,7 @@ extern "C" int dsm_advance_start(dsm_sim* s, double t_end, int64_t step_limit) {
 }
 
 extern "C" int dsm_series_start(dsm_sim* s, const double* t_ends, int32_t n) {
+  const dsm::NvtxRange nvtx_range("dsm_series_start");
   if (!s || !s->ready || !t_ends || n < 1 || s->pending) return DSM_ERR_INVALID;
   *s->h_abort = 0;
   const int rc = series_start(s, t_ends, n);
@@ -1137,6 +1144,7 @@ int dsm::sim_finish_window(dsm_sim* s, uint64_t* events) {
 
 extern "C" int dsm_advance(dsm_sim* s, double t_end, int64_t step_limit, const volatile int32_t* abort_flag,
                            uint64_t* events) {
+  const dsm::NvtxRange nvtx_range("dsm_advance");
   if (!s || !s->ready) return DSM_ERR_INVALID;
   if (!(t_end >= 0.0) || t_end * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
   *s->h_abort = (abort_flag && *abort_flag) ? 1 : 0;
@@ -1170,6 +1178,7 @@ extern "C" int dsm_stress(dsm_sim* s, dsm_stress_plus* out, int32_t* count) {
 }
 
 extern "C" int dsm_gt_raw(dsm_sim* s, double* gsum, int64_t* count) {
+  const dsm::NvtxRange nvtx_range("dsm_gt_raw");
   if (!s || !s->ready) return DSM_ERR_INVALID;
   if (!s->corr) return fail(s, DSM_ERR_INVALID, "no correlator in this simulation (eq_type != 1 or flow)");
   const size_t m = (size_t)s->levels * s->cp;
@@ -1185,6 +1194,7 @@ extern "C" int dsm_gt_raw(dsm_sim* s, double* gsum, int64_t* count) {
 // G(t) (or MSD(t)) points in the order and count gpu_Gt_PCS writes them
 // (ensemble.cu:298-335, correlator.cu:242-257)
 extern "C" int dsm_gt(dsm_sim* s, float* t, float* G, int32_t* n) {
+  const dsm::NvtxRange nvtx_range("dsm_gt");
   if (!s || !n) return DSM_ERR_INVALID;
   const int L = s->levels, p = s->cp, m = s->cm, dmin = p / m;
   std::vector<double> gs((size_t)L * p);
@@ -1270,6 +1280,7 @@ extern "C" int dsm_last_window(const dsm_sim* s, float* kernel_ms, uint64_t* eve
 // shared-memory slot is sized for the largest z_max of the kind.
 extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end, const int64_t* step_limit,
                                  uint64_t* events) {
+  const dsm::NvtxRange nvtx_range("dsm_advance_batch");
   if (!sims || n < 1 || !t_end) return DSM_ERR_INVALID;
   dsm_sim* s = sims[0];
   if (!s || !s->ready) return DSM_ERR_INVALID;

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/dsm.h"
 #include "dsm_internal.h"
@@ -48,6 +49,15 @@ void keep_pool_memory(int device);
 
 // One persistent launch of a polydisperse ensemble's size-class plan: chains
 // order[first .. first+count) with slots of cfg.slot_cap strands
+// NVTX range over one phase of the host API (a no-op unless a tool such as
+// ncu --nvtx is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 struct SizeClass {
   LaunchCfg cfg{4, 0, 0, 32};
   long long first = 0, count = 0;

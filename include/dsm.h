@@ -248,6 +248,19 @@ int dsm_q_sorted(dsm_sim* sim, float* q, int64_t* n);
  * int N_cha, then per chain chain_head, Z float4 QN, Z float tau. */
 int dsm_save_file(dsm_sim* sim, const char* path);
 int dsm_load_file(dsm_sim* sim, const char* path);
+/* Full-state checkpoint for an exact resume (no counterpart in the reference,
+ * whose conformation file above restarts clocks, random streams and G(t)):
+ * per-chain time, Philox event counter, event hash, scale and stall code, the
+ * conformations, every correlator level, and the ensemble's time, behind a
+ * versioned header and a payload checksum.  dsm_checkpoint_load checks that
+ * the file was written by an ensemble of the same shape (chains, z_max, N_K,
+ * per-chain N_K, flow / correlator kind, levels, p, m) and the same random
+ * streams (seed, stream, chain offset), and verifies the checksum, before it
+ * changes anything; on any mismatch it returns DSM_ERR_INVALID with the reason
+ * in dsm_last_error and leaves the ensemble as it was.  Advancing a restored
+ * ensemble gives the same bits as advancing the one that wrote the file. */
+int dsm_checkpoint_save(dsm_sim* sim, const char* path);
+int dsm_checkpoint_load(dsm_sim* sim, const char* path);
 
 /* ---------------------------------------------------------------------
  * Allocation-free time step.  No counterpart in the reference: it exists for

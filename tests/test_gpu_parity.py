@@ -166,6 +166,64 @@ def test_chain_transfer_layout_and_validation(dsm_mod):
     assert np.array_equal(gpu_state(g)["Z"], ok["Z"])
 
 
+@pytest.mark.parametrize("kind", ["gt", "flow", "msd"])
+def test_checkpoint_exact_resume(dsm_mod, tmp_path, kind):
+    """A full-state checkpoint restored into a fresh ensemble continues with
+    the same bits as the ensemble that wrote it: chain state, event hash,
+    G(t) / MSD sums or stress."""
+    kw = dict(nk=60, n_chains=700, seed=19, sync_dt=1.0, t_end=1.0e4)
+    if kind == "gt":
+        kw.update(eq_type=1, corr_p=16, corr_m=2)
+    elif kind == "msd":
+        kw.update(eq_type=2, corr_p=16, corr_m=4)
+    else:
+        kw.update(kappa=(0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0))
+    a = dsm_mod.Ensemble(**kw)
+    a.init_equilibrium()
+    a.advance(30.0)
+    path = tmp_path / "state.ckpt"
+    a.checkpoint(str(path))
+    b = dsm_mod.Ensemble(**kw)
+    b.restore(str(path))
+    for t in (45.0, 70.0):
+        ea, eb = a.advance(t), b.advance(t)
+        assert ea == eb
+        if kind == "flow":
+            assert np.array_equal(a.stress()[0], b.stress()[0])
+    assert_bitexact(gpu_state(b), gpu_state(a), what=f"restored {kind}")
+    if kind != "flow":
+        ga, gb = a.gt_raw(), b.gt_raw()
+        assert np.array_equal(ga[0], gb[0]) and np.array_equal(ga[1], gb[1])
+
+
+def test_checkpoint_rejects_mismatch(dsm_mod, tmp_path):
+    """Restoring checks the ensemble's shape, random streams and the payload
+    checksum first; a rejected restore leaves the ensemble unchanged."""
+    kw = dict(nk=40, n_chains=300, seed=23, eq_type=1, sync_dt=1.0, t_end=1.0e4, corr_p=16, corr_m=2)
+    a = dsm_mod.Ensemble(**kw)
+    a.init_equilibrium()
+    a.advance(10.0)
+    path = tmp_path / "a.ckpt"
+    a.checkpoint(str(path))
+    before = gpu_state(a)
+    for other, why in ((dict(kw, n_chains=301), "number of chains"), (dict(kw, seed=24), "random streams"),
+                       (dict(kw, corr_m=4), "correlator"), (dict(kw, eq_type=0), "correlator")):
+        x = dsm_mod.Ensemble(**other)
+        x.init_equilibrium()
+        with pytest.raises(dsm_mod.api.DSMError, match=why):
+            x.restore(str(path))
+    raw = bytearray(path.read_bytes())
+    raw[len(raw) // 2] ^= 0x40
+    bad = tmp_path / "bad.ckpt"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(dsm_mod.api.DSMError, match="checksum"):
+        a.restore(str(bad))
+    (tmp_path / "short.ckpt").write_bytes(bytes(raw[: len(raw) // 3]))
+    with pytest.raises(dsm_mod.api.DSMError, match="truncated"):
+        a.restore(str(tmp_path / "short.ckpt"))
+    assert_bitexact(gpu_state(a), before, what="unchanged after rejected restores")
+
+
 @pytest.mark.parametrize("nk,n,kappa,z_max", [(25, 1024, (0.0,) * 9, 0), (200, 256, (0.0,) * 9, 0),
                                               (50, 256, (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 0),
                                               (30, 256, (0.0,) * 9, 14)])
