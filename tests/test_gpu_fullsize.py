@@ -9,7 +9,9 @@ compared with it bit for bit elsewhere):
   positive and decaying at short lags, bit-exact reproducibility, and the
   same chains whether run as one ensemble or as two shards (chain_offset);
 - 262144 polydisperse chains (log-normal N_K, mean 150, PDI 1.5, <= 2000)
-  in size classes after autotuning: conservation and no stalls."""
+  in size classes after autotuning: conservation and no stalls;
+- shear start-up, 4 x 32768 chains, N_K=100: conservation, no stalls, shear
+  stress ordered by the Weissenberg number."""
 import math
 
 import numpy as np
@@ -97,3 +99,24 @@ def test_polydisperse_size_classes_full_size(dsm_mod):
     assert np.all(ext["stall"] == 0)
     assert np.all(qn[:, :, 3].sum(axis=1) == nkc)
     assert np.all(heads["Z"] <= nkc)
+
+
+def test_shear_startup_full_size(dsm_mod):
+    """4 x 32768 chains, N_K=100, shear at Wi 1, 10, 100 advanced together
+    (dsm_advance_batch), 500 tau_K: Kuhn steps conserved, no stalls, and the
+    shear stress grows in magnitude with the Weissenberg number (stress
+    -sum 3 Q_x Q_y / N, ensemble_kernel.cu:504-538)."""
+    tau_d = dsm_mod.pcd(1.0, 100)["tau_d"]
+    wis = (1.0, 10.0, 100.0)
+    ens = [dsm_mod.Ensemble(nk=100, n_chains=32768, kappa=(0.0, wi / tau_d, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0),
+                            sync_dt=500.0, t_end=5.0e5, seed=4, stream=k) for k, wi in enumerate(wis)]
+    for e in ens:
+        e.init_equilibrium()
+    ev = dsm_mod.advance_batch(ens, 500.0)
+    assert np.all(np.asarray(ev) > 0)
+    sxy = [e.stress()[0][3] for e in ens]
+    assert sxy[2] < sxy[1] < 0.0 and abs(sxy[2]) > 5 * abs(sxy[1])
+    for e in ens:
+        heads, qn, _ = e.get_chains()
+        assert np.all(e.get_ext()["stall"] == 0)
+        assert np.all(qn[:, :, 3].sum(axis=1) == 100)
