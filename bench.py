@@ -307,6 +307,16 @@ def run_gpu(args):
         gbs = (bytes_chain + lvl_bytes) / (kms / args.steps / 1e3) / 1e9
         roof["hbm_secondary"] = {"achieved": gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                                  "frac": gbs / float(peaks["hbm_gbs"]), "note": "of measured"}
+    if tr.get("warp_instructions_per_event"):
+        # issue slots: the kernel is latency-bound, so the share of warp-scheduler
+        # issue slots it fills (events/s x warp-instructions per event from the
+        # ncu capture, against 4 schedulers x 152 SMs x clock) says how busy the SMs are
+        ipe = float(tr["warp_instructions_per_event"])
+        peak_issue = n_sm * 4 * f_max
+        roof["issue_secondary"] = {"achieved": value / world * ipe / 1e9, "peak": peak_issue / 1e9,
+                                   "unit": "Gwarp-inst/s", "frac": value / world * ipe / peak_issue,
+                                   "per_unit": f"{ipe:g} warp-instructions per kMC event (ncu)",
+                                   "note": "of measured clock"}
 
     if rank != 0:
         return 0
