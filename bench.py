@@ -473,7 +473,7 @@ def prior_events(r) -> float:
     return (0.2 * r["nk"] + 2.0) * r["n_chains"] * r["t_end"]
 
 
-def serve_once(reqs, arrivals, *, max_active, chunk_s, device, policy="fcfs", overlap=1.5, bypass=0.2):
+def serve_once(reqs, arrivals, *, max_active, chunk_s, device, policy="fcfs", overlap=1.0, bypass=0.2):
     import gpu_dsm_gb300 as dsm
 
     srv = dsm.Server(device=device, max_active=max_active, chunk_s=chunk_s, policy=policy, overlap=overlap,
@@ -532,7 +532,7 @@ def run_serve(args, device: int = 0) -> dict:
             continue
         f = spec.split(":")
         pol = f[0]
-        ov = float(f[1]) if len(f) > 1 else 1.5
+        ov = float(f[1]) if len(f) > 1 else 1.0
         bp = float(f[2]) if len(f) > 2 else 0.2
         others[spec], _ = serve_once(reqs, arrivals, max_active=0, chunk_s=args.serve_chunk, device=device,
                                      policy=pol, overlap=ov, bypass=bp)
@@ -544,7 +544,7 @@ def run_serve(args, device: int = 0) -> dict:
             "offered_load_vs_plain": 1.2, "chunk_s": args.serve_chunk, "served": served, "plain": plain,
             "other_policies": others,
             "policies": "served: first come first served with backfill (stream priority by age, running "
-                        "requests up to 1.5 GPUs of chain slots, requests under 0.2 chunk of the GPU start at "
+                        "requests up to 1 GPU of chain slots, requests under 0.2 chunk of the GPU start at "
                         "once); plain: one request at a time, one launch per request / flow output",
             "p99_speedup": plain["p99_s"] / served["p99_s"], "p50_speedup": plain["p50_s"] / served["p50_s"],
             "throughput_ratio": served["events_per_s"] / plain["events_per_s"],

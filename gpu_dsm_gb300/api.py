@@ -505,7 +505,7 @@ class Server:
     POLICIES = {"fcfs": 0, "equal_pace": 1, "fcfs_strict": 2}
 
     def __init__(self, *, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_s: float = 0.0,
-                 policy: str = "fcfs", overlap: float = 1.5, bypass: float = 0.2):
+                 policy: str = "fcfs", overlap: float = 1.0, bypass: float = 0.2):
         self._lib = load_library()
         h = C.c_void_p()
         rc = self._lib.dsm_serve_open(device, hbm_budget, max_active, chunk_s, C.byref(h))

@@ -99,7 +99,7 @@ struct dsm_server {
   double chunk_s = 0.05;     // target duration of one chunk; < 0: whole-request windows
   double rate_est = 1.0e9;   // aggregate kMC events/s while work is in flight
   int policy = 0;            // 0 first come first served with backfill, 1 equal pace per chain
-  double overlap = 1.5;      // running requests may fill up to this many GPUs' worth of chain slots
+  double overlap = 1.0;      // running requests may fill up to this many GPUs' worth of chain slots
   double bypass = 0.2;       // requests shorter than bypass * chunk_s of the whole GPU run at once
   int prio_least = 0, prio_greatest = 0;  // CUDA stream priority range
   int sm_slots = 4864;       // chains resident on the GPU at full occupancy (152 SMs x 32)

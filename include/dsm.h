@@ -342,8 +342,8 @@ int dsm_serve_set_policy(dsm_server* srv, int32_t policy);
  * slots only; above 1, younger requests also run at lower stream priority and
  * take the SMs the older ones leave free at the ends of their launches);
  * policy 0 also starts at once any request whose remaining work is below
- * bypass x chunk_s of the whole GPU.  Defaults 1.5 and 0.2 (on the 200-request
- * stream: p50 7x and p99 1.01x better than one-at-a-time serving). */
+ * bypass x chunk_s of the whole GPU.  Defaults 1 and 0.2 (on the 200-request
+ * stream: p50 about 20x and p99 1.1x better than one-at-a-time serving). */
 int dsm_serve_tune(dsm_server* srv, double overlap, double bypass);
 /* Queue a request; *id identifies it.  DSM_ERR_MEMORY if it can never fit. */
 int dsm_serve_submit(dsm_server* srv, const dsm_params* params, uint64_t* id);
