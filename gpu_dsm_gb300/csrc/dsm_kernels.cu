@@ -1,28 +1,36 @@
 // sm_103a kernels of the DSM kinetic Monte Carlo path.
 //
 // Design (one GB300, one process):
-//   * Each chain is simulated by ONE WARP that keeps the whole chain in shared
-//     memory (slot: {Qx,Qy,Qz,Q^2} float4, N int, tau rate float, quantised
-//     rate uint64 per strand) inside a persistent loop.  Warps pull chains from
-//     an atomic work counter, load them with coalesced float4 loads, run them to
-//     the end of the launch window and write them back: HBM is touched only at
-//     window boundaries and by the long-lag correlator levels.
+//   * Each chain is simulated by a TILE of W lanes (W = 16 by default, two
+//     independent chains per warp; W = 32 for one chain per warp) that keeps
+//     the whole chain in shared memory (slot: {Qx,Qy,Qz,Q^2} float4, N int,
+//     tau rate float, quantised rate uint64 per strand, correlator level 0)
+//     inside a persistent loop.  Tiles pull chains from an atomic work
+//     counter, load them with coalesced float4 loads, run them to the end of
+//     the launch window (or of a group of flow output windows) and write them
+//     back: HBM is touched only at window boundaries and by the long-lag
+//     correlator levels.
 //   * The event pick is exact integer arithmetic: every rate component is
 //     quantised to int64 fixed point (scale 2^S per chain).  The quantised pair
 //     totals and the five chain-end rates form one array of Z-1+5 elements in
 //     the reference's pick order; each lane sums a contiguous odd-width chunk
-//     (bank-conflict free), one warp inclusive scan + ballot finds the lane, the
-//     lane walks its chunk.  Integer sums do not depend on order, so a CPU
+//     (bank-conflict free), one tile inclusive scan + ballot finds the lane,
+//     the lane walks its chunk.  Integer sums do not depend on order, so a CPU
 //     restatement reproduces the pick bit for bit.
 //   * Equilibrium: only the <=3 pair rates touched by an event are recomputed
-//     (in parallel, one lane each), the chain-end rates only when a strand next
-//     to an end changes.  The reference recomputes every pair every step
-//     (ensemble_kernel.cu strent_kernel).  Flow: all strands are deformed and all
-//     rates recomputed every step, as in the reference.
-//   * Insert/remove of strands is a warp-cooperative memmove in shared memory
+//     (two lanes per pair), and the prefix sums are patched with their deltas;
+//     the chain-end rates only when a strand next to an end changes.  The
+//     reference recomputes every pair every step (ensemble_kernel.cu
+//     strent_kernel).  Flow: all strands are deformed and all rates recomputed
+//     every step, as in the reference.
+//   * Insert/remove of strands is a tile-cooperative memmove in shared memory
 //     (the reference defers it to the next step, ensemble_kernel.cu:64-102).
-//   * Randomness: Philox4x32-10; lane l computes the event words of step
-//     base+l, so one Philox evaluation serves 32 consecutive events.
+//   * Randomness: Philox4x32-10 keyed by (seed, event counter, purpose, global
+//     chain id, ensemble); lane l computes the words of event base+l, so one
+//     Philox evaluation serves W consecutive events.
+//   * The hot paths (strand insertion/removal, correlator sampling and level
+//     pushes) are inlined into the event loop: calls would save and restore
+//     the loop's live registers and spread its code (instruction-fetch stalls).
 //   * No tensor cores: nothing on this path is a dense contraction.
 #include <cstdint>
 #include <mutex>
