@@ -372,6 +372,12 @@ static int largest_slot(bool flow, int corr, LaunchCfg cfg, int bps_want, int hi
   return lo;
 }
 
+// Fewer warps per block while the block's slots exceed the per-block shared
+// memory (long chains: one warp per block holds one slot of z_max strands)
+static void fit_block(LaunchCfg& cfg, int optin) {
+  while (cfg.warps_per_block > 1 && step_block_smem(cfg) > (size_t)optin) cfg.warps_per_block /= 2;
+}
+
 // One launch over all chains with slots of the full capacity
 static int plan_single(dsm_sim* s) {
   s->classes.clear();
@@ -379,6 +385,7 @@ static int plan_single(dsm_sim* s) {
   s->cfg.slot_cap = s->cap;
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
+  fit_block(s->cfg, smem_optin);
   if (step_block_smem(s->cfg) > (size_t)smem_optin)
     return fail(s, DSM_ERR_INVALID, "chain capacity z_max=" + std::to_string(s->cap) + " does not fit one shared-memory slot");
   const int bps = step_max_blocks_per_sm(s->flow, s->ck, s->cfg);
@@ -1363,6 +1370,9 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     CK(cudaMemcpyAsync(dE, hE.data(), sizeof(EnsDev) * k, cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(dP, pre.data(), sizeof(long long) * (k + 1), cudaMemcpyHostToDevice, s->st));
     CK(cudaMemsetAsync(dW, 0, 16, s->st));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
+    fit_block(cfg, optin);
     const int bps = step_max_blocks_per_sm(g.flow, g.corr, cfg);
     if (bps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory"); break; }
     const int tiles = cfg.warps_per_block * 32 / cfg.lanes;

@@ -133,6 +133,23 @@ def test_set_get_roundtrip(dsm_mod, oracle_mod, tmp_path):
                     what="loaded")
 
 
+@pytest.mark.parametrize("kappa", [(0.0,) * 9, (0.0, 1.0e-4, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)])
+def test_long_chains_monodisperse(dsm_mod, oracle_mod, kappa):
+    """N_K = 1500: full-capacity slots of 1500 strands do not fit four chains
+    per block, so the launch runs fewer warps per block; the chains still give
+    the oracle's trajectories exactly, alone and through dsm_advance_batch."""
+    g, o = pair(dsm_mod, oracle_mod, nk=1500, n=96, seed=13, kappa=kappa)
+    h = dsm_mod.Ensemble(nk=1500, n_chains=96, seed=13, kappa=kappa)
+    for x in (g, h, o):
+        x.init_equilibrium()
+    ev = g.advance(2.0)
+    assert ev == o.run(2.0)
+    assert dsm_mod.advance_batch([h], 2.0)[0] == ev
+    st = o.get_state()
+    assert_bitexact(gpu_state(g), st, what="N_K=1500")
+    assert_bitexact(gpu_state(h), st, what="N_K=1500 batched")
+
+
 def test_chain_transfer_layout_and_validation(dsm_mod):
     """dsm_get_chains returns the reference layout (slots beyond Z zero, the
     entanglement slot of the last strand zero), also into caller buffers;
