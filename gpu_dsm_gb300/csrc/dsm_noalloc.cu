@@ -168,6 +168,9 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   int sms = 0, optin = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // long chains: fewer warps (chain slots) per block until the block fits
+  while (cfg.warps_per_block > 1 && dsm::step_slot_bytes(cap, 0) * cfg.warps_per_block > (size_t)optin)
+    cfg.warps_per_block /= 2;
   if (dsm::step_slot_bytes(cap, 0) * cfg.warps_per_block > (size_t)optin)
     return fail(DSM_ERR_INVALID, "z_max does not fit one shared-memory slot");
   const int bps = dsm::step_max_blocks_per_sm(flow, false, cfg);

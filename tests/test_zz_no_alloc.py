@@ -40,12 +40,12 @@ def test_noalloc_rejects_oversize(dsm_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kappa", [(0.0,) * 9, (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)])
-def test_noalloc_matches_dsm_advance(dsm_mod, kappa):
+@pytest.mark.parametrize("kappa,nk,n", [((0.0,) * 9, 50, 512), ((0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 50, 512),
+                                        ((0.0,) * 9, 2000, 64)])
+def test_noalloc_matches_dsm_advance(dsm_mod, kappa, nk, n):
     import torch
 
     lib = _bind(dsm_mod)
-    n, nk = 512, 50
     ens = dsm_mod.Ensemble(nk=nk, n_chains=n, seed=3, kappa=kappa)
     ens.init_equilibrium()
     heads, qn, tau = ens.get_chains()
