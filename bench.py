@@ -214,6 +214,8 @@ def run_gpu(args):
         events += ens.advance(t)
         kms += ens.last_window()["kernel_ms"]
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     wall = time.perf_counter() - t0
     clocks = clk.stop()
     lw = ens.last_window()
@@ -319,6 +321,8 @@ def run_gpu(args):
                                    "note": "of measured clock"}
 
     if rank != 0:
+        ens.close()
+        torch.distributed.destroy_process_group()
         return 0
     serve = shear = poly = None
     if world == 1:
