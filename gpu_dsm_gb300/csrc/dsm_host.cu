@@ -1293,6 +1293,7 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
   if (!s || !s->ready) return DSM_ERR_INVALID;
   for (int i = 0; i < n; ++i) {
     if (!sims[i] || !sims[i]->ready) return DSM_ERR_INVALID;
+    if (sims[i]->pending) return fail(s, DSM_ERR_INVALID, "an ensemble of the batch has asynchronous work pending");
     if (sims[i]->P.device != s->P.device) return fail(s, DSM_ERR_INVALID, "batch spans devices");
     if (!(t_end[i] >= 0.0) || t_end[i] * TICKS >= 9.0e18) return fail(s, DSM_ERR_INVALID, "t_end out of range");
     for (int k = 0; k < i; ++k)
