@@ -240,9 +240,10 @@ def run_gpu(args):
         kms_max, events_all = kms, events
     value = events_all / (kms_max / 1e3)
 
-    # ---- e2e through the C ABI with host buffers (pinned), every step
+    # ---- e2e through the C ABI with host buffers (pinned), every step, on
+    # every rank (each its own shard); whole-job events over the slowest rank
     e2e = None
-    if rank == 0 and args.e2e_steps > 0:
+    if args.e2e_steps > 0:
         cap = ens.z_max
         h_heads = torch.empty(N_CHAINS * 16, dtype=torch.uint8, pin_memory=True)
         h_qn = torch.empty(N_CHAINS * cap * 4, dtype=torch.float32, pin_memory=True)
@@ -255,7 +256,8 @@ def run_gpu(args):
         qv[:] = qn
         tv[:] = tau
         ens2 = dsm.Ensemble(beta=BETA, nk=NK, n_chains=N_CHAINS, eq_type=1, sync_dt=SAMPLE_DT,
-                            t_end=T_END_RUN, seed=2, device=local, corr_p=CORR_P, corr_m=CORR_M)
+                            t_end=T_END_RUN, seed=2, device=local, corr_p=CORR_P, corr_m=CORR_M,
+                            chain_offset=rank * N_CHAINS)
         # results come back into pinned buffers of their own
         o_heads = torch.empty(N_CHAINS * 16, dtype=torch.uint8, pin_memory=True)
         o_qn = torch.empty(N_CHAINS * cap * 4, dtype=torch.float32, pin_memory=True)
@@ -266,6 +268,8 @@ def run_gpu(args):
         npts = 0
         for i in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
             s0 = time.perf_counter()
             ens2.set_chains(hv, qv, tv)
             ev = ens2.advance(args.window)
@@ -277,8 +281,15 @@ def run_gpu(args):
             if i > 0:  # first e2e step is a warm-up
                 ev_e += ev
                 t_e += s1 - s0
-        h2d = N_CHAINS * 16 + N_CHAINS * cap * 20
-        d2h = N_CHAINS * 16 + N_CHAINS * cap * 20 + npts * 8
+        h2d = (N_CHAINS * 16 + N_CHAINS * cap * 20) * world
+        d2h = (N_CHAINS * 16 + N_CHAINS * cap * 20 + npts * 8) * world
+        if world > 1:
+            import torch.distributed as dist
+            et = torch.tensor([float(ev_e)], dtype=torch.float64, device="cuda")
+            tt_e = torch.tensor([t_e], dtype=torch.float64, device="cuda")
+            dist.all_reduce(et, op=dist.ReduceOp.SUM)
+            dist.all_reduce(tt_e, op=dist.ReduceOp.MAX)
+            ev_e, t_e = int(et.item()), float(tt_e.item())
         e2e = {"value": ev_e / t_e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "steps": args.e2e_steps, "host_buffers": "pinned (torch pin_memory)",
                "calls": "dsm_set_chains + dsm_advance + dsm_get_chains + dsm_gt"}
