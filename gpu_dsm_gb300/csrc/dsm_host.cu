@@ -425,7 +425,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   const double msd = margin_sd > 0.f ? (double)margin_sd : 5.0;
   std::vector<int> big, mid, small;
   int nk_big = 0;
-  double w_big = 0.0, w_mid = 0.0, w_all = 0.0;
+  double w_big = 0.0, w_all = 0.0;
   for (int i = 0; i < n; ++i) {
     const int nk = s->nk_chain[i];
     const double m = 1.0 + (nk - 1) * pe, sd = std::sqrt(std::max(0.0, (nk - 1) * pe * (1.0 - pe)));
@@ -434,7 +434,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     const double w = (double)nk * (m + 40.0);
     w_all += w;
     if (zb <= small_cap) small.push_back(i);
-    else if (zb <= mid_cap) { mid.push_back(i); w_mid += w; }
+    else if (zb <= mid_cap) mid.push_back(i);
     else { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
   }
   auto by_nk = [&](int a, int b) { return s->nk_chain[a] != s->nk_chain[b] ? s->nk_chain[a] > s->nk_chain[b] : a < b; };
@@ -471,14 +471,16 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     B.grid = g;
   }
   if (!mid.empty()) {
-    // persistent blocks of 4 chains, as many as its share of the work
+    // persistent blocks of 4 chains, a full grid: the middle class competes
+    // with the small one for block slots, and a work-share grid left it
+    // finishing alone at the end of every window (measured 9.6e8 vs 1.2e9
+    // events/s on the 262144-chain log-normal melt)
     M.cfg = LaunchCfg{4, mid_cap, s->cfg.pmax, 32};
     M.bps = step_max_blocks_per_sm(s->flow, s->ck, M.cfg);
     if (M.bps < 1) return fail(s, DSM_ERR_INVALID, "middle slot does not fit shared memory");
     M.first = B.count;
     M.count = (long long)mid.size();
-    const long long g = (long long)std::ceil(w_mid / std::max(w_all, 1.0) * tiles_per_sm_full * s->sm_count / 4.0);
-    M.grid = (int)std::max<long long>(1, std::min<long long>({g, (M.count + 3) / 4, (long long)M.bps * s->sm_count}));
+    M.grid = (int)std::max<long long>(1, std::min<long long>((M.count + 3) / 4, (long long)M.bps * s->sm_count));
   }
   Sm.cfg = LaunchCfg{4, small_cap, s->cfg.pmax, sc.lanes};
   Sm.bps = step_max_blocks_per_sm(s->flow, s->ck, Sm.cfg);
