@@ -452,7 +452,7 @@ class Ensemble:
     def schedule(self) -> list:
         """[{slot, warps_per_block, lanes, grid, chains}, ...]; empty for one launch over all chains."""
         n = C.c_int32()
-        info = np.zeros(20, np.int32)  # DSM_SCHEDULE_INFO
+        info = np.zeros(25, np.int32)  # DSM_SCHEDULE_INFO
         self._check(self._lib.dsm_get_schedule(self._h, C.byref(n), _ptr(info)))
         keys = ("slot", "warps_per_block", "lanes", "grid", "chains")
         m = n.value + 1 if n.value else 0

@@ -423,9 +423,14 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   // (mean + margin_sd sd of 1 + Binomial(N_K - 1, 1/(1+beta)), plus 2) go there
   const double pe = 1.0 / (1.0 + (double)P.beta);
   const double msd = margin_sd > 0.f ? (double)margin_sd : 5.0;
-  std::vector<int> big, mid, small;
-  int nk_big = 0;
+  std::vector<int> huge, big, mid, small;
+  int nk_big = 0, nk_huge = 0;
   double w_big = 0.0, w_all = 0.0;
+  // chains beyond the middle (or small) slot: a large class with slots sized
+  // for twice that bound, and the few longer ones in a huge class with slots
+  // of the longest chain -- one slot size for all of them would spend most of
+  // its shared memory on strands the typical large chain never has
+  const int large_cap = std::min(s->cap, 2 * std::max(small_cap, mid_cap));
   for (int i = 0; i < n; ++i) {
     const int nk = s->nk_chain[i];
     const double m = 1.0 + (nk - 1) * pe, sd = std::sqrt(std::max(0.0, (nk - 1) * pe * (1.0 - pe)));
@@ -435,13 +440,16 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     w_all += w;
     if (zb <= small_cap) small.push_back(i);
     else if (zb <= mid_cap) mid.push_back(i);
-    else { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
+    else if (zb <= large_cap) { big.push_back(i); nk_big = std::max(nk_big, nk); w_big += w; }
+    else { huge.push_back(i); nk_huge = std::max(nk_huge, nk); }
   }
   auto by_nk = [&](int a, int b) { return s->nk_chain[a] != s->nk_chain[b] ? s->nk_chain[a] > s->nk_chain[b] : a < b; };
+  std::sort(huge.begin(), huge.end(), by_nk);
   std::sort(big.begin(), big.end(), by_nk);
   std::sort(mid.begin(), mid.end(), by_nk);
   std::sort(small.begin(), small.end(), by_nk);
-  std::vector<int> order(big);
+  std::vector<int> order(huge);
+  order.insert(order.end(), big.begin(), big.end());
   order.insert(order.end(), mid.begin(), mid.end());
   order.insert(order.end(), small.begin(), small.end());
   if (!s->d_order) {
@@ -450,20 +458,32 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     CK(cudaMallocAsync((void**)&s->d_works, 8 * sizeof(unsigned int), s->st));
     CK(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, s->prio));
     CK(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, s->prio));
+    CK(cudaStreamCreateWithPriority(&s->side3, cudaStreamNonBlocking, s->prio));
     CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&s->ev_join2, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&s->ev_join3, cudaEventDisableTiming));
   }
   CK(cudaMemcpyAsync(s->d_order, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s->st));
   const int tiles_per_sm_full = 16;
-  SizeClass B, M, Sm;
+  SizeClass H, B, M, Sm;
+  H.stream = 3;
   B.stream = 1;
   M.stream = 2;
+  if (!huge.empty()) {
+    // few chains: one warp each, all at once
+    H.cfg = LaunchCfg{1, std::min(s->cap, nk_huge), s->cfg.pmax, 32};
+    H.bps = step_max_blocks_per_sm(s->flow, s->ck, H.cfg);
+    if (H.bps < 1) return fail(s, DSM_ERR_INVALID, "largest chains do not fit one shared-memory slot");
+    H.first = 0;
+    H.count = (long long)huge.size();
+    H.grid = (int)std::min<long long>(H.count, (long long)H.bps * s->sm_count);
+  }
   if (!big.empty()) {
-    B.cfg = LaunchCfg{1, std::min(s->cap, nk_big), s->cfg.pmax, 32};
+    B.cfg = LaunchCfg{1, std::min(s->cap, std::min(nk_big, large_cap)), s->cfg.pmax, 32};
     B.bps = step_max_blocks_per_sm(s->flow, s->ck, B.cfg);
-    if (B.bps < 1) return fail(s, DSM_ERR_INVALID, "largest chains do not fit one shared-memory slot");
-    B.first = 0;
+    if (B.bps < 1) return fail(s, DSM_ERR_INVALID, "large chains do not fit one shared-memory slot");
+    B.first = H.count;
     B.count = (long long)big.size();
     int g = big_grid > 0 ? big_grid
                          : (int)std::ceil(w_big / std::max(w_all, 1.0) * tiles_per_sm_full * s->sm_count);
@@ -478,14 +498,14 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
     M.cfg = LaunchCfg{4, mid_cap, s->cfg.pmax, 32};
     M.bps = step_max_blocks_per_sm(s->flow, s->ck, M.cfg);
     if (M.bps < 1) return fail(s, DSM_ERR_INVALID, "middle slot does not fit shared memory");
-    M.first = B.count;
+    M.first = H.count + B.count;
     M.count = (long long)mid.size();
     M.grid = (int)std::max<long long>(1, std::min<long long>((M.count + 3) / 4, (long long)M.bps * s->sm_count));
   }
   Sm.cfg = LaunchCfg{4, small_cap, s->cfg.pmax, sc.lanes};
   Sm.bps = step_max_blocks_per_sm(s->flow, s->ck, Sm.cfg);
   if (Sm.bps < 1) return fail(s, DSM_ERR_INVALID, "small slot does not fit shared memory");
-  Sm.first = B.count + M.count;
+  Sm.first = H.count + B.count + M.count;
   Sm.count = (long long)small.size();
   {
     const int tiles = 4 * 32 / Sm.cfg.lanes;
@@ -497,6 +517,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   s->cleanup.bps = step_max_blocks_per_sm(s->flow, s->ck, s->cleanup.cfg);
   if (s->cleanup.bps < 1) return fail(s, DSM_ERR_INVALID, "chain capacity does not fit one shared-memory slot");
   s->cleanup.grid = s->cleanup.bps * s->sm_count;
+  if (H.count > 0) s->classes.push_back(H);
   if (B.count > 0) s->classes.push_back(B);
   if (M.count > 0) s->classes.push_back(M);
   s->classes.push_back(Sm);
@@ -511,6 +532,7 @@ extern "C" void dsm_destroy(dsm_sim* s) {
   if (s->st) series_free(s);
   if (s->side) cudaStreamSynchronize(s->side);
   if (s->side2) cudaStreamSynchronize(s->side2);
+  if (s->side3) cudaStreamSynchronize(s->side3);
   void* ptrs[] = {s->d_tables, s->d_QN, s->d_tau, s->d_cs, s->d_stress, s->d_cshift, s->d_cacc, s->d_cavg,
                   s->d_ccnt, s->d_gsum, s->d_gcnt, s->d_pcd_by_nk, s->d_nk_chain, s->d_ens, s->d_prefix,
                   s->d_work, s->d_status, s->d_counters, s->d_red, s->d_order, s->d_defer, s->d_works, s->d_gex};
@@ -519,8 +541,10 @@ extern "C" void dsm_destroy(dsm_sim* s) {
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
   if (s->ev_join) cudaEventDestroy(s->ev_join);
   if (s->ev_join2) cudaEventDestroy(s->ev_join2);
+  if (s->ev_join3) cudaEventDestroy(s->ev_join3);
   if (s->side) cudaStreamDestroy(s->side);
   if (s->side2) cudaStreamDestroy(s->side2);
+  if (s->side3) cudaStreamDestroy(s->side3);
   dsm::host_words_give(s->hw);
   if (s->ev_done) cudaEventDestroy(s->ev_done);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -599,7 +623,9 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
       }
       const int rc = plan_classes(s, sm, 0, lanes, 0.f);
       if (rc != DSM_OK) return rc;
-      const int g0 = s->classes.size() > 1 && s->classes[0].stream == 1 ? s->classes[0].grid : 0;
+      int g0 = 0;  // grid of the large class, whose size the candidates vary
+      for (const SizeClass& k : s->classes)
+        if (k.stream == 1) g0 = k.grid;
       if (g0 == 0) { cands.push_back({sm, 0, lanes}); continue; }
       for (int g : {std::max(1, g0 / 2), g0, 2 * g0}) cands.push_back({sm, g, lanes});
     }
@@ -830,20 +856,23 @@ static int enqueue_step(dsm_sim* s) {
   CK(cudaEventRecord(s->ev_fork, s->st));
   CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
   CK(cudaStreamWaitEvent(s->side2, s->ev_fork, 0));
+  CK(cudaStreamWaitEvent(s->side3, s->ev_fork, 0));
   for (const SizeClass& k : s->classes) {
     StepList l;
     l.order = s->d_order + k.first;
     l.defer = s->d_defer;
     l.n_defer = s->d_works + 3;
-    cudaStream_t st = k.stream == 1 ? s->side : k.stream == 2 ? s->side2 : s->st;
-    unsigned int* work = s->d_works + (k.stream == 1 ? 1 : k.stream == 2 ? 4 : 0);
+    cudaStream_t st = k.stream == 1 ? s->side : k.stream == 2 ? s->side2 : k.stream == 3 ? s->side3 : s->st;
+    unsigned int* work = s->d_works + (k.stream == 1 ? 1 : k.stream == 2 ? 4 : k.stream == 3 ? 5 : 0);
     CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, work, s->flow, s->ck, k.cfg, s->d_abort, s->d_status,
                    k.grid, st, l));
   }
   CK(cudaEventRecord(s->ev_join, s->side));
   CK(cudaEventRecord(s->ev_join2, s->side2));
+  CK(cudaEventRecord(s->ev_join3, s->side3));
   CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
   CK(cudaStreamWaitEvent(s->st, s->ev_join2, 0));
+  CK(cudaStreamWaitEvent(s->st, s->ev_join3, 0));
   StepList l;
   l.order = s->d_defer;
   l.dyn_total = s->d_works + 3;
@@ -1099,14 +1128,17 @@ extern "C" int dsm_set_priority(dsm_sim* s, int32_t priority) {
   CK(cudaStreamSynchronize(s->st));
   if (s->side) CK(cudaStreamSynchronize(s->side));
   if (s->side2) CK(cudaStreamSynchronize(s->side2));
-  cudaStream_t st = nullptr, side = nullptr, side2 = nullptr;
+  if (s->side3) CK(cudaStreamSynchronize(s->side3));
+  cudaStream_t st = nullptr, side = nullptr, side2 = nullptr, side3 = nullptr;
   CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, pr));
   if (s->side) CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, pr));
   if (s->side2) CK(cudaStreamCreateWithPriority(&side2, cudaStreamNonBlocking, pr));
+  if (s->side3) CK(cudaStreamCreateWithPriority(&side3, cudaStreamNonBlocking, pr));
   cudaStreamDestroy(s->st);
   s->st = st;
   if (s->side) { cudaStreamDestroy(s->side); s->side = side; }
   if (s->side2) { cudaStreamDestroy(s->side2); s->side2 = side2; }
+  if (s->side3) { cudaStreamDestroy(s->side3); s->side3 = side3; }
   s->prio = pr;
   return DSM_OK;
 }

@@ -62,7 +62,7 @@ struct SizeClass {
   LaunchCfg cfg{4, 0, 0, 32};
   long long first = 0, count = 0;
   int grid = 0, bps = 0;
-  int stream = 0;  // 0 the handle's stream, 1 side, 2 side2
+  int stream = 0;  // 0 the handle's stream, 1 side, 2 side2, 3 side3
 };
 }  // namespace dsm
 
@@ -113,17 +113,17 @@ struct dsm_sim {
   int* d_abort = nullptr;
   dsm::HostWords* hw = nullptr;
   // size classes (polydisperse ensembles whose largest chains do not fit a
-  // full-occupancy slot): large slots (one warp per block), middle slots (one
-  // warp per chain, when the small class runs two chains per warp) and small
-  // slots, run concurrently on three streams; chains that outgrow a slot
-  // finish in the cleanup launch
+  // full-occupancy slot): huge and large slots (one warp per block), middle
+  // slots (one warp per chain, when the small class runs two chains per warp)
+  // and small slots, run concurrently on four streams; chains that outgrow a
+  // slot finish in the cleanup launch
   std::vector<dsm::SizeClass> classes;
   dsm::SizeClass cleanup;
   int* d_order = nullptr;
   int* d_defer = nullptr;
-  unsigned int* d_works = nullptr;  // [0] small, [1] large, [2] cleanup, [3] deferred count, [4] middle
-  cudaStream_t side = nullptr, side2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
+  unsigned int* d_works = nullptr;  // [0] small, [1] large, [2] cleanup, [3] deferred count, [4] middle, [5] huge
+  cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_join3 = nullptr;
   int prio = 0;  // CUDA stream priority of st and side
   int sched_version = 0;  // bumped whenever the launch schedule changes
   cudaEvent_t ev_done = nullptr;  // end of the last enqueued window / series, readback included

@@ -205,9 +205,9 @@ int dsm_pcd(double beta, int32_t nk, double* out);
 int dsm_set_schedule(dsm_sim* sim, int32_t small_slot, int32_t large_grid, int32_t lanes, float z_margin_sd);
 /* Current schedule: n_classes (0 = one launch over all chains), then per
  * class {slot strands, warps per block, lanes, grid, chains} in info[5*i..]
- * (info holds DSM_SCHEDULE_INFO = 20 ints: up to three classes -- large,
+ * (info holds DSM_SCHEDULE_INFO = 25 ints: up to four classes -- huge, large,
  * middle, small -- and the overflow launch, which has no fixed chain count). */
-#define DSM_SCHEDULE_INFO 20
+#define DSM_SCHEDULE_INFO 25
 int dsm_get_schedule(const dsm_sim* sim, int32_t* n_classes, int32_t* info);
 
 /* Autotuner (online): runs one real window of `window` tau_K with each

@@ -293,13 +293,13 @@ def test_size_classes_bitexact(dsm_mod, oracle_mod, small_slot, margin, kappa, l
     if small_slot:
         g.set_schedule(small_slot=small_slot, z_margin_sd=margin, lanes=lanes)
     sch = g.schedule()
-    if lanes == 16:
-        assert len(sch) == 4 and [k["warps_per_block"] for k in sch] == [1, 4, 4, 1]
-        assert [k["lanes"] for k in sch[:3]] == [32, 32, 16] and min(k["chains"] for k in sch[:3]) > 0
-        assert sum(k["chains"] for k in sch[:3]) == 400
-    else:
-        assert len(sch) == 3 and sch[0]["warps_per_block"] == 1 and sch[1]["warps_per_block"] == 4
-        assert sch[0]["chains"] + sch[1]["chains"] == 400
+    classes, overflow = sch[:-1], sch[-1]
+    assert overflow["warps_per_block"] == 1 and overflow["chains"] == 0
+    assert sum(k["chains"] for k in classes) == 400 and min(k["chains"] for k in classes) > 0
+    assert classes[-1]["warps_per_block"] == 4 and classes[-1]["lanes"] == (16 if lanes == 16 else 32)
+    assert classes[0]["warps_per_block"] == 1  # the longest chains: one warp per block
+    if lanes == 16:  # a middle class of one chain per warp
+        assert any(k["warps_per_block"] == 4 and k["lanes"] == 32 for k in classes)
     g.init_equilibrium()
     o.init_equilibrium()
     deferred = 0
