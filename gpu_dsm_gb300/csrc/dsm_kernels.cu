@@ -319,30 +319,45 @@ __device__ __forceinline__ Slot make_slot(unsigned char* base, int slot_cap, int
   return s;
 }
 
-// warp-cooperative moves inside the slot
-template <class T, int W>
-__device__ __forceinline__ void move_up(T* a, int lo, int hi, const Tile<W>& t) {  // [lo,hi) -> [lo+1,hi+1)
+// Whole-strand moves: Q and N over [lo, hi), the pair arrays T, R and P over
+// [lo_p, hi - 1), one place up or down.  All arrays of a lane's strand are
+// loaded before the tile synchronises and stored after it; a round's stores
+// never touch what the next round loads, and a store into a slot that the
+// previous round loaded comes after this round's synchronisation, so one
+// synchronisation per round and one at the end suffice.
+template <int W>
+__device__ __forceinline__ void move_strands_up(Slot& sl, int lo, int hi, const Tile<W>& t) {  // -> +1
   for (int top = hi - 1; top >= lo; top -= W) {
     const int s = top - t.lane;
-    T v;
-    const bool act = s >= lo;
-    if (act) v = a[s];
+    const bool act = s >= lo, pr = act && s < hi - 1;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    int n = 0;
+    float ta = 0.f;
+    unsigned long long r = 0, p = 0;
+    if (act) { q = sl.Q[s]; n = sl.N[s]; }
+    if (pr) { ta = sl.T[s]; r = sl.R[s]; p = sl.P[s]; }
     t.sync();
-    if (act) a[s + 1] = v;
-    t.sync();
+    if (act) { sl.Q[s + 1] = q; sl.N[s + 1] = n; }
+    if (pr) { sl.T[s + 1] = ta; sl.R[s + 1] = r; sl.P[s + 1] = p; }
   }
+  t.sync();
 }
-template <class T, int W>
-__device__ __forceinline__ void move_down(T* a, int lo, int hi, const Tile<W>& t) {  // [lo,hi) -> [lo-1,hi-1)
-  for (int bot = lo; bot < hi; bot += W) {
+template <int W>
+__device__ __forceinline__ void move_strands_down(Slot& sl, int lo, int lo_p, int hi, const Tile<W>& t) {  // -> -1
+  for (int bot = min(lo, lo_p); bot < hi; bot += W) {
     const int s = bot + t.lane;
-    T v;
-    const bool act = s < hi;
-    if (act) v = a[s];
+    const bool act = s >= lo && s < hi, pr = s >= lo_p && s < hi - 1;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    int n = 0;
+    float ta = 0.f;
+    unsigned long long r = 0, p = 0;
+    if (act) { q = sl.Q[s]; n = sl.N[s]; }
+    if (pr) { ta = sl.T[s]; r = sl.R[s]; p = sl.P[s]; }
     t.sync();
-    if (act) a[s - 1] = v;
-    t.sync();
+    if (act) { sl.Q[s - 1] = q; sl.N[s - 1] = n; }
+    if (pr) { sl.T[s - 1] = ta; sl.R[s - 1] = r; sl.P[s - 1] = p; }
   }
+  t.sync();
 }
 
 // float components {CD destruction, shift +1, shift -1, CD creation} of pair p
@@ -731,8 +746,7 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
     const int N1 = sl.N[j];
     const float4 q1 = sl.Q[j];
     t.sync();
-    move_up(sl.Q, j, Z, t); move_up(sl.N, j, Z, t);
-    move_up(sl.T, j, Z - 1, t); move_up(sl.R, j, Z - 1, t); move_up(sl.P, j, Z - 1, t);
+    move_strands_up(sl, j, Z, t);
     if (lane == 0) {
       const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
       const float ra = __fdiv_rn((float)newn, (float)N1);
@@ -750,8 +764,7 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
     const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
     const int nd = (evn == SDC_HEAD) ? 1 : newn;
     t.sync();
-    move_up(sl.Q, 0, Z, t); move_up(sl.N, 0, Z, t);
-    move_up(sl.T, 0, Z - 1, t); move_up(sl.R, 0, Z - 1, t); move_up(sl.P, 0, Z - 1, t);
+    move_strands_up(sl, 0, Z, t);
     if (lane == 0) {
       const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
       const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
@@ -794,8 +807,7 @@ __device__ DSM_APPLY_ATTR void apply_destroy(Slot& sl, int evn, int j, int Z, co
     const float4 a = sl.Q[j], b = sl.Q[j + 1];
     const bool endp = (j == Z - 2) || (j == 0);
     t.sync();
-    move_down(sl.Q, j + 2, Z, t); move_down(sl.N, j + 2, Z, t);
-    move_down(sl.T, j + 1, Z - 1, t); move_down(sl.R, j + 1, Z - 1, t); move_down(sl.P, j + 1, Z - 1, t);
+    move_strands_down(sl, j + 2, j + 1, Z, t);
     if (lane == 0) {
       const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
       const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
@@ -811,8 +823,7 @@ __device__ DSM_APPLY_ATTR void apply_destroy(Slot& sl, int evn, int j, int Z, co
     const int n = sl.N[1] + 1;
     const float4 b = sl.Q[1];
     t.sync();
-    move_down(sl.Q, 1, Z, t); move_down(sl.N, 1, Z, t);
-    move_down(sl.T, 1, Z - 1, t); move_down(sl.R, 1, Z - 1, t); move_down(sl.P, 1, Z - 1, t);
+    move_strands_down(sl, 1, 1, Z, t);
     if (lane == 0) {
       sl.N[0] = n; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (msd) {  // eq_ensemble_kernel.cu:645-653
@@ -1036,7 +1047,17 @@ __global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict
       if (lane == L) {
         r = pr - excl;
         jj = j0;
-        while (r >= sl.R[jj]) { r -= sl.R[jj]; ++jj; }
+        // three loads in flight per round; jj stays below ne = Z + 4, so
+        // jj + 2 <= slot_cap + 5 is inside the R array (slot_cap + NEND + 1)
+        for (;;) {
+          const unsigned long long a = sl.R[jj], b = sl.R[jj + 1], d = sl.R[jj + 2];
+          if (r < a) break;
+          r -= a; ++jj;
+          if (r < b) break;
+          r -= b; ++jj;
+          if (r < d) break;
+          r -= d; ++jj;
+        }
       }
       jj = t.shfl(jj, L);
       r = t.shfl(r, L);
