@@ -46,9 +46,16 @@ namespace dsm {
 
 #define FULL_MASK 0xffffffffu
 #define NEND 5
-// minimum resident blocks of 4 warps per SM the step kernel is compiled for
+// minimum resident blocks of 4 warps per SM the step kernel is compiled for:
+// DSM_MINB (register budget 128) for every kind, and DSM_MINB_HI (budget 80)
+// for the kinds without a correlator, whose code needs fewer registers and
+// gains from more resident warps when the slots leave the shared memory for
+// them (shear at N_K = 100: 6 blocks per SM instead of 4)
 #ifndef DSM_MINB
 #define DSM_MINB 4
+#endif
+#ifndef DSM_MINB_HI
+#define DSM_MINB_HI 6
 #endif
 // strand insertion / removal handlers: inlined (0) or out of line (1)
 #ifndef DSM_APPLY_NOINLINE
@@ -843,8 +850,8 @@ __device__ DSM_APPLY_ATTR void apply_destroy(Slot& sl, int evn, int j, int Z, co
 // ------------------------------------------------------------------ step kernel
 // CK: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD (compile
 // time, so that the stress kernel carries no MSD code)
-template <bool FLOW, int CK, int W>
-__global__ void __launch_bounds__(128, DSM_MINB) k_step(const EnsDev* __restrict__ ens, int n_ens,
+template <bool FLOW, int CK, int W, int MB>
+__global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens, int n_ens,
                                                  const long long* __restrict__ prefix, long long total,
                                                  unsigned int* work, int slot_cap, int pmax,
                                                  const volatile int* abort_flag, int* status, StepList lst) {
@@ -1435,16 +1442,19 @@ __global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win,
 }
 
 // ------------------------------------------------------------------ launchers
-template <bool FLOW, int CK, int W>
-static void* step_fn() { return (void*)k_step<FLOW, CK, W>; }
+template <bool FLOW, int CK, int W, int MB>
+static void* step_fn() { return (void*)k_step<FLOW, CK, W, MB>; }
 
+// hi: the variant compiled for DSM_MINB_HI blocks per SM (kinds without a
+// correlator only)
 template <int W>
-static void* pick_step_w(bool flow, int ck) {
-  if (flow) return step_fn<true, 0, W>();
-  return ck == 2 ? step_fn<false, 2, W>() : ck == 1 ? step_fn<false, 1, W>() : step_fn<false, 0, W>();
+static void* pick_step_w(bool flow, int ck, bool hi) {
+  if (flow) return hi ? step_fn<true, 0, W, DSM_MINB_HI>() : step_fn<true, 0, W, DSM_MINB>();
+  if (ck == 0) return hi ? step_fn<false, 0, W, DSM_MINB_HI>() : step_fn<false, 0, W, DSM_MINB>();
+  return ck == 2 ? step_fn<false, 2, W, DSM_MINB>() : step_fn<false, 1, W, DSM_MINB>();
 }
-static void* pick_step(bool flow, int ck, int lanes) {
-  return lanes == 16 ? pick_step_w<16>(flow, ck) : pick_step_w<32>(flow, ck);
+static void* pick_step(bool flow, int ck, int lanes, bool hi) {
+  return lanes == 16 ? pick_step_w<16>(flow, ck, hi) : pick_step_w<32>(flow, ck, hi);
 }
 
 static int tile_lanes(const LaunchCfg& cfg) { return cfg.lanes == 16 ? 16 : 32; }
@@ -1480,14 +1490,56 @@ static cudaError_t prep_step(void* fn, size_t sm) {
   return cudaSuccess;
 }
 
-int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg) {
-  const size_t sm = step_smem(cfg);
-  void* fn = pick_step(flow, corr, tile_lanes(cfg));
+static int blocks_per_sm(void* fn, const LaunchCfg& cfg, size_t sm) {
   if (prep_step(fn, sm) != cudaSuccess) return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, cfg.warps_per_block * 32, sm) != cudaSuccess) return 0;
   return nb;
 }
+
+// The step kernel of a launch shape and its resident blocks per SM.  Kinds
+// without a correlator have a second build for more resident blocks; it is
+// taken when the shape's shared memory lets more of its blocks reside than of
+// the standard build's (its smaller register budget costs a little per warp,
+// so a tie keeps the standard build).  The choice depends on the shape and the
+// device only and is cached, so planning and launching always agree.
+struct StepChoice {
+  void* fn;
+  int bps;
+};
+static StepChoice choose_step(bool flow, int ck, const LaunchCfg& cfg) {
+  struct Key {
+    int dev, flow, ck, lanes, warps;
+    size_t sm;
+    StepChoice v;
+  };
+  static std::mutex mu;
+  static std::vector<Key> cache;
+  const size_t sm = step_smem(cfg);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return {pick_step(flow, ck, tile_lanes(cfg), false), 0};
+  const int lanes = tile_lanes(cfg), fl = flow ? 1 : 0, kk = flow ? 0 : ck;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Key& k : cache)
+      if (k.dev == dev && k.flow == fl && k.ck == kk && k.lanes == lanes && k.warps == cfg.warps_per_block && k.sm == sm)
+        return k.v;
+  }
+  void* std_fn = pick_step(flow, ck, lanes, false);
+  StepChoice c{std_fn, blocks_per_sm(std_fn, cfg, sm)};
+  if (flow || ck == 0) {
+    void* hi_fn = pick_step(flow, ck, lanes, true);
+    const int nb = blocks_per_sm(hi_fn, cfg, sm);
+    if (nb > c.bps) c = StepChoice{hi_fn, nb};
+  }
+  if (c.bps > 0) {
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back(Key{dev, fl, kk, lanes, cfg.warps_per_block, sm, c});
+  }
+  return c;
+}
+
+int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg) { return choose_step(flow, corr, cfg).bps; }
 
 size_t step_block_smem(const LaunchCfg& cfg) { return step_smem(cfg); }
 
@@ -1496,7 +1548,7 @@ cudaError_t launch_step(const EnsDev* d_ens, int n_ens, const long long* d_prefi
                         const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
                         const StepList& lst) {
   const size_t sm = step_smem(cfg);
-  void* fn = pick_step(flow, corr, tile_lanes(cfg));
+  void* fn = choose_step(flow, corr, cfg).fn;
   cudaError_t err = prep_step(fn, sm);
   if (err != cudaSuccess) return err;
   StepList l = lst;
