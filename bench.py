@@ -430,8 +430,7 @@ def run_poly(args, device: int = 0) -> dict:
     p=64 m=8 (levels for t_end=1e6).  One persistent launch per size class,
     the schedule chosen by the online autotuner on --poly-tune-window windows,
     then --poly-windows timed windows of --poly-window tau_K (default 4 x 250,
-    1e3 tau_K as for the monodisperse workload) replayed as one CUDA graph
-    (dsm_advance_series)."""
+    1e3 tau_K as for the monodisperse workload) in one dsm_advance_series call."""
     import gpu_dsm_gb300 as dsm
 
     n = args.poly_chains
@@ -452,7 +451,8 @@ def run_poly(args, device: int = 0) -> dict:
                         f"max {int(nkc.max())}), beta=1, G(t) p=64 m=8",
             "events_per_s": ev / (ms / 1e3), "events": int(ev), "kernel_ms": ms,
             "windows": args.poly_windows, "window_tau": args.poly_window, "autotune": best, "schedule": sched,
-            "timing": "CUDA events around one graph replay of the windows (size-class launches + overflow launch)"}
+            "timing": "CUDA events around the windows of one dsm_advance_series call (size-class launches + "
+                      "overflow launch per window, issued without host synchronisation)"}
 
 
 # ---------------------------------------------------------------- serving

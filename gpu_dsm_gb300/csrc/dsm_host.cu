@@ -928,22 +928,26 @@ static void series_free(dsm_sim* s) {
 static long long* ser_win_h(dsm_sim* s) { return (long long*)s->ser_h; }
 static double* ser_out_h(dsm_sim* s) { return (double*)((char*)s->ser_h + (size_t)s->ser_cap * 2 * sizeof(long long)); }
 
-static int series_capture(dsm_sim* s, int n, cudaGraphExec_t* exec) {
+// The work of n windows on s->st: window ends in, per window (equilibrium) or
+// per group of windows (flow) the step launch(es), sums and counters out.
+// Captured into a graph, or (capturing = false) issued directly.
+static int series_enqueue(dsm_sim* s, int n, bool capturing) {
   const size_t win_bytes = (size_t)s->ser_cap * 2 * sizeof(long long);
   long long* d_win = (long long*)s->ser_d;
   double* d_out = (double*)((char*)s->ser_d + win_bytes);
-  CK(cudaStreamSynchronize(s->st));
-  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
   int rc = DSM_OK;
   auto cap = [&](cudaError_t e, const char* what) {
     if (e != cudaSuccess && rc == DSM_OK) rc = fail(s, DSM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
   };
+  // timing events inside a capture must be real event-record nodes (a plain
+  // record there only orders streams)
+  auto record = [&](cudaEvent_t ev) {
+    cap(capturing ? cudaEventRecordWithFlags(ev, s->st, cudaEventRecordExternal) : cudaEventRecord(ev, s->st), "event");
+  };
   cap(cudaMemcpyAsync(d_win, s->ser_h, win_bytes, cudaMemcpyHostToDevice, s->st), "series window copy");
   cap(cudaMemsetAsync(s->d_status, 0, sizeof(int), s->st), "memset");
   cap(cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), s->st), "memset");
-  // timing events must be real event-record nodes (a plain record inside a
-  // capture only orders streams)
-  cap(cudaEventRecordWithFlags(s->ev0, s->st, cudaEventRecordExternal), "event");
+  record(s->ev0);
   if (s->flow) {
     for (int w0 = 0; w0 < n && rc == DSM_OK; w0 += kSeriesGroup) {
       const int k = std::min(kSeriesGroup, n - w0);
@@ -957,10 +961,17 @@ static int series_capture(dsm_sim* s, int n, cudaGraphExec_t* exec) {
       if (rc == DSM_OK) rc = enqueue_step(s);
     }
   }
-  cap(cudaEventRecordWithFlags(s->ev1, s->st, cudaEventRecordExternal), "event");
+  record(s->ev1);
   cap(cudaMemcpyAsync(ser_out_h(s), d_out, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st), "copy");
   cap(cudaMemcpyAsync(s->hw->cnt, s->d_counters, sizeof(s->hw->cnt), cudaMemcpyDeviceToHost, s->st), "copy");
   cap(cudaMemcpyAsync(&s->hw->status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->st), "copy");
+  return rc;
+}
+
+static int series_capture(dsm_sim* s, int n, cudaGraphExec_t* exec) {
+  CK(cudaStreamSynchronize(s->st));
+  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+  const int rc = series_enqueue(s, n, true);
   cudaGraph_t g = nullptr;
   const cudaError_t ee = cudaStreamEndCapture(s->st, &g);
   if (rc != DSM_OK) { if (g) cudaGraphDestroy(g); return rc; }
@@ -985,6 +996,7 @@ static int series_prepare(dsm_sim* s, int n, cudaGraphExec_t* exec) {
     if (s->flow) s->h.win_stress = (float*)((char*)s->ser_d + (hbytes + 255) / 256 * 256);
     s->ser_version = s->sched_version;
   }
+  if (!exec) return DSM_OK;  // buffers only (windows issued directly)
   for (auto& g : s->ser_graphs)
     if (g.first == n) { *exec = g.second; return DSM_OK; }
   cudaGraphExec_t e = nullptr;
@@ -1003,8 +1015,13 @@ static int series_start(dsm_sim* s, const double* ends, int n) {
       return fail(s, DSM_ERR_INVALID, "series end times must ascend from the current time");
     t_prev = ends[w];
   }
+  // equilibrium with size classes: the windows are issued directly.  Replayed
+  // from one graph, every window after the first ran 10-20 % slower on the
+  // 262144-chain log-normal melt (a graph of one window did not), while a few
+  // launches per window cost nothing next to windows of seconds.
+  const bool direct = !s->flow && !s->classes.empty();
   cudaGraphExec_t exec = nullptr;
-  const int rc = series_prepare(s, n, &exec);
+  int rc = series_prepare(s, n, direct ? nullptr : &exec);
   if (rc != DSM_OK) return rc;
   long long* h_win = ser_win_h(s);
   t_prev = s->t_done;
@@ -1018,7 +1035,12 @@ static int series_start(dsm_sim* s, const double* ends, int n) {
   EnsDev& E = s->h;
   E.step_limit = INT64_MAX;
   CK(cudaMemcpyAsync(s->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
-  CK(cudaGraphLaunch(exec, s->st));
+  if (direct) {
+    rc = series_enqueue(s, n, false);
+    if (rc != DSM_OK) return rc;
+  } else {
+    CK(cudaGraphLaunch(exec, s->st));
+  }
   CK(cudaEventRecord(s->ev_done, s->st));
   return DSM_OK;
 }
