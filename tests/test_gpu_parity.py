@@ -369,7 +369,10 @@ def test_graph_series_equals_windows(dsm_mod, oracle_mod):
     assert_bitexact(gpu_state(b), gpu_state(a), what="series replay")
 
 
-def test_graph_series_size_classes(dsm_mod, oracle_mod):
+def test_series_size_classes(dsm_mod, oracle_mod):
+    """An equilibrium series of a melt in size classes (its windows issued
+    directly on the handle's streams, not from a graph), twice in a row:
+    events and state equal the oracle's."""
     nkc = _lognormal_nk(300, 31, 150, 0.64, 10, 900)
     g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=300, seed=37, nk_chain=nkc)
     g.set_schedule(small_slot=48, z_margin_sd=0.01)
@@ -378,6 +381,10 @@ def test_graph_series_size_classes(dsm_mod, oracle_mod):
     ev, _ = g.advance_series(1.5, 4)
     assert ev == o.run(6.0)
     assert_bitexact(gpu_state(g), o.get_state(), what="series with size classes")
+    ev, _ = g.advance_series(1.5, 3)
+    assert ev == o.run(10.5)
+    assert g.window_stats()["events"] == ev
+    assert_bitexact(gpu_state(g), o.get_state(), what="second series with size classes")
 
 
 @pytest.mark.parametrize("lanes", [0, 32])
