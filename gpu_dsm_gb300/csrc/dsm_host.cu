@@ -1015,11 +1015,12 @@ static int series_start(dsm_sim* s, const double* ends, int n) {
       return fail(s, DSM_ERR_INVALID, "series end times must ascend from the current time");
     t_prev = ends[w];
   }
-  // equilibrium with size classes: the windows are issued directly.  Replayed
-  // from one graph, every window after the first ran 10-20 % slower on the
-  // 262144-chain log-normal melt (a graph of one window did not), while a few
-  // launches per window cost nothing next to windows of seconds.
-  const bool direct = !s->flow && !s->classes.empty();
+  // size classes: the windows (flow: the groups of windows) are issued
+  // directly.  Replayed from one graph, every window after the first ran
+  // 10-20 % slower on the 262144-chain log-normal melt (a graph of one window
+  // did not), while a few launches per window cost nothing next to windows of
+  // seconds.
+  const bool direct = !s->classes.empty();
   cudaGraphExec_t exec = nullptr;
   int rc = series_prepare(s, n, direct ? nullptr : &exec);
   if (rc != DSM_OK) return rc;
