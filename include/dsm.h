@@ -126,7 +126,8 @@ int dsm_advance(dsm_sim* sim, double t_end, int64_t step_limit, const volatile i
 /* Advance through n windows of dt tau_K from the current time (window w ends
  * at t + dt*(w+1), the times dsm_advance calls would use) as one CUDA graph
  * launch, captured on the first call for this n and launch schedule and
- * replayed afterwards.  Flow ensembles: out[w] (n entries, may be NULL)
+ * replayed afterwards (with size classes the same launches are issued
+ * directly, with no host synchronisation between windows).  Flow ensembles: out[w] (n entries, may be NULL)
  * receives the stress at the end of window w, as dsm_stress would after each
  * window.  Replaces the host loop of time_step_call_block +
  * calc_stress_call_block per output time (common/main_cuda.cu flow loop,
