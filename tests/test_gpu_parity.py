@@ -540,3 +540,20 @@ def test_chain_offset_shards_equal_one_ensemble(dsm_mod):
     gw, _ = whole.gt_raw()
     gp = sum(e.gt_raw()[0] for e in parts)
     assert np.allclose(gp, gw, rtol=1e-12, atol=0.0)
+
+
+def test_resident_blocks_by_kind(dsm_mod, oracle_mod):
+    """Kinds without a correlator take the build for 6 blocks per SM when their
+    slots leave the shared memory for it (N_K = 100, 16 lanes: 33 KB blocks);
+    G(t) keeps the 4-block build.  The 6-block runs equal the oracle."""
+    kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    cases = [(dict(kappa=kap), 6), (dict(), 6), (dict(corr=True, t_end=400.0, corr_p=64, corr_m=8), 4)]
+    for kw, bps in cases:
+        g, o = pair(dsm_mod, oracle_mod, nk=100, n=2048, seed=53, **kw)
+        g.init_equilibrium()
+        o.init_equilibrium()
+        ev = g.advance(2.0)
+        assert g.last_window()["blocks_per_sm"] == bps, kw
+        if bps == 6:
+            assert ev == o.run(2.0)
+            assert_bitexact(gpu_state(g), o.get_state(), what=f"6-block build {kw}")
