@@ -47,10 +47,9 @@ namespace dsm {
 #define FULL_MASK 0xffffffffu
 #define NEND 5
 // minimum resident blocks of 4 warps per SM the step kernel is compiled for:
-// DSM_MINB (register budget 128) for every kind, and DSM_MINB_HI (budget 80)
-// for the kinds without a correlator, whose code needs fewer registers and
-// gains from more resident warps when the slots leave the shared memory for
-// them (shear at N_K = 100: 6 blocks per SM instead of 4)
+// DSM_MINB (register budget 128) and DSM_MINB_HI (budget 80) for every kind;
+// the second build gains from more resident warps when small slots leave the
+// shared memory for them (shear at N_K = 100: 6 blocks per SM instead of 4)
 #ifndef DSM_MINB
 #define DSM_MINB 4
 #endif
@@ -1445,13 +1444,13 @@ __global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win,
 template <bool FLOW, int CK, int W, int MB>
 static void* step_fn() { return (void*)k_step<FLOW, CK, W, MB>; }
 
-// hi: the variant compiled for DSM_MINB_HI blocks per SM (kinds without a
-// correlator only)
+// hi: the variant compiled for DSM_MINB_HI blocks per SM
 template <int W>
 static void* pick_step_w(bool flow, int ck, bool hi) {
   if (flow) return hi ? step_fn<true, 0, W, DSM_MINB_HI>() : step_fn<true, 0, W, DSM_MINB>();
   if (ck == 0) return hi ? step_fn<false, 0, W, DSM_MINB_HI>() : step_fn<false, 0, W, DSM_MINB>();
-  return ck == 2 ? step_fn<false, 2, W, DSM_MINB>() : step_fn<false, 1, W, DSM_MINB>();
+  if (ck == 2) return hi ? step_fn<false, 2, W, DSM_MINB_HI>() : step_fn<false, 2, W, DSM_MINB>();
+  return hi ? step_fn<false, 1, W, DSM_MINB_HI>() : step_fn<false, 1, W, DSM_MINB>();
 }
 static void* pick_step(bool flow, int ck, int lanes, bool hi) {
   return lanes == 16 ? pick_step_w<16>(flow, ck, hi) : pick_step_w<32>(flow, ck, hi);
@@ -1497,12 +1496,12 @@ static int blocks_per_sm(void* fn, const LaunchCfg& cfg, size_t sm) {
   return nb;
 }
 
-// The step kernel of a launch shape and its resident blocks per SM.  Kinds
-// without a correlator have a second build for more resident blocks; it is
-// taken when the shape's shared memory lets more of its blocks reside than of
-// the standard build's (its smaller register budget costs a little per warp,
-// so a tie keeps the standard build).  The choice depends on the shape and the
-// device only and is cached, so planning and launching always agree.
+// The step kernel of a launch shape and its resident blocks per SM.  Every
+// kind has a second build for more resident blocks; it is taken when the
+// shape's shared memory lets more of its blocks reside than of the standard
+// build's (its smaller register budget costs a little per warp, so a tie
+// keeps the standard build).  The choice depends on the shape and the device
+// only and is cached, so planning and launching always agree.
 struct StepChoice {
   void* fn;
   int bps;
@@ -1527,10 +1526,15 @@ static StepChoice choose_step(bool flow, int ck, const LaunchCfg& cfg) {
   }
   void* std_fn = pick_step(flow, ck, lanes, false);
   StepChoice c{std_fn, blocks_per_sm(std_fn, cfg, sm)};
-  if (flow || ck == 0) {
+  {
     void* hi_fn = pick_step(flow, ck, lanes, true);
     const int nb = blocks_per_sm(hi_fn, cfg, sm);
-    if (nb > c.bps) c = StepChoice{hi_fn, nb};
+    // with a correlator the smaller register budget costs more per warp: the
+    // 6-block build pays only with half as many blocks again (measured: +6 %
+    // at N_K = 50, p = 16 with 6 blocks; 2-11 % slower with 5 blocks at
+    // N_K = 100 and 150, p = 64)
+    const bool take = (flow || ck == 0) ? nb > c.bps : 2 * nb >= 3 * c.bps;
+    if (take && nb > c.bps) c = StepChoice{hi_fn, nb};
   }
   if (c.bps > 0) {
     std::lock_guard<std::mutex> lk(mu);
