@@ -570,16 +570,16 @@ static int default_schedule(dsm_sim* s) {
   int cap16 = largest_slot(s->flow, s->ck, c, 4, s->cap);
   const double pe = 1.0 / (1.0 + (double)s->P.beta), nk = (double)s->P.nk;
   const double zb = 1.0 + (nk - 1.0) * pe + 5.0 * std::sqrt(std::max(0.0, (nk - 1.0) * pe * (1.0 - pe))) + 2.0;
-  // kinds without a correlator gain from more resident blocks (their second
-  // build): the largest slot that keeps 6, else 5, blocks per SM when the
-  // chains' bound still fits it
-  if (s->flow || s->ck == 0) {
-    for (int b : {6, 5}) {
-      const int cb = largest_slot(s->flow, s->ck, c, b, s->cap);
-      if (cb >= 8 && zb <= cb) {
-        cap16 = cb;
-        break;
-      }
+  // more resident blocks pay (the second build): the largest slot that keeps
+  // 6, else 5, blocks per SM when the chains' bound still fits it; with a
+  // correlator only 6 (the second build is taken only at half as many blocks
+  // again)
+  for (int b : {6, 5}) {
+    if (b == 5 && !(s->flow || s->ck == 0)) break;
+    const int cb = largest_slot(s->flow, s->ck, c, b, s->cap);
+    if (cb >= 8 && zb <= cb) {
+      cap16 = cb;
+      break;
     }
   }
   if (cap16 >= s->cap) {
