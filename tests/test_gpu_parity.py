@@ -546,11 +546,14 @@ def test_resident_blocks_by_kind(dsm_mod, oracle_mod):
     """The build for 6 blocks per SM is taken when the slots leave the shared
     memory for it: without a correlator as soon as more blocks fit (N_K = 100,
     16 lanes: 33 KB blocks), with G(t) only at half as many blocks again
-    (N_K = 25, p = 16: 6 blocks; N_K = 100, p = 64: 5 would fit, the 4-block
-    build stays).  The 6-block runs equal the oracle."""
+    (N_K = 25, p = 16: 6 blocks).  The default schedule picks a smaller slot
+    that keeps 6 blocks when the chains fit it (N_K = 100 with G(t), p = 64),
+    and keeps 4 blocks when they do not (N_K = 200, p = 64).  The 6-block runs
+    equal the oracle."""
     kap = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
-    cases = [(100, dict(kappa=kap), 6), (100, dict(), 6), (100, dict(corr=True, t_end=400.0, corr_p=64, corr_m=8), 4),
-             (25, dict(corr=True, t_end=400.0, corr_p=16, corr_m=2), 6)]
+    cases = [(100, dict(kappa=kap), 6), (100, dict(), 6), (100, dict(corr=True, t_end=400.0, corr_p=64, corr_m=8), 6),
+             (25, dict(corr=True, t_end=400.0, corr_p=16, corr_m=2), 6),
+             (200, dict(corr=True, t_end=400.0, corr_p=64, corr_m=8), 4)]
     for nk, kw, bps in cases:
         g, o = pair(dsm_mod, oracle_mod, nk=nk, n=2048, seed=53, **kw)
         g.init_equilibrium()
