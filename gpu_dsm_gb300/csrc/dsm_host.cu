@@ -1442,17 +1442,51 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     CK(cudaMemsetAsync(dW, 0, 16, s->st));
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
-    fit_block(cfg, optin);
-    const int bps = step_max_blocks_per_sm(g.flow, g.corr, cfg);
+    // when every ensemble of the group planned a small-slot class (its own
+    // schedule), the group runs in the smallest of those slots and the chains
+    // that outgrow it finish in an overflow launch with slots of the group's
+    // largest capacity, as in dsm_advance; otherwise one launch with slots of
+    // that capacity
+    int small = cfg.slot_cap;
+    for (int q = 0; q < k; ++q) {
+      const dsm_sim* x = sims[g.idx[q]];
+      const bool own = !x->classes.empty() && x->classes.back().cfg.lanes == g.lanes;
+      small = own ? std::min(small, x->classes.back().cfg.slot_cap) : cfg.slot_cap + 1;
+      if (!own) break;
+    }
+    const bool overflow = small < cfg.slot_cap;
+    LaunchCfg run = cfg;
+    if (overflow) run.slot_cap = small;
+    fit_block(run, optin);
+    const int bps = step_max_blocks_per_sm(g.flow, g.corr, run);
     if (bps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory"); break; }
-    const int tiles = cfg.warps_per_block * 32 / cfg.lanes;
+    const int tiles = run.warps_per_block * 32 / run.lanes;
     const long long want = (pre[k] + tiles - 1) / tiles;
     const int grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
+    StepList lst;
+    LaunchCfg oc{1, cfg.slot_cap, cfg.pmax, 32};
+    int ogrid = 0;
+    if (overflow) {
+      const int obps = step_max_blocks_per_sm(g.flow, g.corr, oc);
+      if (obps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch capacity does not fit one shared-memory slot"); break; }
+      ogrid = obps * s->sm_count;
+      int* dDef = nullptr;
+      CK(cudaMallocAsync((void**)&dDef, sizeof(int) * (size_t)pre[k], s->st));
+      tmp.push_back(dDef);
+      lst.defer = dDef;
+      lst.n_defer = dW + 2;
+    }
     if (fan) {
       CK(cudaEventRecord(ready, s->st));
       CK(cudaStreamWaitEvent(gs, ready, 0));
     }
-    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, cfg, nullptr, (int*)(dW + 1), grid, gs));
+    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, run, nullptr, (int*)(dW + 1), grid, gs, lst));
+    if (overflow) {
+      StepList ol;
+      ol.order = lst.defer;
+      ol.dyn_total = dW + 2;
+      CK(launch_step(dE, k, dP, 0, dW + 3, g.flow, g.corr, oc, nullptr, (int*)(dW + 1), ogrid, gs, ol));
+    }
     if (fan) {
       cudaEvent_t j = nullptr;
       CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));

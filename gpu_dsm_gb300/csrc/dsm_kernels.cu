@@ -109,6 +109,17 @@ struct Tile {
     for (int o = W / 2; o > 0; o >>= 1) v = __fadd_rn(v, shfl_xor(v, o));
     return v;
   }
+  // Sums over the strands of a chain that come out the same for both tile
+  // widths: strand i is accumulated into partial i mod 16 in index order and
+  // the 16 partials meet in a 16-lane xor tree.  A 32-lane tile does this on
+  // its lanes 0..15 and hands lane 0's result to every lane; the callers loop
+  // over strands with stride 16 on those lanes only.
+  __device__ __forceinline__ bool strand_sum_lane() const { return W == 16 || lane < 16; }
+  __device__ __forceinline__ float strand_sum(float v) const {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) v = __fadd_rn(v, shfl_xor(v, o));
+    return W == 16 ? v : shfl(v, 0);
+  }
   __device__ __forceinline__ int maxi(int v) const {
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) v = max(v, shfl_xor(v, o));
@@ -528,7 +539,7 @@ __device__ __forceinline__ void flow_deform(const EnsDev& E, Slot& sl, int Z, fl
 template <int W>
 __device__ __forceinline__ void flow_stress(const EnsDev& E, const Slot& sl, int Z, const Tile<W>& t, float* o) {
   float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int i = t.lane; i < Z; i += W) {
+  for (int i = t.lane; t.strand_sum_lane() && i < Z; i += 16) {
     const float4 q = sl.Q[i];
     const float w = __ldg(&E.INV3N[sl.N[i]]);
     s[0] = __fmaf_rn(-__fmul_rn(q.x, q.x), w, s[0]);
@@ -540,7 +551,7 @@ __device__ __forceinline__ void flow_stress(const EnsDev& E, const Slot& sl, int
     s[6] = __fadd_rn(s[6], __fsqrt_rn(q.w));
   }
 #pragma unroll
-  for (int q = 0; q < 7; ++q) s[q] = t.sum(s[q]);
+  for (int q = 0; q < 7; ++q) s[q] = t.strand_sum(s[q]);
   if (t.lane == 0) {
 #pragma unroll
     for (int q = 0; q < 7; ++q) o[q] = s[q];
@@ -661,14 +672,14 @@ __device__ __forceinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, i
       chain_com<W>(E, sl, Z, c, t, v);
     } else {
       float sxy = 0.f, syz = 0.f, sxz = 0.f;
-      for (int s = lane; s < Z; s += W) {
+      for (int s = lane; t.strand_sum_lane() && s < Z; s += 16) {
         const float4 q = sl.Q[s];
         const float w = __ldg(&E.INV3N[sl.N[s]]);
         sxy = __fmaf_rn(-__fmul_rn(q.x, q.y), w, sxy);
         syz = __fmaf_rn(-__fmul_rn(q.y, q.z), w, syz);
         sxz = __fmaf_rn(-__fmul_rn(q.x, q.z), w, sxz);
       }
-      v[0] = t.sum(sxy); v[1] = t.sum(syz); v[2] = t.sum(sxz);
+      v[0] = t.strand_sum(sxy); v[1] = t.strand_sum(syz); v[2] = t.strand_sum(sxz);
     }
     const int ins = k0.ins;
     const long long n0 = k0.nins + 1;

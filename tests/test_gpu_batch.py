@@ -39,6 +39,39 @@ def test_batch_equals_separate(dsm_mod, oracle_mod):
     assert_bitexact(gpu_state(batch[1]), o.get_state(), what="batch vs oracle")
 
 
+def test_batch_small_slots_overflow(dsm_mod, oracle_mod):
+    """Ensembles whose own schedules run small slots are batched in the
+    smallest of them; chains that outgrow it finish in the batch's overflow
+    launch.  Shear and equilibrium ensembles, slots forced small so that many
+    chains are handed over: events and state equal separate dsm_advance calls
+    and the oracle."""
+    shear = lambda g: (0.0, g, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    specs = [dict(nk=60, n_chains=300, kappa=shear(2e-3), seed=12, stream=0),
+             dict(nk=60, n_chains=200, kappa=shear(8e-3), seed=12, stream=1),
+             dict(nk=50, n_chains=256, seed=13, stream=2),
+             dict(nk=70, n_chains=128, seed=14, stream=3)]
+    batch = [dsm_mod.Ensemble(**s) for s in specs]
+    single = [dsm_mod.Ensemble(**s) for s in specs]
+    for e, slot in zip(batch + single, [30, 28, 26, 34] * 2):
+        e.set_schedule(small_slot=slot, z_margin_sd=0.01)
+        e.init_equilibrium()
+    deferred = 0
+    for t in (6.0, 15.0):
+        ev_b = dsm_mod.advance_batch(batch, t)
+        deferred += sum(e.window_stats()["deferred"] for e in batch)
+        ev_s = [e.advance(t) for e in single]
+        assert list(ev_b) == ev_s
+        for b, s in zip(batch, single):
+            assert_bitexact(gpu_state(b), gpu_state(s), what="batch with overflow vs single")
+        for k in (0, 1):
+            assert np.array_equal(batch[k].stress()[0], single[k].stress()[0])
+    assert deferred > 0
+    o = oracle_mod.Oracle(nk=60, n_chains=200, kappa=shear(8e-3), seed=12, stream=1)
+    o.init_equilibrium()
+    o.run(15.0)
+    assert_bitexact(gpu_state(batch[1]), o.get_state(), what="batch with overflow vs oracle")
+
+
 def test_async_handles_overlap(dsm_mod, oracle_mod):
     """Windows and graph series enqueued on several handles at once (each on
     its own stream) and polled give the synchronous results."""

@@ -563,3 +563,25 @@ def test_resident_blocks_by_kind(dsm_mod, oracle_mod):
         if bps == 6:
             assert ev == o.run(2.0)
             assert_bitexact(gpu_state(g), o.get_state(), what=f"6-block build {kw}")
+
+
+def test_observables_independent_of_tile_width(dsm_mod):
+    """Stress sums over the strands of a chain take the same order for 16- and
+    32-lane tiles, so the flow stress and the G(t) sums do not depend on where
+    a chain ran: one chain per warp and two per warp give the same bits."""
+    kap = (0.0, 3.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    specs = [dict(nk=70, n_chains=400, kappa=kap, seed=61),
+             dict(nk=70, n_chains=400, eq_type=1, sync_dt=1.0, t_end=200.0, corr_p=16, corr_m=2, seed=62)]
+    for spec in specs:
+        a = dsm_mod.Ensemble(**spec, lanes_per_chain=16)
+        b = dsm_mod.Ensemble(**spec, lanes_per_chain=32)
+        for x in (a, b):
+            x.init_equilibrium()
+            x.advance(40.0)
+        assert_bitexact(gpu_state(a), gpu_state(b), what="16 vs 32 lanes")
+        if "kappa" in spec:
+            assert np.array_equal(a.stress()[0], b.stress()[0])
+        else:
+            ga, ca = a.gt_raw()
+            gb, cb = b.gt_raw()
+            assert np.array_equal(ca, cb) and np.array_equal(ga, gb)
