@@ -157,8 +157,11 @@ int dsm_set_priority(dsm_sim* sim, int32_t priority);
  * (step_limit may be NULL) in one persistent launch per kind (equilibrium,
  * equilibrium with G(t), flow).  No counterpart in the reference, which runs
  * one ensemble per process; used for multi-condition runs (several flow
- * rates) and by the serving loop.  events[i] (may be NULL) receives the kMC
- * events of ensemble i.  Results equal per-ensemble dsm_advance calls. */
+ * rates) and by the serving loop.  When every ensemble of a launch planned a
+ * small-slot class, the launch uses the smallest of those slots and the chains
+ * that outgrow it finish in an overflow launch with full-capacity slots.
+ * events[i] (may be NULL) receives the kMC events of ensemble i.  Results
+ * equal per-ensemble dsm_advance calls. */
 int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end, const int64_t* step_limit,
                       uint64_t* events);
 
@@ -199,7 +202,8 @@ int dsm_pcd(double beta, int32_t nk, double* out);
  * stops at a step boundary and finishes in a third launch with slots of the
  * full capacity.  A chain goes to the small class when the mean of its
  * equilibrium strand count plus z_margin_sd standard deviations fits the
- * small slot.  Results do not depend on the schedule.  Arguments <= 0 choose
+ * small slot.  Results do not depend on the schedule (state, flow stress and
+ * G(t) to the bit; the MSD centre-of-mass sums to rounding).  Arguments <= 0 choose
  * the defaults (largest slot with 4 blocks per SM; large-class blocks in
  * proportion to its share of the work; lanes of the handle; 5 sd).  No
  * counterpart in the reference (one thread per chain, ensemble_kernel.cu). */
