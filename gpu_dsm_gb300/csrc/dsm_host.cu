@@ -1447,14 +1447,15 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     // that outgrow it finish in an overflow launch with slots of the group's
     // largest capacity, as in dsm_advance; otherwise one launch with slots of
     // that capacity
+    bool all_small = true;
     int small = cfg.slot_cap;
-    for (int q = 0; q < k; ++q) {
+    for (int q = 0; q < k && all_small; ++q) {
       const dsm_sim* x = sims[g.idx[q]];
-      const bool own = !x->classes.empty() && x->classes.back().cfg.lanes == g.lanes;
-      small = own ? std::min(small, x->classes.back().cfg.slot_cap) : cfg.slot_cap + 1;
-      if (!own) break;
+      // the small class is the last of an ensemble's classes
+      all_small = !x->classes.empty() && x->classes.back().cfg.lanes == g.lanes;
+      if (all_small) small = std::min(small, x->classes.back().cfg.slot_cap);
     }
-    const bool overflow = small < cfg.slot_cap;
+    const bool overflow = all_small && small < cfg.slot_cap;
     LaunchCfg run = cfg;
     if (overflow) run.slot_cap = small;
     fit_block(run, optin);
