@@ -9,7 +9,7 @@
 // dynamics, common/ensemble_kernel.cu:64-102); here an event is applied as soon
 // as it is picked, which yields the same state sequence.
 //
-// Two arithmetic modes:
+// Three arithmetic modes:
 //   mode 0 (FP32 mirror): FP32 strand state, rates from per-N tables and the
 //       element-wise functions of orc_math.h, rates quantised to int64 fixed
 //       point so that the event pick is an exact integer computation.  This is
@@ -18,6 +18,14 @@
 //   mode 1 (FP64 transcription): the reference formulas evaluated literally in
 //       double precision with libm (pow/exp/log/sin/cos), double state, double
 //       sums.  Used as the accuracy reference for statistics.
+//   mode 2 (reference arithmetic): the reference's chain-parallel kernels
+//       restated expression for expression in immediate-apply form: FP32
+//       rates with libm expf/powf, the running-subtraction scan with FP32 sums
+//       (flow kernel) or FP64 sums (equilibrium kernel), FP32 time relative to
+//       sync windows of at most 1e5, the reference's sample and stop rules,
+//       and random numbers from ref_tape.h.  The reference's own kernels,
+//       compiled for the host by ref_step.cpp with the same random stream,
+//       must give the same states bit for bit.
 // The measurement path (stress samples, multi-tau correlator, flow stress) is
 // accumulated in FP64 in both modes.
 //
@@ -49,6 +57,7 @@
 #endif
 
 #include "orc_math.h"
+#include "ref_tape.h"
 
 using namespace orc;
 
@@ -60,7 +69,7 @@ typedef struct orc_params {
   int32_t z_max;         // strand capacity per chain (reference: NK, ensemble.cu:99)
   int32_t cd_flag;       // input.dat line 5
   float kappa[9];        // velocity-gradient transpose, row-major (input.dat line 4)
-  int32_t mode;          // 0 FP32 mirror, 1 FP64 transcription
+  int32_t mode;          // 0 FP32 mirror, 1 FP64 transcription, 2 reference arithmetic
   uint32_t stream;       // Philox counter word 3 (ensemble id)
   uint64_t seed;         // Philox key (job_ID)
   int32_t corr_type;     // -1 none, 0 stress G(t), 1 centre-of-mass MSD(t)
@@ -246,6 +255,8 @@ struct Chain {
   R dt_prev = 0;
   int64_t k_next = 0;     // next sample index
   R r1[3] = {0, 0, 0};    // MSD mode: first entanglement in the lab frame (eq_ensemble_kernel.cu:275-277)
+  float tf = 0.0f;        // mode 2: FP32 time since the window start (chain_head.time, chain.h:47-50)
+  bool halted = false;    // mode 2: stopped by the event limit in the current run
   std::vector<int32_t> N;
   std::vector<R> Qx, Qy, Qz, q2, tau;
   // multi-tau correlator (FP64), common/eq_ensemble_kernel.cu:133-227
@@ -268,6 +279,9 @@ struct Ensemble {
   std::vector<Chain<float>> cf;
   std::vector<Chain<double>> cd;
   bool poly = false;
+  double block_time = 0.0;  // mode 2: time the block has been advanced to (ensemble_call_block.cu:67,218)
+  reftape::Key key{};
+  reftape::Law law{};
 };
 
 static inline U4 rng(const Ensemble& E, uint32_t purpose, uint64_t ctr, uint32_t hi24, uint32_t chain) {
@@ -322,7 +336,7 @@ static inline PCD partner_pcd(const Ensemble& E, uint32_t w, bool cd_created) {
     const float* T = cd_created ? E.P.gex_Md : E.P.gex_M;
     const int n = cd_created ? E.P.gex_nd : E.P.gex_n;
     const float st = cd_created ? E.P.gex_step_d : E.P.gex_step;
-    if (E.P.mode == 0) {
+    if (E.P.mode != 1) {
       const float x = u01(w) / st;
       int i = (int)std::floor(x);
       float di = x - (float)i;
@@ -460,7 +474,7 @@ void init_chain(const Ensemble& E, Chain<R>& c, uint32_t ci) {
   c.N[c.Z - 1] = nk - 1 - prev;
   for (int i = 1; i < c.Z - 1; ++i) {
     const U4 r = rng(E, P_QINIT, (uint64_t)i, 0, ci);
-    if (E.P.mode == 0) {
+    if (E.P.mode != 1) {
       float g0, g1, g2, g3;
       m_gauss2(r.x, r.y, &g0, &g1);
       m_gauss2(r.z, r.w, &g2, &g3);
@@ -477,14 +491,14 @@ void init_chain(const Ensemble& E, Chain<R>& c, uint32_t ci) {
     }
   }
   for (int i = 0; i < c.Z; ++i) {
-    if (E.P.mode == 0) c.q2[i] = (R)m_q2((float)c.Qx[i], (float)c.Qy[i], (float)c.Qz[i]);
+    if (E.P.mode != 1) c.q2[i] = (R)m_q2((float)c.Qx[i], (float)c.Qy[i], (float)c.Qz[i]);
     else c.q2[i] = c.Qx[i] * c.Qx[i] + c.Qy[i] * c.Qy[i] + c.Qz[i] * c.Qz[i];
   }
   for (int k = 0; k < c.Z - 1; ++k) {
     const U4 r = rng(E, P_TAUINIT, (uint64_t)k, 0, ci);
     const PCD pp = partner_pcd(E, r.y, false);
     if (!E.P.cd_flag) { c.tau[k] = 0; continue; }
-    if (E.P.mode == 0) c.tau[k] = (R)rate_f_t(pp, u01(r.x));
+    if (E.P.mode != 1) c.tau[k] = (R)rate_f_t(pp, u01(r.x));
     else c.tau[k] = (R)rate_f_t_d(pp, ((r.x >> 8) + 1u) * (1.0 / 16777216.0));
   }
   c.T = 0; c.Td = 0; c.step = 0; c.dt_prev = 0; c.stall = 0; c.k_next = 0;
@@ -877,6 +891,333 @@ static bool is_flow(const Ensemble& E) {
   return false;
 }
 
+// ------------------------------------------------------------------ mode 2: reference arithmetic
+// The reference's chain-parallel kernels (chain_kernel, ensemble_kernel.cu:188-502;
+// EQ_chain_kernel, eq_ensemble_kernel.cu:242-663) with the strand-parallel pass
+// (strent_kernel :114-186, EQ_strent_kernel :50-130), evaluated with the same
+// float/double expressions, written in immediate-apply form: a creation or
+// destruction is applied to the chain at once instead of through the offset
+// codec that the next step's strand pass applies.  The intrinsics are taken as
+// IEEE a/b, powf, expf, sqrtf, and fdivide(1, sumW) as (float)(1.0 / sumW),
+// as the host build of the reference kernels (refshim/cuda_runtime.h) does.
+
+static inline float rq2(float x, float y, float z) { return x * x + y * y + z * z; }
+
+// SD shift rates of pair (strand 1, strand 2): W+ moves a Kuhn step into
+// strand 1, W- out of it (ensemble_kernel.cu:149-179, :335-358)
+static inline void ref_shift(float n1, float Q, float n2, float Q2, float& wx, float& wy) {
+  wx = 0.0f;
+  wy = 0.0f;
+  if (n2 > 1.0f) {
+    const float sig1 = 0.75f / (n1 * (n1 + 1));
+    const float sig2 = 0.75f / (n2 * (n2 - 1));
+    const float pf1 = (Q == 0.0f) ? 1.0f : n1 / (n1 + 1);
+    const float pf2 = (Q2 == 0.0f) ? 1.0f : n2 / (n2 - 1);
+    const float f1 = (Q == 0.0f) ? 2.0f * n1 + 0.5f : n1;
+    const float f2 = (Q2 == 0.0f) ? 2.0f * n2 - 0.5f : n2;
+    const float fr = 2.0f / (f1 + f2);
+    wx = fr * powf(pf1 * pf2, 0.75f) * expf(Q * sig1 - Q2 * sig2);
+  }
+  if (n1 > 1.0f) {
+    const float sig1 = 0.75f / (n1 * (n1 - 1.0f));
+    const float sig2 = 0.75f / (n2 * (n2 + 1.0f));
+    const float pf1 = (Q == 0.0f) ? 1.0f : n1 / (n1 - 1.0f);
+    const float pf2 = (Q2 == 0.0f) ? 1.0f : n2 / (n2 + 1.0f);
+    const float f1 = (Q == 0.0f) ? 2.0f * n1 - 0.5f : n1;
+    const float f2 = (Q2 == 0.0f) ? 2.0f * n2 + 0.5f : n2;
+    const float fr = 2.0f / (f1 + f2);
+    wy = fr * powf(pf1 * pf2, 0.75f) * expf(-Q * sig1 + Q2 * sig2);
+  }
+}
+
+// pair rate sum written by the strand pass (ensemble_kernel.cu:181,
+// eq_ensemble_kernel.cu:126)
+static inline float ref_pair_total(const Ensemble& E, const Chain<float>& c, int j) {
+  const float n1 = (float)c.N[j], n2 = (float)c.N[j + 1];
+  float wx, wy;
+  ref_shift(n1, rq2(c.Qx[j], c.Qy[j], c.Qz[j]), n2, rq2(c.Qx[j + 1], c.Qy[j + 1], c.Qz[j + 1]), wx, wy);
+  const float tcd = E.P.cd_flag ? c.tau[j] : 0.0f;
+  return wx + wy + (float)E.P.cd_flag * (tcd + E.prefact * (n1 - 1.0f));
+}
+
+// flow deformation kappa() (ensemble_kernel.cu:105-110)
+static inline void ref_kappa(const float* k, float dt, float& x, float& y, float& z) {
+  const float nx = x + dt * k[0] * x + dt * k[1] * y + dt * k[2] * z;
+  const float ny = y + dt * k[3] * x + dt * k[4] * y + dt * k[5] * z;
+  const float nz = z + dt * k[6] * x + dt * k[7] * y + dt * k[8] * z;
+  x = nx;
+  y = ny;
+  z = nz;
+}
+
+static inline void set_strand(Chain<float>& c, int i, float x, float y, float z, float n) {
+  c.Qx[i] = x; c.Qy[i] = y; c.Qz[i] = z; c.N[i] = (int32_t)n;
+  c.q2[i] = rq2(x, y, z);
+}
+
+// scan and event of one step (the part of the chain kernel after dt):
+// P = double for the equilibrium kernel (FP64 sums, eq_ensemble_kernel.cu:334-662),
+// float for the flow kernel (ensemble_kernel.cu:211-501)
+template <class P>
+static uint32_t ref_scan(const Ensemble& E, Chain<float>& c, uint32_t ci, bool eq, P pr, const float* tsum, P Wcdz,
+                         P Wc1, P Wcz, P Wd1, P Wdz) {
+  const int Z = c.Z, cd = E.P.cd_flag;
+  const float pf = E.prefact;
+  const bool msd = eq && E.P.corr_type == 1;
+  const uint64_t ev = c.step - 1;
+  float g[4];
+  auto draw = [&](bool cd_created) { reftape::creation(E.key, E.law, ev, ci, cd_created, g); };
+  int j = 0;
+  float tpr = 0.0f;
+  if (Z != 1) tpr = tsum[0];
+  while ((pr >= tpr) && (j < Z - 2)) {
+    pr -= tpr;
+    j++;
+    tpr = tsum[j];
+  }
+  if (pr < tpr) {
+    const float n1 = (float)c.N[j], n2 = (float)c.N[j + 1];
+    const float x1 = c.Qx[j], y1 = c.Qy[j], z1 = c.Qz[j];
+    const float x2 = c.Qx[j + 1], y2 = c.Qy[j + 1], z2 = c.Qz[j + 1];
+    // 1. CD destruction of entanglement j: strands j, j+1 merge
+    const float wcdd = cd ? c.tau[j] : 0.0f;
+    if (pr < wcdd) {
+      float tx = x1 + x2, ty = y1 + y2, tz = z1 + z2;
+      if ((j == Z - 2) || (j == 0)) { tx = 0.0f; ty = 0.0f; tz = 0.0f; }
+      if (msd && j == 0) { c.r1[0] = c.r1[0] + x2; c.r1[1] = c.r1[1] + y2; c.r1[2] = c.r1[2] + z2; }
+      remove_strand(c, j + 1);
+      remove_tau(c, j);
+      set_strand(c, j, tx, ty, tz, n1 + n2);
+      c.Z = Z - 1;
+      return (uint32_t)CDD << 24 | (uint32_t)j;
+    }
+    pr -= wcdd;
+    // 2. SD shift
+    float wx, wy;
+    ref_shift(n1, rq2(x1, y1, z1), n2, rq2(x2, y2, z2), wx, wy);
+    if (pr < wx + wy) {
+      if (pr < wx) { c.N[j] += 1; c.N[j + 1] -= 1; return (uint32_t)SDP << 24 | (uint32_t)j; }
+      c.N[j] -= 1; c.N[j + 1] += 1;
+      return (uint32_t)SDM << 24 | (uint32_t)j;
+    }
+    pr -= wx + wy;
+    // 3. CD creation inside strand j
+    const P wcdc = eq ? (P)((float)cd * pf * (n1 - 1.0f)) : (P)(pf * (n1 - 1.0f));
+    if (pr < wcdc) {
+      if (Z == E.z_max) return (uint32_t)(CDC_MID | NULL_FLAG) << 24 | (uint32_t)j;
+      draw(true);
+      const float trate = g[3];
+      const float newn = floorf(0.5f + (float)(pr * (P)(n1 - 2.0f)) / (float)wcdc) + 1.0f;
+      if (j == 0) {
+        const float tw = n1 - newn;
+        const float sg = sqrtf(tw / 3.0f);
+        const float tx = g[0] * sg, ty = g[1] * sg, tz = g[2] * sg;
+        insert_at(c, 0);
+        set_strand(c, 0, 0.0f, 0.0f, 0.0f, newn);
+        set_strand(c, 1, tx, ty, tz, tw);
+        c.tau[0] = trate;
+        if (msd) { c.r1[0] = c.r1[0] + -tx; c.r1[1] = c.r1[1] + -ty; c.r1[2] = c.r1[2] + -tz; }
+      } else {
+        const float sg = sqrtf((newn * (n1 - newn)) / (3.0f * n1));
+        const float ra = newn / n1;
+        float tx = g[0] * sg, ty = g[1] * sg, tz = g[2] * sg;
+        tx = tx + x1 * ra;
+        ty = ty + y1 * ra;
+        tz = tz + z1 * ra;
+        insert_at(c, j);
+        set_strand(c, j, tx, ty, tz, newn);
+        set_strand(c, j + 1, x1 - tx, y1 - ty, z1 - tz, n1 - newn);
+        c.tau[j] = trate;
+      }
+      c.Z = Z + 1;
+      return (uint32_t)CDC_MID << 24 | (uint32_t)j | (uint32_t)newn << 8;
+    }
+    pr -= wcdc;
+  } else {
+    pr -= tpr;
+  }
+  const float Nh = (float)c.N[0], Nt = (float)c.N[Z - 1];
+  // 4. CD creation in the tail strand
+  if (pr < Wcdz) {
+    if (Z == E.z_max) return (uint32_t)(CDC_TAIL | NULL_FLAG) << 24;
+    draw(true);
+    const float newn = 1.0f + floorf(0.5f + (float)(pr * (P)(Nt - 2.0f)) / (float)Wcdz);
+    const float sg = (Z == 1) ? 0.0f : sqrtf(newn / 3.0f);
+    c.tau[Z] = c.tau[Z - 1];
+    set_strand(c, Z, 0.0f, 0.0f, 0.0f, Nt - newn);
+    set_strand(c, Z - 1, g[0] * sg, g[1] * sg, g[2] * sg, newn);
+    c.tau[Z - 1] = g[3];
+    c.Z = Z + 1;
+    return (uint32_t)CDC_TAIL << 24 | (uint32_t)newn << 8;
+  }
+  pr -= Wcdz;
+  // 5. SD creation at the head or the tail
+  if (pr < Wc1 + Wcz) {
+    if (Z == E.z_max) return (uint32_t)(SDC_HEAD | NULL_FLAG) << 24;
+    draw(false);
+    if (pr < Wc1) {
+      const float tw = Nh - 1.0f;
+      const float sg = (Z == 1) ? 0.0f : sqrtf(tw / 3.0f);
+      const float tx = g[0] * sg, ty = g[1] * sg, tz = g[2] * sg;
+      insert_at(c, 0);
+      set_strand(c, 0, 0.0f, 0.0f, 0.0f, 1.0f);
+      set_strand(c, 1, tx, ty, tz, tw);
+      c.tau[0] = g[3];
+      if (msd) { c.r1[0] = c.r1[0] + -tx; c.r1[1] = c.r1[1] + -ty; c.r1[2] = c.r1[2] + -tz; }
+      c.Z = Z + 1;
+      return (uint32_t)SDC_HEAD << 24;
+    }
+    const float tw = Nt - 1.0f;
+    const float sg = (Z == 1) ? 0.0f : sqrtf(tw / 3.0f);
+    c.tau[Z] = c.tau[Z - 1];
+    set_strand(c, Z, 0.0f, 0.0f, 0.0f, 1.0f);
+    set_strand(c, Z - 1, g[0] * sg, g[1] * sg, g[2] * sg, tw);
+    c.tau[Z - 1] = g[3];
+    c.Z = Z + 1;
+    return (uint32_t)SDC_TAIL << 24;
+  }
+  pr -= Wc1 + Wcz;
+  // 6. SD destruction at the head or the tail
+  if (pr < Wd1 + Wdz) {
+    if (pr < Wd1) {
+      const float n1 = (float)c.N[1];
+      if (msd) { c.r1[0] = c.r1[0] + c.Qx[1]; c.r1[1] = c.r1[1] + c.Qy[1]; c.r1[2] = c.r1[2] + c.Qz[1]; }
+      remove_strand(c, 0);
+      remove_tau(c, 0);
+      set_strand(c, 0, 0.0f, 0.0f, 0.0f, n1 + 1.0f);
+      c.Z = Z - 1;
+      return (uint32_t)SDD_HEAD << 24;
+    }
+    set_strand(c, Z - 2, 0.0f, 0.0f, 0.0f, (float)c.N[Z - 2] + 1.0f);
+    c.Z = Z - 1;
+    return (uint32_t)SDD_TAIL << 24;
+  }
+  return (uint32_t)NULL_FLAG << 24 | 0xffffu;  // no process matched (roundoff)
+}
+
+// rates, dt, clock, uniform, then ref_scan (chain_kernel :211-290,
+// EQ_chain_kernel :333-417)
+static void ref_event(const Ensemble& E, Chain<float>& c, uint32_t ci, bool eq) {
+  const int Z = c.Z, cd = E.P.cd_flag;
+  const float be = (float)E.P.beta, pf = E.prefact;
+  static thread_local std::vector<float> tsum;
+  tsum.resize(Z > 1 ? (size_t)(Z - 1) : 1);
+  for (int j = 0; j < Z - 1; ++j) tsum[j] = ref_pair_total(E, c, j);
+  const float Nh = (float)c.N[0], Nt = (float)c.N[Z - 1];
+  float wc1 = 0.0f, wd1 = 0.0f, wcz = 0.0f, wdz = 0.0f;
+  if (Z == 1) {
+    wc1 = 1.0f / (be * (float)c.nk);
+    wcz = wc1;
+  } else {
+    if (Nh == 1.0f) {
+      const float nn = (float)c.N[1];
+      const float f2 = (Z == 2) ? nn + 0.25f : 0.5f * nn;
+      wd1 = 1.0f / (0.75f + f2);
+    } else {
+      wc1 = 2.0f / (be * (Nh + 0.5f));
+    }
+    if (Nt == 1.0f) {
+      const float np = (float)c.N[Z - 2];
+      const float f1 = (Z == 2) ? np + 0.25f : 0.5f * np;
+      wdz = eq ? 1.0f / (0.75f + f1) : 1.0f / (f1 + 0.75f);
+    } else {
+      wcz = 2.0f / (be * (Nt + 0.5f));
+    }
+  }
+  float dt;
+  uint32_t code;
+  if (eq) {
+    double swp = 0.0;
+    for (int j = 0; j < Z - 1; ++j) swp += tsum[j];
+    const double wcdz = (double)cd * (double)pf * (Nt - 1.0f);
+    const double sumw = swp + (double)wc1 + (double)wcz + (double)wd1 + (double)wdz + wcdz;
+    dt = (float)(1.0 / sumw);
+    if (dt == 0.0f) c.stall = 1;
+    if (std::isnan(dt)) c.stall = 2;
+    if (std::isinf(dt)) c.stall = 3;
+    c.tf += dt;
+    const float u = reftape::uniform(E.key, c.step, ci);
+    c.step++;
+    code = ref_scan<double>(E, c, ci, true, sumw * u, tsum.data(), wcdz, wc1, wcz, wd1, wdz);
+  } else {
+    float swp = 0.0f;
+    for (int j = 0; j < Z - 1; ++j) swp += tsum[j];
+    const float wcdz = pf * (Nt - 1.0f);
+    const float sumw = swp + wc1 + wcz + wd1 + wdz + wcdz;
+    dt = 1.0f / sumw;
+    if (dt == 0.0f) c.stall = 1;
+    if (std::isnan(dt)) c.stall = 2;
+    if (std::isinf(dt)) c.stall = 3;
+    c.tf += dt;
+    const float u = reftape::uniform(E.key, c.step, ci);
+    c.step++;
+    code = ref_scan<float>(E, c, ci, false, sumw * u, tsum.data(), wcdz, wc1, wcz, wd1, wdz);
+  }
+  c.dt_prev = dt;
+  c.hash = hash_step(c.hash, code);
+}
+
+// One chain through one sync window (universal time ut, window length sync),
+// one iteration per step of the reference's loop: the strand pass (flow
+// deformation by the previous dt), then the chain kernel's stop test, its
+// sample (equilibrium, eq_ensemble_kernel.cu:260-331) and its event.
+static int64_t run_ref_window(const Ensemble& E, Chain<float>& c, uint32_t ci, float ut, float sync,
+                              int64_t limit, bool flow) {
+  const bool eq = !flow;
+  const bool corr = eq && E.P.corr_type >= 0;
+  const int res = (int)E.P.corr_dt;
+  int64_t done = 0;
+  if (c.halted) return 0;
+  for (;;) {
+    if (flow)
+      for (int i = 0; i < c.Z; ++i) ref_kappa(E.kap, c.dt_prev, c.Qx[i], c.Qy[i], c.Qz[i]);
+    if (limit >= 0 && (int64_t)c.step >= limit) {
+      c.halted = true;
+      c.dt_prev = 0.0f;
+      return done;
+    }
+    bool reach;
+    if (corr) reach = ((c.tf >= sync) && (ut + sync <= (float)((int)c.k_next * res))) || (c.stall != 0);
+    else reach = (c.tf >= sync) || (c.stall != 0);
+    if (reach) {
+      c.tf -= sync;
+      c.dt_prev = 0.0f;
+      return done;
+    }
+    if (corr && ut + c.tf > (float)((int)c.k_next * res)) {
+      double v[3];
+      if (E.P.corr_type == 1) com_sample(c, v); else stress_sample(c, v);
+      corr_add(E, c, v, 0);
+      c.k_next++;
+      if (ut + c.tf > (float)((int)c.k_next * res)) continue;
+    }
+    ref_event(E, c, ci, eq);
+    ++done;
+  }
+}
+
+// the step loops of time_step_call_block / EQ_time_step_call_block
+// (ensemble_call_block.cu:106-379): sync windows of at most 1e5 from the
+// block's time to reach_time; limit >= 0 also stops a chain after that many
+// steps in this run.
+int64_t run_ref(Ensemble& E, double reach_time, int64_t limit, int nthreads) {
+  const bool flow = is_flow(E);
+  const int n = E.P.n_chains;
+  for (auto& c : E.cf) c.halted = false;
+  const float interval = (float)(reach_time - E.block_time);
+  const int nsync = int(std::floor((interval - 0.5) / 1e5)) + 1;
+  int64_t total = 0;
+  for (int is = 0; is < nsync; ++is) {
+    float sync = 1e5f;
+    if (is + 1 == nsync) sync = (float)(interval - is * 1e5);
+    const float ut = (float)(E.block_time + is * 1e5);
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : total) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int i = 0; i < n; ++i) total += run_ref_window(E, E.cf[i], (uint32_t)i, ut, sync, limit, flow);
+  }
+  E.block_time = reach_time;
+  return total;
+}
+
 // Run one chain until its time reaches t_end (or step_limit events).  Per
 // iteration (common/ensemble_kernel.cu:114-207, eq_ensemble_kernel.cu:260-331):
 // deform by the previous dt (flow), take due stress samples (equilibrium),
@@ -955,9 +1296,12 @@ void* orc_create(const orc_params* p) {
   E->prefact_d = E->prefact;
   E->tab = make_tables(nkmax, E->P.beta, E->prefact);
   E->dt_sample_ticks = (int64_t)std::llrint(p->corr_dt * TICKS);
-  if (p->mode == 0) E->cf.resize(p->n_chains); else E->cd.resize(p->n_chains);
+  if (p->mode != 1) E->cf.resize(p->n_chains); else E->cd.resize(p->n_chains);
+  E->key = reftape::Key{p->seed, p->stream, p->chain_offset};
+  E->law = reftape::Law{E->pcd.c1, E->pcd.At, E->pcd.tau_0, E->pcd.alpha, E->pcd.normdt,
+                        E->pcd.Adt, E->pcd.Bdt, E->pcd.tau_d, E->pcd.g};
   for (int i = 0; i < p->n_chains; ++i) {
-    if (p->mode == 0) E->cf[i].nk = E->nk_chain[i]; else E->cd[i].nk = E->nk_chain[i];
+    if (p->mode != 1) E->cf[i].nk = E->nk_chain[i]; else E->cd[i].nk = E->nk_chain[i];
   }
   return E;
 }
@@ -969,7 +1313,7 @@ int orc_init_equilibrium(void* h, int nthreads) {
   const int n = E->P.n_chains;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
   for (int i = 0; i < n; ++i) {
-    if (E->P.mode == 0) init_chain(*E, E->cf[i], (uint32_t)i);
+    if (E->P.mode != 1) init_chain(*E, E->cf[i], (uint32_t)i);
     else init_chain(*E, E->cd[i], (uint32_t)i);
   }
   if (E->P.mode == 0) {
@@ -995,7 +1339,7 @@ int orc_init_equilibrium(void* h, int nthreads) {
 int orc_set_state(void* h, const int32_t* Z, const float* QN, const float* tau, const int64_t* T,
                   const uint64_t* step, const float* dt_prev, const int32_t* stall, const int32_t* S) {
   Ensemble* E = (Ensemble*)h;
-  if (E->P.mode != 0) return -3;
+  if (E->P.mode == 1) return -3;
   const int cap = E->z_max;
   for (int i = 0; i < E->P.n_chains; ++i) {
     Chain<float>& c = E->cf[i];
@@ -1016,8 +1360,12 @@ int orc_set_state(void* h, const int32_t* Z, const float* QN, const float* tau, 
     c.S = S ? S[i] : E->s0;
     c.hash = 0xCBF29CE484222325ull;
     c.k_next = 0;
+    c.tf = 0.0f;
+    c.halted = false;
+    c.r1[0] = c.r1[1] = c.r1[2] = 0.0f;
     corr_alloc(*E, c);
   }
+  E->block_time = 0.0;
   return 0;
 }
 
@@ -1026,7 +1374,7 @@ int orc_get_state(void* h, int32_t* Z, float* QN, float* tau, int64_t* T, uint64
   Ensemble* E = (Ensemble*)h;
   const int cap = E->z_max;
   for (int i = 0; i < E->P.n_chains; ++i) {
-    if (E->P.mode == 0) {
+    if (E->P.mode != 1) {
       const Chain<float>& c = E->cf[i];
       if (Z) Z[i] = c.Z;
       if (QN) for (int s = 0; s < cap; ++s) {
@@ -1065,6 +1413,7 @@ int orc_get_state(void* h, int32_t* Z, float* QN, float* tau, int64_t* T, uint64
 // Returns the number of kMC events done.
 int64_t orc_run(void* h, double t_end, int64_t step_limit, int nthreads) {
   Ensemble* E = (Ensemble*)h;
+  if (E->P.mode == 2) return run_ref(*E, t_end, step_limit, nthreads);
   const int n = E->P.n_chains;
   int64_t total = 0;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : total) num_threads(nthreads > 0 ? nthreads : 1)
@@ -1095,7 +1444,7 @@ int orc_stress(void* h, double* out, int32_t* count) {
       }
       s[7] = c.Z;
     };
-    if (E->P.mode == 0) sum(E->cf[i]); else sum(E->cd[i]);
+    if (E->P.mode != 1) sum(E->cf[i]); else sum(E->cd[i]);
     if (stall != 0 || s[0] != s[0]) continue;
     for (int q = 0; q < 8; ++q) acc[q] += s[q];
     ++cnt;
@@ -1124,7 +1473,7 @@ int orc_gt(void* h, double* gsum, int64_t* count) {
           if (count && i == 0) count[k * p + j] = n;
         }
     };
-    if (E->P.mode == 0) add(E->cf[i]); else add(E->cd[i]);
+    if (E->P.mode != 1) add(E->cf[i]); else add(E->cd[i]);
   }
   return 0;
 }
@@ -1188,12 +1537,37 @@ int orc_corr_series(int type, int p, int m, int levels, int64_t n, const double*
 int orc_get_r1(void* h, double* r1) {
   Ensemble* E = (Ensemble*)h;
   for (int i = 0; i < E->P.n_chains; ++i) {
-    if (E->P.mode == 0) {
+    if (E->P.mode != 1) {
       for (int q = 0; q < 3; ++q) r1[3 * i + q] = E->cf[i].r1[q];
     } else {
       for (int q = 0; q < 3; ++q) r1[3 * i + q] = E->cd[i].r1[q];
     }
   }
+  return 0;
+}
+
+// Mode 2: FP32 clocks since the window start, sample counters, R1 (n x 3).
+int orc_get_ref(void* h, float* tf, int32_t* corr_k, float* r1) {
+  Ensemble* E = (Ensemble*)h;
+  if (E->P.mode == 1) return -3;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    const Chain<float>& c = E->cf[i];
+    if (tf) tf[i] = c.tf;
+    if (corr_k) corr_k[i] = (int32_t)c.k_next;
+    if (r1) for (int q = 0; q < 3; ++q) r1[3 * i + q] = c.r1[q];
+  }
+  return 0;
+}
+
+// Parameters the compiled reference kernels need to run this ensemble: the
+// CD creation prefactor and the lifetime-law constants of the random stream
+// (c1, At, tau0, alpha, normdt, Adt, Bdt, tau_d, g).
+int orc_ref_params(void* h, float* prefact, double* law) {
+  Ensemble* E = (Ensemble*)h;
+  *prefact = E->prefact;
+  const double v[9] = {E->law.c1, E->law.At, E->law.tau0, E->law.alpha, E->law.normdt,
+                       E->law.Adt, E->law.Bdt, E->law.tau_d, E->law.g};
+  for (int q = 0; q < 9; ++q) law[q] = v[q];
   return 0;
 }
 

@@ -1,9 +1,11 @@
 """ORACLE — test infrastructure only.
 
 ctypes binding of ``oracle/liboracle.so`` (the CPU restatement of the
-reference DSM kMC path, see dsm_oracle.cpp) and of ``oracle/_ref/libdsmref.so``
+reference DSM kMC path, see dsm_oracle.cpp), of ``oracle/_ref/libdsmref.so``
 (the reference's own host initialiser and p_cd, compiled from the reference
-tree).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline /
+tree) and of ``oracle/_ref/libdsmrefstep.so`` (the reference's kMC kernels
+compiled unchanged for the host, driven by ref_step.cpp).  The reference tree is
+found at $GPU_DSM_REFERENCE (default /root/reference).  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline /
 reference legs use this module, as the checker or the timed CPU restatement.
 """
 from __future__ import annotations
@@ -19,7 +21,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REFLIB = HERE / "_ref" / "libdsmref.so"
-REFSRC = Path("/root/reference/common")
+REFSTEPLIB = HERE / "_ref" / "libdsmrefstep.so"
+REFSRC = Path(os.environ.get("GPU_DSM_REFERENCE", "/root/reference")) / "common"
 
 
 class OrcParams(C.Structure):
@@ -39,7 +42,7 @@ def build(ref: bool = False) -> None:
     """make liboracle.so (and _ref/libdsmref.so when the reference tree exists)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
     if ref and REFSRC.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"GPU_DSM_REFERENCE={REFSRC.parent}"], check=True)
 
 
 _lib = None
@@ -69,6 +72,8 @@ def lib() -> C.CDLL:
         L.orc_num_threads.restype = C.c_int
         L.orc_corr_series.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp]
         L.orc_get_r1.argtypes = [vp, vp]
+        L.orc_get_ref.argtypes = [vp, vp, vp, vp]
+        L.orc_ref_params.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -85,7 +90,10 @@ def corr_levels_for(t_end: float, dt: float, p: int, m: int) -> int:
 
 class Oracle:
     """One ensemble on the CPU.  mode 0 = FP32 mirror of the GPU arithmetic,
-    mode 1 = FP64 literal transcription."""
+    mode 1 = FP64 literal transcription, mode 2 = the reference's own
+    arithmetic (FP32 rates, running-sum scan, FP32 window clocks).  In mode 2
+    ``run(t_end, step_limit)`` follows the reference's step loops: t_end is the
+    absolute time to reach, step_limit an absolute event count."""
 
     def __init__(self, *, beta=1.0, nk, n_chains, z_max=0, cd_flag=1, kappa=(0.0,) * 9, mode=0, seed=1,
                  stream=0, corr=False, corr_p=64, corr_m=8, corr_levels=0, sync_dt=1.0, t_end=0.0,
@@ -176,6 +184,21 @@ class Oracle:
         lib().orc_get_r1(self._h, _p(out))
         return out
 
+    def ref_clock(self):
+        """Mode 2: FP32 time since the window start, sample counters, R1."""
+        tf = np.zeros(self.n, np.float32)
+        k = np.zeros(self.n, np.int32)
+        r1 = np.zeros((self.n, 3), np.float32)
+        assert lib().orc_get_ref(self._h, _p(tf), _p(k), _p(r1)) == 0
+        return tf, k, r1
+
+    def ref_params(self):
+        """CD creation prefactor and lifetime-law constants (ref_tape.h order)."""
+        pf = np.zeros(1, np.float32)
+        law = np.zeros(9, np.float64)
+        lib().orc_ref_params(self._h, _p(pf), _p(law))
+        return float(pf[0]), law
+
     def gt_raw(self):
         L, p = self.p.corr_levels, self.p.corr_p
         g = np.zeros(L * p, np.float64)
@@ -234,6 +257,116 @@ def ref_lib() -> Optional[C.CDLL]:
         R.ref_tau_samples.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref = R
     return _ref
+
+
+class RefParams(C.Structure):
+    _fields_ = [
+        ("n_chains", C.c_int32), ("nk", C.c_int32), ("z_max", C.c_int32), ("cd_flag", C.c_int32),
+        ("beta", C.c_float), ("prefact", C.c_float), ("kappa", C.c_float * 9), ("eq", C.c_int32),
+        ("corr_type", C.c_int32), ("corr_p", C.c_int32), ("corr_m", C.c_int32), ("corr_levels", C.c_int32),
+        ("corr_res", C.c_int32), ("seed", C.c_uint64), ("stream", C.c_uint32), ("chain_offset", C.c_uint32),
+        ("law", C.c_double * 9),
+    ]
+
+
+_refstep = None
+
+
+def refstep_lib() -> Optional[C.CDLL]:
+    """The reference's kMC kernels compiled for the host (None without the reference tree)."""
+    global _refstep
+    if _refstep is None:
+        if not REFSTEPLIB.exists():
+            if REFSRC.exists():
+                build(ref=True)
+            else:
+                return None
+        R = C.CDLL(str(REFSTEPLIB))
+        vp = C.c_void_p
+        R.ref_create.argtypes = [C.POINTER(RefParams)]
+        R.ref_create.restype = vp
+        R.ref_destroy.argtypes = [vp]
+        R.ref_set_chains.argtypes = [vp] * 5
+        R.ref_run.argtypes = [vp, C.c_double, C.c_int64]
+        R.ref_get_chains.argtypes = [vp] * 9
+        R.ref_stress.argtypes = [vp, vp, vp]
+        R.ref_gt.argtypes = [vp, vp, vp, vp]
+        _refstep = R
+    return _refstep
+
+
+class RefStep:
+    """One call block of the reference's own kMC kernels (common/ensemble_kernel.cu,
+    common/eq_ensemble_kernel.cu) run on the host by oracle/ref_step.cpp, fed
+    the random stream of ``like`` (a mode-2 Oracle of the same ensemble).
+    Equilibrium runs always carry the reference's correlator (sample interval
+    ``corr_res``)."""
+
+    def __init__(self, like: "Oracle", *, corr_res: int = 1):
+        R = refstep_lib()
+        assert R is not None, "reference tree not available"
+        o = like.p
+        pf, law = like.ref_params()
+        p = RefParams()
+        p.n_chains, p.nk, p.z_max, p.cd_flag = o.n_chains, o.nk, o.z_max, o.cd_flag
+        p.beta, p.prefact = o.beta, pf
+        for i in range(9):
+            p.kappa[i] = o.kappa[i]
+        flow = any(o.kappa[i] != 0.0 for i in range(9))
+        p.eq = 0 if flow else 1
+        p.corr_type = max(o.corr_type, 0)
+        p.corr_p, p.corr_m, p.corr_levels = o.corr_p, o.corr_m, o.corr_levels
+        p.corr_res = int(corr_res)
+        p.seed, p.stream, p.chain_offset = o.seed, o.stream, o.chain_offset
+        for i in range(9):
+            p.law[i] = law[i]
+        self.p = p
+        self.n, self.cap = o.n_chains, o.z_max
+        self._h = R.ref_create(C.byref(p))
+
+    def close(self):
+        if self._h:
+            refstep_lib().ref_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_chains(self, Z, QN, tau, R1=None):
+        a = lambda x, t: None if x is None else np.ascontiguousarray(x, dtype=t)
+        Z, QN, tau, R1 = a(Z, np.int32), a(QN, np.float32), a(tau, np.float32), a(R1, np.float32)
+        assert refstep_lib().ref_set_chains(self._h, _p(Z), _p(QN), _p(tau), _p(R1)) == 0
+
+    def run(self, reach_time: float, event_limit: int = -1) -> int:
+        """Returns 0, or the code of the first out-of-range surface access."""
+        return int(refstep_lib().ref_run(self._h, float(reach_time), int(event_limit)))
+
+    def get_state(self) -> dict:
+        n, cap = self.n, self.cap
+        d = {"Z": np.zeros(n, np.int32), "QN": np.zeros((n, cap, 4), np.float32), "tau": np.zeros((n, cap), np.float32),
+             "time": np.zeros(n, np.float32), "stall": np.zeros(n, np.int32), "events": np.zeros(n, np.int64),
+             "R1": np.zeros((n, 4), np.float32), "corr_time": np.zeros(n, np.int32)}
+        refstep_lib().ref_get_chains(self._h, _p(d["Z"]), _p(d["QN"]), _p(d["tau"]), _p(d["time"]), _p(d["stall"]),
+                                     _p(d["events"]), _p(d["R1"]), _p(d["corr_time"]))
+        return d
+
+    def stress(self):
+        out = np.zeros(8, np.float64)
+        cnt = np.zeros(1, np.int32)
+        assert refstep_lib().ref_stress(self._h, _p(out), _p(cnt)) == 0
+        return out, int(cnt[0])
+
+    def gt(self):
+        """corr_function_calc_kernel's ensemble sums (levels x p, float) and lags."""
+        L, p = self.p.corr_levels, self.p.corr_p
+        corr = np.zeros(L * p, np.float32)
+        lag = np.zeros(L * p, np.float32)
+        n0 = np.zeros(L * p, np.float32)
+        refstep_lib().ref_gt(self._h, _p(corr), _p(lag), _p(n0))
+        return corr.reshape(L, p), lag.reshape(L, p), n0.reshape(L, p)
 
 
 def corr_series(series: np.ndarray, p: int, m: int, levels: int, kind: int = 0):

@@ -17,6 +17,13 @@ Outputs (small JSON files, committed):
                         from oracle/_ref/ref_gex (a separate process: the
                         reference reads uninitialised memory at the end of the
                         CD-weighted inversion, see oracle/ref_gex_main.cpp)
+  ref_step_reference.npz  chains advanced by the reference's own kMC kernels
+                        (common/ensemble_kernel.cu, common/eq_ensemble_kernel.cu
+                        compiled for the host, oracle/_ref/libdsmrefstep.so) on
+                        the random stream of oracle/ref_tape.h: initial and final
+                        chains, FP32 clocks, event counts and G(t) sums, for the
+                        equilibrium and flow kernels (written on x86_64 glibc,
+                        whose expf/powf both sides use)
 """
 from __future__ import annotations
 
@@ -105,7 +112,36 @@ def main():
     (HERE / "gex_reference.json").write_text(json.dumps({"source": "common/gamma.cpp:174-263 (compiled)",
                                                          "rows": gex}))
     (HERE / "tau_reference.json").write_text(json.dumps({"source": "common/pcd_tau.h:67-82 (compiled)", "rows": tq}, indent=1))
+    ref_step_fixture()
     print("golden fixtures written to", HERE)
+
+
+def ref_step_fixture():
+    """Reference-kernel trajectories (see the module docstring)."""
+    xy = (0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    cases = {"eq_nk25_events": dict(nk=25, n=32, seed=11, kappa=(0.0,) * 9, t_end=1000.0, limit=1500),
+             "eq_nk25_time": dict(nk=25, n=16, seed=12, kappa=(0.0,) * 9, t_end=120.0, limit=-1),
+             "eq_nk200_events": dict(nk=200, n=4, seed=13, kappa=(0.0,) * 9, t_end=1000.0, limit=2000),
+             "flow_nk50_events": dict(nk=50, n=16, seed=14, kappa=xy, t_end=1000.0, limit=1000)}
+    out = {"cases": np.array(list(cases))}
+    for name, c in cases.items():
+        flow = any(c["kappa"])
+        o = orc.Oracle(nk=c["nk"], n_chains=c["n"], mode=2, seed=c["seed"], kappa=c["kappa"], corr=not flow,
+                       sync_dt=1.0, t_end=c["t_end"], corr_p=16, corr_m=2)
+        o.init_equilibrium()
+        st = o.get_state()
+        r = orc.RefStep(o, corr_res=1)
+        r.set_chains(st["Z"], st["QN"], st["tau"])
+        assert r.run(c["t_end"], c["limit"]) == 0
+        b = r.get_state()
+        g = {"nk": c["nk"], "n": c["n"], "seed": c["seed"], "kappa": np.array(c["kappa"], np.float32),
+             "t_end": c["t_end"], "limit": c["limit"], "Z0": st["Z"], "QN0": st["QN"], "tau0": st["tau"],
+             "Z": b["Z"], "QN": b["QN"], "time": b["time"], "events": b["events"]}
+        if not flow:
+            g["G"] = r.gt()[0]
+        for k, v in g.items():
+            out[f"{name}/{k}"] = np.asarray(v)
+    np.savez_compressed(HERE / "ref_step_reference.npz", **out)
 
 
 if __name__ == "__main__":
