@@ -86,7 +86,9 @@ typedef struct orc_params {
   int32_t pad2_;
   double gex_prefact;    // CD creation prefactor of the background law (ensemble.cu:137-146)
   uint32_t chain_offset; // global id of chain 0 (Philox keyed by global chain id)
-  int32_t pad3_;
+  int32_t partner_n;     // > 0: per-chain N_K of the whole ensemble that partners are drawn
+  const int32_t* partner_nk;  // from, and the CD prefactor averaged over, when these chains
+                              // are a slice of a larger polydisperse ensemble
 } orc_params;
 }
 
@@ -268,6 +270,7 @@ struct Chain {
 struct Ensemble {
   orc_params P{};
   std::vector<int32_t> nk_chain;
+  std::vector<int32_t> partner;  // polydisperse partner list (default: nk_chain)
   PCD pcd{};                    // monodisperse / prefactor source
   std::vector<PCD> pcd_by_nk;   // polydisperse partner laws (index = NK)
   float prefact = 0.f;          // CD creation prefactor (ensemble.cu:136-148)
@@ -352,8 +355,8 @@ static inline PCD partner_pcd(const Ensemble& E, uint32_t w, bool cd_created) {
     return make_pcd(E.P.beta, mw * (double)E.P.gex_scale);
   }
   if (!E.poly) return E.pcd;
-  const uint32_t idx = (uint32_t)(((uint64_t)w * (uint64_t)E.P.n_chains) >> 32);
-  return E.pcd_by_nk[E.nk_chain[idx]];
+  const uint32_t idx = (uint32_t)(((uint64_t)w * (uint64_t)E.partner.size()) >> 32);
+  return E.pcd_by_nk[E.partner[idx]];
 }
 
 template <class R>
@@ -1275,6 +1278,9 @@ void* orc_create(const orc_params* p) {
   E->nk_chain.assign(p->n_chains, p->nk);
   if (E->poly) for (int i = 0; i < p->n_chains; ++i) E->nk_chain[i] = p->nk_chain[i];
   E->P.nk_chain = nullptr;
+  if (E->poly && p->partner_nk && p->partner_n > 0) E->partner.assign(p->partner_nk, p->partner_nk + p->partner_n);
+  else E->partner = E->nk_chain;
+  E->P.partner_nk = nullptr;
   const float be_f = (float)p->beta;
   E->P.beta = (double)be_f;
   int nkmax = 0;
@@ -1282,12 +1288,14 @@ void* orc_create(const orc_params* p) {
   if (E->poly) {
     // CD creation prefactor = <normdt>/beta over the partner law
     // (role of ensemble.cu:137-146)
-    E->pcd_by_nk.assign(nkmax + 1, PCD{});
-    std::vector<char> seen(nkmax + 1, 0);
-    for (int v : E->nk_chain) if (!seen[v]) { seen[v] = 1; E->pcd_by_nk[v] = make_pcd(E->P.beta, v); }
+    int pmax = nkmax;
+    for (int v : E->partner) pmax = std::max(pmax, v);
+    E->pcd_by_nk.assign(pmax + 1, PCD{});
+    std::vector<char> seen(pmax + 1, 0);
+    for (int v : E->partner) if (!seen[v]) { seen[v] = 1; E->pcd_by_nk[v] = make_pcd(E->P.beta, v); }
     double s = 0;
-    for (int v : E->nk_chain) s += E->pcd_by_nk[v].normdt;
-    E->prefact = (float)((s / p->n_chains) / E->P.beta);
+    for (int v : E->partner) s += E->pcd_by_nk[v].normdt;
+    E->prefact = (float)((s / (double)E->partner.size()) / E->P.beta);
     E->pcd = make_pcd(E->P.beta, p->nk);
   } else {
     E->pcd = make_pcd(E->P.beta, p->nk);
@@ -1474,6 +1482,27 @@ int orc_gt(void* h, double* gsum, int64_t* count) {
         }
     };
     if (E->P.mode != 1) add(E->cf[i]); else add(E->cd[i]);
+  }
+  return 0;
+}
+
+// Per-chain correlator output: out[(i*L + k)*p + j] = acc/count of chain i
+// (0 where the lag has no entries), for error bars of the ensemble average.
+int orc_gt_chains(void* h, double* out) {
+  Ensemble* E = (Ensemble*)h;
+  if (E->P.corr_type < 0) return -3;
+  const int L = E->P.corr_levels, p = E->P.corr_p;
+  for (int i = 0; i < E->P.n_chains; ++i) {
+    auto put = [&](auto& c) {
+      for (int k = 0; k < L; ++k)
+        for (int j = 0; j < p; ++j) {
+          const int64_t n = c.cnins[k] - j;
+          double v = 0.0;
+          if (n > 0 && !(k > 0 && j < p / E->P.corr_m)) v = c.cacc[(size_t)k * p + j] / (double)n;
+          out[((size_t)i * L + k) * p + j] = v;
+        }
+    };
+    if (E->P.mode != 1) put(E->cf[i]); else put(E->cd[i]);
   }
   return 0;
 }

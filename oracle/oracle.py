@@ -34,7 +34,8 @@ class OrcParams(C.Structure):
         ("nk_chain", C.c_void_p), ("s0", C.c_int32), ("gex", C.c_int32),
         ("gex_M", C.c_void_p), ("gex_Md", C.c_void_p), ("gex_n", C.c_int32), ("gex_nd", C.c_int32),
         ("gex_step", C.c_float), ("gex_step_d", C.c_float), ("gex_scale", C.c_float), ("pad2_", C.c_int32),
-        ("gex_prefact", C.c_double), ("chain_offset", C.c_uint32), ("pad3_", C.c_int32),
+        ("gex_prefact", C.c_double), ("chain_offset", C.c_uint32), ("partner_n", C.c_int32),
+        ("partner_nk", C.c_void_p),
     ]
 
 
@@ -74,6 +75,7 @@ def lib() -> C.CDLL:
         L.orc_get_r1.argtypes = [vp, vp]
         L.orc_get_ref.argtypes = [vp, vp, vp, vp]
         L.orc_ref_params.argtypes = [vp, vp, vp]
+        L.orc_gt_chains.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -98,7 +100,7 @@ class Oracle:
     def __init__(self, *, beta=1.0, nk, n_chains, z_max=0, cd_flag=1, kappa=(0.0,) * 9, mode=0, seed=1,
                  stream=0, corr=False, corr_p=64, corr_m=8, corr_levels=0, sync_dt=1.0, t_end=0.0,
                  nk_chain: Optional[np.ndarray] = None, s0=0, threads=0, msd=False, gex_tables=None,
-                 chain_offset=0):
+                 chain_offset=0, partner_nk: Optional[np.ndarray] = None):
         L = lib()
         p = OrcParams()
         p.beta = float(np.float32(beta))
@@ -123,6 +125,12 @@ class Oracle:
         p.nk_chain = None if self._nk_chain is None else self._nk_chain.ctypes.data
         p.s0 = s0
         p.chain_offset = chain_offset
+        # polydisperse slice of a larger ensemble: partners and the CD prefactor
+        # come from the whole ensemble's per-chain N_K
+        self._partner = None if partner_nk is None else np.ascontiguousarray(partner_nk, dtype=np.int32)
+        if self._partner is not None:
+            p.partner_nk = self._partner.ctypes.data
+            p.partner_n = len(self._partner)
         if gex_tables is not None:
             # GEX background: inverse tables and prefactor as the product builds them
             self._gex_M = np.ascontiguousarray(gex_tables["M"], np.float32)
@@ -183,6 +191,13 @@ class Oracle:
         out = np.zeros((self.n, 3), np.float64)
         lib().orc_get_r1(self._h, _p(out))
         return out
+
+    def gt_chains(self):
+        """Per-chain correlator averages acc/count (n, levels, p)."""
+        L, p = self.p.corr_levels, self.p.corr_p
+        out = np.zeros(self.n * L * p, np.float64)
+        assert lib().orc_gt_chains(self._h, _p(out)) == 0
+        return out.reshape(self.n, L, p)
 
     def ref_clock(self):
         """Mode 2: FP32 time since the window start, sample counters, R1."""
@@ -377,3 +392,26 @@ def corr_series(series: np.ndarray, p: int, m: int, levels: int, kind: int = 0):
     nins = np.zeros(levels, np.int64)
     lib().orc_corr_series(kind, p, m, levels, len(x), _p(x), _p(acc), _p(nins))
     return acc.reshape(levels, p), nins
+
+
+def gt_error_vs_fp64(g_test: np.ndarray, fp64: "Oracle", prec: float = 0.02) -> dict:
+    """Error of a G(t) (or MSD) estimate against the FP64 oracle run on the
+    same chains and random stream.  Both inputs are correlator sums of shape
+    (levels, p) normalised the same way; the FP64 ensemble's per-chain values
+    give the statistical error sigma of its mean at every lag.
+
+    rel_resolved: max |dG| / |G| over the lags the ensemble resolves to
+        ``prec`` statistical precision (sigma < prec |G|);
+    dev_sigma: max |dG| / sigma over all populated lags;
+    rel_scale: max |dG| / |G(lag 0)|."""
+    g_ref, cnt = fp64.gt_raw()
+    per = fp64.gt_chains()
+    n = per.shape[0]
+    sig = per.std(axis=0, ddof=1) * n / np.sqrt(n)  # error of the sum over n chains
+    m = cnt > 0
+    d = np.abs(np.asarray(g_test, np.float64) - g_ref)
+    res = m & (sig < prec * np.abs(g_ref))
+    return {"rel_resolved": float((d[res] / np.abs(g_ref[res])).max()) if res.any() else None,
+            "resolved_lags": int(res.sum()), "lags": int(m.sum()), "precision": prec,
+            "dev_sigma": float((d[m] / np.maximum(sig[m], 1e-300)).max()),
+            "rel_scale": float(d[m].max() / abs(g_ref[0, 0]))}
