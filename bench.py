@@ -16,7 +16,12 @@ Also reported:
                 L_eq(Z) = 2(Z-1) + 152 against 152 SMs x 128 lanes x f_max
   cpu_baseline  the oracle (CPU restatement of the reference path) on the
                 host cores, bounded sample of the same workload
+  gt_err_vs_fp64  the CPU leg also checks the GPU's results against the FP64
+                transcription of the reference path (oracle mode 1) on the same
+                chains and random streams: G(t) of 512 chains of the headline
+                ensemble, sigma_xy of shear samples, G(t) of served requests
   --impl reference  times that CPU restatement as the reference arm
+  --gpus N      without a torchrun environment, starts N ranks itself
 """
 from __future__ import annotations
 
@@ -173,6 +178,113 @@ def profile_traffic() -> dict:
     return json.loads(p.read_text()) if p.exists() else {}
 
 
+def fp64_accuracy(args, device: int, shear: dict | None, serve: dict | None) -> dict:
+    """Part of the CPU leg: the FP64 transcription (oracle mode 1) on chains the
+    GPU also runs, with the same random streams (Philox keyed by chain and
+    event), compared with the GPU's results against the FP64 estimate's own
+    chain-to-chain error (oracle.gt_error_vs_fp64):
+      headline  G(t) of chains 30000-30511 of the headline ensemble over 500 tau_K;
+      shear     sigma_xy of 256 chains at Wi 10 and 100 (N_K=100) at five
+                outputs, deviation in units of sigma;
+      serve     G(t) of the two cheapest G(t) requests of the served stream,
+                re-run on the CPU with the request's parameters."""
+    import gpu_dsm_gb300 as dsm
+    from oracle import oracle as orc
+
+    out = {}
+    kw = dict(nk=NK, n_chains=512, beta=BETA, sync_dt=SAMPLE_DT, t_end=T_END_RUN, corr_p=CORR_P, corr_m=CORR_M,
+              seed=1, chain_offset=30000)
+    g = dsm.Ensemble(eq_type=1, device=device, **kw)
+    f = orc.Oracle(corr=True, mode=1, **kw)
+    g.init_equilibrium()
+    f.init_equilibrium()
+    g.advance(500.0)
+    f.run(500.0)
+    out["headline"] = {**orc.gt_error_vs_fp64(g.gt_raw()[0], f),
+                       "sample": "chains 30000-30511 of the headline ensemble, 500 tau_K, G(t) sums"}
+    g.close()
+    if shear is not None and "failed" not in shear:
+        tau_d = dsm.pcd(1.0, 100)["tau_d"]
+        rows = []
+        for wi in (10.0, 100.0):
+            kap = (0.0, wi / tau_d, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+            skw = dict(nk=100, n_chains=256, kappa=kap, seed=4, stream=3)
+            ge = dsm.Ensemble(sync_dt=100.0, t_end=5.0e5, device=device, **skw)
+            fe = orc.Oracle(mode=1, **skw)
+            ge.init_equilibrium()
+            fe.init_equilibrium()
+            worst = 0.0
+            for w in range(1, 6):
+                ge.advance(100.0 * w)
+                fe.run(100.0 * w)
+                sg = ge.stress()[0][3]
+                sf = fe.stress()[0][3]
+                st = fe.get_state()
+                q = st["QN"].astype(np.float64)
+                idx = np.arange(q.shape[1])[None, :] < st["Z"][:, None]
+                per = -3.0 * np.where(idx, q[:, :, 0] * q[:, :, 1] / np.where(idx, q[:, :, 3], 1.0), 0.0).sum(axis=1)
+                worst = max(worst, abs(sg - sf) / (per.std(ddof=1) / math.sqrt(len(per))))
+            ge.close()
+            rows.append({"wi": wi, "dev_sigma": worst})
+        shear["stress_err_vs_fp64"] = {"rows": rows, "sample": "256 chains, N_K=100, outputs every 100 tau_K "
+                                       "to 500 tau_K; |sigma_xy(GPU) - sigma_xy(FP64)| / sigma of the FP64 "
+                                       "estimate; consistent when below 3 sqrt(2)"}
+        out["shear"] = shear["stress_err_vs_fp64"]
+    if serve is not None and serve.get("_samples"):
+        rows = []
+        for r, gp in serve.pop("_samples"):
+            fo = orc.Oracle(nk=r["nk"], n_chains=r["n_chains"], beta=r["beta"], seed=r["seed"], stream=r["stream"],
+                            corr=True, sync_dt=r["sync_dt"], t_end=r["t_end"], corr_p=r["corr_p"],
+                            corr_m=r["corr_m"], mode=1)
+            fo.init_equilibrium()
+            fo.run(r["t_end"])
+            rows.append({**orc.gt_points_error_vs_fp64(gp, fo),
+                         "request": {k: r[k] for k in ("nk", "beta", "n_chains", "t_end")}})
+        serve["gt_err_vs_fp64"] = rows
+        out["serve"] = rows
+    return out
+
+
+def latency_probe(args, device: int, f_hz: float, tiles_per_sm: int, value: float) -> dict:
+    """Latency model of the step kernel: 304 chains of the headline workload
+    run as one warp (two 16-lane chain tiles) per block, so that each SM holds
+    a single warp; their events per second give the critical-path cycles per
+    event of a chain that waits for nothing but its own dependencies.  The
+    bound is every resident chain tile of the headline schedule running at that
+    speed; frac = achieved / bound."""
+    import gpu_dsm_gb300 as dsm
+
+    n = 2 * 152
+    e = dsm.Ensemble(beta=BETA, nk=NK, n_chains=n, eq_type=1, sync_dt=SAMPLE_DT, t_end=T_END_RUN, seed=9,
+                     device=device, corr_p=CORR_P, corr_m=CORR_M, lanes_per_chain=16, warps_per_block=1)
+    e.init_equilibrium()
+    e.advance(50.0)
+    ev = e.advance(2050.0)
+    lw = e.last_window()
+    e.close()
+    rate = ev / (lw["kernel_ms"] / 1e3)
+    cyc = f_hz * n / rate
+    bound = 152 * tiles_per_sm * f_hz / cyc
+    return {"critical_path_cycles_per_event": cyc, "probe": f"{n} chains, 1 warp (2 chain tiles) per SM, "
+            f"{ev} events, {lw['grid']} blocks", "resident_chain_tiles_per_sm": tiles_per_sm,
+            "achieved": value / 1e9, "peak": bound / 1e9, "unit": "Gevents/s", "frac": value / bound,
+            "cycles_per_event_at_load": 152 * tiles_per_sm * f_hz / value,
+            "note": "peak = 152 SMs x resident chain tiles x clock / critical-path cycles per event"}
+
+
+def spawn_ranks(args) -> int:
+    """--gpus N outside torchrun: start N ranks with torch.distributed.run on
+    127.0.0.1 (one process per GPU) and pass rank 0's JSON line through."""
+    import socket
+
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"), *sys.argv[1:]]
+    return subprocess.run(cmd).returncode
+
+
 def run_gpu(args):
     import torch
     import gpu_dsm_gb300 as dsm
@@ -181,10 +293,16 @@ def run_gpu(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus:
+        raise SystemExit(f"bench: --gpus {args.gpus} but WORLD_SIZE={world}")
+    comm = {"backend": None, "world_size": 1}
     if world > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+        comm = {"backend": dist.get_backend(), "world_size": dist.get_world_size()}
+        if comm["world_size"] != args.gpus:
+            raise SystemExit(f"bench: NCCL communicator of {comm['world_size']} ranks, --gpus {args.gpus}")
     if rank == 0:
         native.build()
     if world > 1:
@@ -331,6 +449,14 @@ def run_gpu(args):
                                    "per_unit": f"{ipe:g} warp-instructions per kMC event (ncu)",
                                    "note": "of measured clock"}
 
+    if rank == 0 and not args.no_latency:
+        try:
+            tiles = int(lw["blocks_per_sm"]) * (128 // max(16, int(sched[0]["lanes"]) if sched else 16))
+            roof["latency_secondary"] = latency_probe(args, local, float(clocks.get("sm_mhz") or 2070.0) * 1e6,
+                                                      tiles, value / world)
+        except Exception as e:  # reported, never silently replaced
+            roof["latency_secondary"] = {"failed": repr(e)}
+
     if rank != 0:
         ens.close()
         torch.distributed.destroy_process_group()
@@ -354,17 +480,26 @@ def run_gpu(args):
         except Exception as e:  # reported, never silently replaced
             serve = {"failed": repr(e)}
     cpu = None
+    acc = None
     if not args.no_cpu:
         try:
             cpu, _ = cpu_sample(args.cpu_seconds)
         except Exception as e:  # the baseline is reported, never a fallback
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+        if world == 1:
+            try:
+                acc = fp64_accuracy(args, local, shear, serve)
+            except Exception as e:  # reported, never silently replaced
+                acc = {"failed": repr(e)}
+    if isinstance(serve, dict):
+        serve.pop("_samples", None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": kms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic equilibrium melt",
             "config": config(args.window, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clocks, "gpu_launches": args.steps * launches_per_step, "shear": shear, "poly": poly,
-            "serve": serve,
+            "serve": serve, "gt_err_vs_fp64": (acc or {}).get("headline", acc),
+            "comm": comm,
             "detail": {"events": events_all, "wall_s": wall, "kernel_ms_total": kms, "mean_Z": zmean,
                        "sharded_gt_points": gt_points,
                        "grid": lw["grid"], "blocks_per_sm": lw["blocks_per_sm"], "schedule": sched}}
@@ -555,6 +690,9 @@ def run_serve(args, device: int = 0) -> dict:
     for r, a, b in zip(reqs, out_s, out_p):
         if r.get("eq_type") == 1 and len(a) and len(b):
             err = max(err, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30)))
+    # the two cheapest G(t) requests, for the CPU leg's check against the FP64 oracle
+    cheap = sorted((prior_events(r) * r["nk"], i) for i, r in enumerate(reqs)
+                   if r.get("eq_type") == 1 and len(out_s[i]))[:2]
     return {"requests": len(reqs), "t_end_scale": args.serve_scale, "arrival_rate_per_s": lam,
             "offered_load_vs_plain": 1.2, "chunk_s": args.serve_chunk, "served": served, "plain": plain,
             "other_policies": others,
@@ -564,6 +702,7 @@ def run_serve(args, device: int = 0) -> dict:
             "p99_speedup": plain["p99_s"] / served["p99_s"], "p50_speedup": plain["p50_s"] / served["p50_s"],
             "throughput_ratio": served["events_per_s"] / plain["events_per_s"],
             "gt_max_rel_diff_served_vs_plain": err,
+            "_samples": [(reqs[i], out_s[i]) for _, i in cheap],
             "stream": "Poisson arrivals (seed 11); N_K log-uniform [20,500], beta {0.5,1,2}, 1024-65536 chains, "
                       "50% G(t) / 50% shear Wi log-uniform [0.1,100], t_end log-uniform [1e4,1e6] x t_end_scale"}
 
@@ -575,7 +714,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--window", type=float, default=500.0, help="tau_K advanced per step")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--no-latency", action="store_true", help="skip the latency-model probe")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--chains", type=int, default=65536, help="chains per GPU (65536 = headline workload)")
@@ -583,7 +723,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-stream leg")
     ap.add_argument("--no-shear", action="store_true", help="skip the shear start-up leg")
     ap.add_argument("--shear-only", action="store_true", help="run only the shear start-up leg")
-    ap.add_argument("--shear-windows", type=int, default=2)
+    ap.add_argument("--shear-windows", type=int, default=6)
     ap.add_argument("--no-poly", action="store_true", help="skip the polydisperse leg")
     ap.add_argument("--poly-only", action="store_true", help="run only the polydisperse leg")
     ap.add_argument("--poly-chains", type=int, default=262144)
@@ -605,6 +745,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_ranks(args)
     if args.poly_only:
         from gpu_dsm_gb300 import build as native
         native.build()

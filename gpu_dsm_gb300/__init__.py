@@ -8,6 +8,7 @@ There is no CPU fallback: if the native library is missing, importing the
 simulator raises.
 """
 from .api import (  # noqa: F401
+    HEAD_DTYPE,
     DSMError,
     Ensemble,
     Server,
@@ -20,4 +21,4 @@ from .api import (  # noqa: F401
     pcd,
 )
 
-__all__ = ["DSMError", "Ensemble", "Server", "StressPlus", "advance_batch", "lib_path", "load_library", "make_params", "pcd", "gex_tables"]
+__all__ = ["HEAD_DTYPE", "DSMError", "Ensemble", "Server", "StressPlus", "advance_batch", "lib_path", "load_library", "make_params", "pcd", "gex_tables"]

@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-I", str(ROOT / "include")]
 SOURCES = ["dsm_kernels.cu", "dsm_host.cu", "dsm_compat.cu", "dsm_noalloc.cu", "dsm_serve.cu", "dsm_distr.cu", "dsm_gex.cpp",
-           "dsm_checkpoint.cu"]
+           "dsm_checkpoint.cu", "dsm_refapi.cu"]
 
 
 def nvcc() -> str:
@@ -54,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile libgpudsm.so and gpu_DSM if any source is newer than them."""
     BUILD.mkdir(exist_ok=True)
     nv = nvcc()
-    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "dsm.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     objs = []
     jobs = []
     for src in SOURCES:

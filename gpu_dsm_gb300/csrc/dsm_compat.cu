@@ -39,7 +39,7 @@ int read_input(const char* path, InputDat* in) {
 }
 
 // common/ensemble.cu:394-431, from the device histogram of N over all strands
-static void write_N_distr(const std::string& fn, const std::vector<uint64_t>& hist, bool cumulative) {
+void write_N_distr(const std::string& fn, const std::vector<uint64_t>& hist, bool cumulative) {
   std::ofstream f(fn);
   if (!f) { std::cout << "file error\n"; return; }
   int nmin = -1, nmax = -1;
@@ -56,7 +56,7 @@ static void write_N_distr(const std::string& fn, const std::vector<uint64_t>& hi
 }
 
 // common/ensemble.cu:356-392, from the device histogram of Z over chains
-static void write_Z_distr(const std::string& fn, const std::vector<uint64_t>& hist, int n_chains, bool cumulative) {
+void write_Z_distr(const std::string& fn, const std::vector<uint64_t>& hist, int n_chains, bool cumulative) {
   std::ofstream f(fn);
   if (!f) { std::cout << "file error\n"; return; }
   int zmin = -1, zmax = -1;
@@ -72,7 +72,7 @@ static void write_Z_distr(const std::string& fn, const std::vector<uint64_t>& hi
 
 // common/ensemble.cu:439-484: cumulative distribution of |Q| of the internal
 // strands, every 10th of the sorted lengths (sorted on the device)
-static void write_Q_distr(const std::string& fn, const std::vector<float>& Q) {
+void write_Q_distr(const std::string& fn, const std::vector<float>& Q) {
   std::ofstream f(fn);
   if (!f) { std::cout << "file error\n"; return; }
   const size_t n = Q.size();
@@ -108,6 +108,13 @@ int write_distributions(dsm_sim* sim, int n_chains, int cap, bool cd_flag) {
 using namespace dsmc;
 
 extern "C" int main_cuda(bool* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID, bool distr,
+                         int* progress_bar) {
+  return main_cuda_impl(run_flag, job_ID, savefile, loadfile, device_ID, distr, progress_bar);
+}
+
+// common/main_cuda.cu:34-185; exported as main_cuda with C linkage (above) and
+// with the reference GUI's C++ linkage (dsm_refapi.cu)
+int dsmc::main_cuda_impl(bool* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID, bool distr,
                          int* progress_bar) {
   if (job_ID != 0) {
     std::cout << "job_ID: " << job_ID << '\n';

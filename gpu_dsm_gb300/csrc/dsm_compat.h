@@ -1,6 +1,8 @@
 // Reference-compatible file formats and driver helpers (dsm_compat.cu).
 #pragma once
+#include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/dsm.h"
 
@@ -18,5 +20,12 @@ struct InputDat {
 std::string filename_ID(const std::string& name, int job_ID);
 int read_input(const char* path, InputDat* in);
 int write_distributions(dsm_sim* sim, int n_chains, int cap, bool cd_flag);
+// -distr file writers from histograms (common/ensemble.cu:356-484)
+void write_Z_distr(const std::string& fn, const std::vector<uint64_t>& hist, int n_chains, bool cumulative);
+void write_N_distr(const std::string& fn, const std::vector<uint64_t>& hist, bool cumulative);
+void write_Q_distr(const std::string& fn, const std::vector<float>& Q);
+// the reference driver main_cuda (common/main_cuda.cu:34-185)
+int main_cuda_impl(bool* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID, bool distr,
+                   int* progress_bar);
 
 }  // namespace dsmc

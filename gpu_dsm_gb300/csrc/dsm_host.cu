@@ -73,11 +73,16 @@ extern "C" int dsm_pcd(double beta, int32_t nk, double* out) {
 // in double, rounded to float.  x^0.75 = sqrt(x)*sqrt(sqrt(x)).
 static double pow075(double x) { return std::sqrt(x) * std::sqrt(std::sqrt(x)); }
 
-void dsm::make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off) {
+size_t dsm::table_floats(int nmax) {
+  const size_t n = (size_t)nmax + 2;
+  return 8 * n + (8 * n + 8) + n + 4;
+}
+
+void dsm::make_tables(int nmax, double beta_f, float prefact, float* buf, TableOffsets& off) {
   const size_t n = (size_t)nmax + 2;
   const size_t nf = 8 * n + 8;
   off.NT = 0; off.NE = 4 * n; off.FRIC = 8 * n; off.INV3N = 8 * n + nf;
-  buf.assign(off.INV3N + n + 4, 0.f);
+  std::memset(buf, 0, table_floats(nmax) * sizeof(float));
   for (size_t N = 1; N < n; ++N) {
     const double d = (double)N;
     float* nt = &buf[off.NT + 4 * N];
@@ -93,6 +98,11 @@ void dsm::make_tables(int nmax, double beta_f, float prefact, std::vector<float>
     buf[off.INV3N + N] = (float)(3.0 / d);
   }
   for (size_t i = 1; i < nf; ++i) buf[off.FRIC + i] = (float)(4.0 / (double)i);
+}
+
+void dsm::make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off) {
+  buf.assign(table_floats(nmax), 0.f);
+  make_tables(nmax, beta_f, prefact, buf.data(), off);
 }
 
 // ------------------------------------------------------------------ helpers
@@ -1237,9 +1247,12 @@ extern "C" int dsm_advance(dsm_sim* s, double t_end, int64_t step_limit, const v
 extern "C" int dsm_stress(dsm_sim* s, dsm_stress_plus* out, int32_t* count) {
   if (!s || !s->ready || !out) return DSM_ERR_INVALID;
   if (!s->flow) {
-    // equilibrium ensembles: evaluate the stress of the current state with a
-    // zero-length flow-free pass (same kernel path as a window end)
-    return fail(s, DSM_ERR_INVALID, "dsm_stress is defined for flow ensembles (kappa != 0)");
+    // equilibrium ensembles keep no per-chain stress: evaluate it from the
+    // current state, with the sums and the reduction of a flow window end
+    // (the per-chain buffer the flow kernel writes is free here)
+    if (s->pending) return fail(s, DSM_ERR_INVALID, "asynchronous work pending");
+    CK(launch_state_stress(s->d_ens, s->P.n_chains, s->d_stress, s->d_red, s->st));
+    CK(cudaMemcpyAsync(s->hw->red, s->d_red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
   }
   // sums of the last window end, copied back with its counters
   CK(cudaStreamSynchronize(s->st));
@@ -1405,113 +1418,125 @@ extern "C" int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end,
     CK(cudaMemcpyAsync(q->d_ens, &E, sizeof(EnsDev), cudaMemcpyHostToDevice, s->st));
     CK(cudaMemsetAsync(q->d_counters, 0, 4 * sizeof(unsigned long long), s->st));
   }
-  std::vector<void*> tmp;
-  int rc = DSM_OK;
   // groups run concurrently, each on the stream of its first ensemble, after
-  // the descriptor copies on s->st; s->st then waits for all of them
+  // the descriptor copies on s->st; s->st then waits for all of them.  Every
+  // exit of enqueue(), an error included, passes through the clean-up below:
+  // events destroyed, stream-ordered temporaries released once nothing that
+  // reads them can still run.
+  std::vector<void*> tmp;
+  std::vector<cudaStream_t> used;
   cudaEvent_t ready = nullptr;
   std::vector<cudaEvent_t> joins;
   const bool fan = groups.size() > 1;
-  if (fan) {
-    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-    CK(cudaEventRecord(ready, s->st));
-  }
-  for (auto& g : groups) {
-    const int k = (int)g.idx.size();
-    std::vector<EnsDev> hE(k);
-    std::vector<long long> pre(k + 1, 0);
-    LaunchCfg cfg{4, 0, 0, g.lanes};
-    cudaStream_t gs = fan ? sims[g.idx[0]]->st : s->st;
-    for (int q = 0; q < k; ++q) {
-      dsm_sim* x = sims[g.idx[q]];
-      hE[q] = x->h;
-      pre[q + 1] = pre[q] + x->P.n_chains;
-      cfg.slot_cap = std::max(cfg.slot_cap, x->cap);
-      if (g.corr) cfg.pmax = std::max(cfg.pmax, x->cp);
-    }
-    EnsDev* dE = nullptr;
-    long long* dP = nullptr;
-    unsigned int* dW = nullptr;
-    CK(cudaMallocAsync((void**)&dE, sizeof(EnsDev) * k, s->st));
-    tmp.push_back(dE);
-    CK(cudaMallocAsync((void**)&dP, sizeof(long long) * (k + 1) + 16, s->st));
-    tmp.push_back(dP);
-    dW = (unsigned int*)(dP + k + 1);
-    CK(cudaMemcpyAsync(dE, hE.data(), sizeof(EnsDev) * k, cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemcpyAsync(dP, pre.data(), sizeof(long long) * (k + 1), cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemsetAsync(dW, 0, 16, s->st));
-    int optin = 0;
-    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
-    // when every ensemble of the group planned a small-slot class (its own
-    // schedule), the group runs in the smallest of those slots and the chains
-    // that outgrow it finish in an overflow launch with slots of the group's
-    // largest capacity, as in dsm_advance; otherwise one launch with slots of
-    // that capacity
-    bool all_small = true;
-    int small = cfg.slot_cap;
-    for (int q = 0; q < k && all_small; ++q) {
-      const dsm_sim* x = sims[g.idx[q]];
-      // the small class is the last of an ensemble's classes
-      all_small = !x->classes.empty() && x->classes.back().cfg.lanes == g.lanes;
-      if (all_small) small = std::min(small, x->classes.back().cfg.slot_cap);
-    }
-    const bool overflow = all_small && small < cfg.slot_cap;
-    LaunchCfg run = cfg;
-    if (overflow) run.slot_cap = small;
-    fit_block(run, optin);
-    const int bps = step_max_blocks_per_sm(g.flow, g.corr, run);
-    if (bps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory"); break; }
-    const int tiles = run.warps_per_block * 32 / run.lanes;
-    const long long want = (pre[k] + tiles - 1) / tiles;
-    const int grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
-    StepList lst;
-    LaunchCfg oc{1, cfg.slot_cap, cfg.pmax, 32};
-    int ogrid = 0;
-    if (overflow) {
-      const int obps = step_max_blocks_per_sm(g.flow, g.corr, oc);
-      if (obps < 1) { rc = fail(s, DSM_ERR_INVALID, "batch capacity does not fit one shared-memory slot"); break; }
-      ogrid = obps * s->sm_count;
-      int* dDef = nullptr;
-      CK(cudaMallocAsync((void**)&dDef, sizeof(int) * (size_t)pre[k], s->st));
-      tmp.push_back(dDef);
-      lst.defer = dDef;
-      lst.n_defer = dW + 2;
-    }
+  auto enqueue = [&]() -> int {
     if (fan) {
+      CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
       CK(cudaEventRecord(ready, s->st));
-      CK(cudaStreamWaitEvent(gs, ready, 0));
     }
-    CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, run, nullptr, (int*)(dW + 1), grid, gs, lst));
-    if (overflow) {
-      StepList ol;
-      ol.order = lst.defer;
-      ol.dyn_total = dW + 2;
-      CK(launch_step(dE, k, dP, 0, dW + 3, g.flow, g.corr, oc, nullptr, (int*)(dW + 1), ogrid, gs, ol));
+    for (auto& g : groups) {
+      const int k = (int)g.idx.size();
+      std::vector<EnsDev> hE(k);
+      std::vector<long long> pre(k + 1, 0);
+      LaunchCfg cfg{4, 0, 0, g.lanes};
+      cudaStream_t gs = fan ? sims[g.idx[0]]->st : s->st;
+      for (int q = 0; q < k; ++q) {
+        dsm_sim* x = sims[g.idx[q]];
+        hE[q] = x->h;
+        pre[q + 1] = pre[q] + x->P.n_chains;
+        cfg.slot_cap = std::max(cfg.slot_cap, x->cap);
+        if (g.corr) cfg.pmax = std::max(cfg.pmax, x->cp);
+      }
+      EnsDev* dE = nullptr;
+      long long* dP = nullptr;
+      unsigned int* dW = nullptr;
+      CK(cudaMallocAsync((void**)&dE, sizeof(EnsDev) * k, s->st));
+      tmp.push_back(dE);
+      CK(cudaMallocAsync((void**)&dP, sizeof(long long) * (k + 1) + 16, s->st));
+      tmp.push_back(dP);
+      dW = (unsigned int*)(dP + k + 1);
+      CK(cudaMemcpyAsync(dE, hE.data(), sizeof(EnsDev) * k, cudaMemcpyHostToDevice, s->st));
+      CK(cudaMemcpyAsync(dP, pre.data(), sizeof(long long) * (k + 1), cudaMemcpyHostToDevice, s->st));
+      CK(cudaMemsetAsync(dW, 0, 16, s->st));
+      int optin = 0;
+      CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->P.device));
+      // when every ensemble of the group planned a small-slot class (its own
+      // schedule), the group runs in the smallest of those slots and the chains
+      // that outgrow it finish in an overflow launch with slots of the group's
+      // largest capacity, as in dsm_advance; otherwise one launch with slots of
+      // that capacity
+      bool all_small = true;
+      int small = cfg.slot_cap;
+      for (int q = 0; q < k && all_small; ++q) {
+        const dsm_sim* x = sims[g.idx[q]];
+        // the small class is the last of an ensemble's classes
+        all_small = !x->classes.empty() && x->classes.back().cfg.lanes == g.lanes;
+        if (all_small) small = std::min(small, x->classes.back().cfg.slot_cap);
+      }
+      const bool overflow = all_small && small < cfg.slot_cap;
+      LaunchCfg run = cfg;
+      if (overflow) run.slot_cap = small;
+      fit_block(run, optin);
+      const int bps = step_max_blocks_per_sm(g.flow, g.corr, run);
+      if (bps < 1) return fail(s, DSM_ERR_INVALID, "batch slot does not fit shared memory");
+      const int tiles = run.warps_per_block * 32 / run.lanes;
+      const long long want = (pre[k] + tiles - 1) / tiles;
+      const int grid = (int)std::min<long long>(want, (long long)bps * s->sm_count);
+      StepList lst;
+      LaunchCfg oc{1, cfg.slot_cap, cfg.pmax, 32};
+      int ogrid = 0;
+      if (overflow) {
+        const int obps = step_max_blocks_per_sm(g.flow, g.corr, oc);
+        if (obps < 1) return fail(s, DSM_ERR_INVALID, "batch capacity does not fit one shared-memory slot");
+        ogrid = obps * s->sm_count;
+        int* dDef = nullptr;
+        CK(cudaMallocAsync((void**)&dDef, sizeof(int) * (size_t)pre[k], s->st));
+        tmp.push_back(dDef);
+        lst.defer = dDef;
+        lst.n_defer = dW + 2;
+      }
+      if (fan) {
+        CK(cudaEventRecord(ready, s->st));
+        CK(cudaStreamWaitEvent(gs, ready, 0));
+      }
+      used.push_back(gs);
+      CK(launch_step(dE, k, dP, pre[k], dW, g.flow, g.corr, run, nullptr, (int*)(dW + 1), grid, gs, lst));
+      if (overflow) {
+        StepList ol;
+        ol.order = lst.defer;
+        ol.dyn_total = dW + 2;
+        CK(launch_step(dE, k, dP, 0, dW + 3, g.flow, g.corr, oc, nullptr, (int*)(dW + 1), ogrid, gs, ol));
+      }
+      if (fan) {
+        cudaEvent_t j = nullptr;
+        CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+        joins.push_back(j);
+        CK(cudaEventRecord(j, gs));
+      }
     }
-    if (fan) {
-      cudaEvent_t j = nullptr;
-      CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
-      joins.push_back(j);
-      CK(cudaEventRecord(j, gs));
+    for (cudaEvent_t j : joins) CK(cudaStreamWaitEvent(s->st, j, 0));
+    for (int i = 0; i < n; ++i) {
+      dsm_sim* q = sims[i];
+      if (q->flow) {
+        CK(launch_stress_reduce_dev(q->d_ens, q->d_red, s->st));
+        CK(cudaMemcpyAsync(q->hw->red, q->d_red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+      }
+      CK(cudaMemcpyAsync(q->hw->cnt, q->d_counters, sizeof(q->hw->cnt), cudaMemcpyDeviceToHost, s->st));
     }
-  }
-  for (cudaEvent_t j : joins) {
-    CK(cudaStreamWaitEvent(s->st, j, 0));
-    cudaEventDestroy(j);
-  }
+    return DSM_OK;
+  };
+  const int rc = enqueue();
+  // on an error the side streams may still run launches that read the
+  // temporaries without s->st waiting for them: wait for each first
+  if (rc != DSM_OK)
+    for (cudaStream_t u : used) cudaStreamSynchronize(u);
+  for (cudaEvent_t j : joins) cudaEventDestroy(j);
   if (ready) cudaEventDestroy(ready);
-  for (int i = 0; i < n && rc == DSM_OK; ++i) {
-    dsm_sim* q = sims[i];
-    if (q->flow) {
-      CK(launch_stress_reduce_dev(q->d_ens, q->d_red, s->st));
-      CK(cudaMemcpyAsync(q->hw->red, q->d_red, 9 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
-    }
-    CK(cudaMemcpyAsync(q->hw->cnt, q->d_counters, sizeof(q->hw->cnt), cudaMemcpyDeviceToHost, s->st));
-  }
   for (void* p : tmp) cudaFreeAsync(p, s->st);
-  CK(cudaStreamSynchronize(s->st));
-  CK(cudaGetLastError());
+  const cudaError_t sync_err = cudaStreamSynchronize(s->st);
   if (rc != DSM_OK) return rc;
+  if (sync_err != cudaSuccess)
+    return fail(s, DSM_ERR_CUDA, std::string("dsm_advance_batch: ") + cudaGetErrorString(sync_err));
+  CK(cudaGetLastError());
   for (int i = 0; i < n; ++i) {
     const unsigned long long* cnt = sims[i]->hw->cnt;
     if (events) events[i] = cnt[0];

@@ -29,6 +29,11 @@ struct GexTable {
   double prefact = 0.0;      // CD creation prefactor step * sum normdt / beta
 };
 int make_gex_table(float a, float b, float mp, float mk, double beta, GexTable* out);
+// Per-N rate tables (sliding factors, end rates, CD creation, 3/N, 4/i
+// frictions) in one buffer of table_floats(nmax) floats; the vector form
+// sizes the buffer itself.
+size_t table_floats(int nmax);
+void make_tables(int nmax, double beta_f, float prefact, float* buf, TableOffsets& off);
 void make_tables(int nmax, double beta_f, float prefact, std::vector<float>& buf, TableOffsets& off);
 int corr_levels_for(double t_end, double dt, int p, int m);
 

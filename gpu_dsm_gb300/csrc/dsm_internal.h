@@ -139,5 +139,7 @@ cudaError_t launch_gt_reduce_dev(const EnsDev* d_ens, int levels, int p, double*
                                  cudaStream_t st);
 cudaError_t launch_window_begin(EnsDev* d_ens, const long long* d_win, int n, int w, cudaStream_t st);
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st);
+// stress of every chain from its state in HBM (d_out8: n_chains x 8 floats), then the reduction
+cudaError_t launch_state_stress(const EnsDev* d_ens, int n_chains, float* d_out8, double* d_out9, cudaStream_t st);
 
 }  // namespace dsm

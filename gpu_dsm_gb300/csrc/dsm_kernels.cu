@@ -1370,12 +1370,14 @@ __global__ void k_gt_reduce(const EnsDev* __restrict__ ensp, double* gsum, long 
 // Ensemble average of the window-end stress over non-stalled, non-NaN chains
 // (ensemble_call_block.cu:471-491), FP64, fixed tree order.  out[0..7] sums,
 // out[8] chain count.
-__global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
+// per_chain: n_chains x 8 floats (NULL: the flow kernel's E.out_stress)
+__global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, const float* __restrict__ per_chain, double* out) {
   const EnsDev& E = *ensp;
   __shared__ double red[9][256];
   double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const float* src = per_chain != nullptr ? per_chain : E.out_stress;
   for (int c = threadIdx.x; c < E.n_chains; c += blockDim.x) {
-    const float* s = E.out_stress + (size_t)c * 8;
+    const float* s = src + (size_t)c * 8;
     if (E.cs[c].stall != 0 || s[0] != s[0]) continue;
 #pragma unroll
     for (int q = 0; q < 8; ++q) a[q] += (double)s[q];
@@ -1396,6 +1398,41 @@ __global__ void k_stress_reduce(const EnsDev* __restrict__ ensp, double* out) {
 
 // Slots beyond a chain's strands are not maintained by the step kernel; the
 // reference layout has them zero.  One thread per (chain, slot).
+// Stress of every chain from its state in HBM, for ensembles whose step
+// kernel keeps no per-chain stress (equilibrium): the sums of flow_stress
+// (ensemble_kernel.cu:504-538) in the same order, strand i into partial
+// i mod 16 and a 16-lane tree, one warp per chain; out8 gets n_chains x 8.
+__global__ void k_state_stress(const EnsDev* __restrict__ ensp, float* out8) {
+  const EnsDev& E = *ensp;
+  const int lane = threadIdx.x & 31;
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= E.n_chains) return;
+  const int Z = E.cs[c].Z;
+  const float4* q = E.QN + (size_t)c * E.cap;
+  float s[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = lane; lane < 16 && i < Z; i += 16) {
+    const float4 v = q[i];
+    const float w = __ldg(&E.INV3N[(int)v.w]);
+    s[0] = __fmaf_rn(-__fmul_rn(v.x, v.x), w, s[0]);
+    s[1] = __fmaf_rn(-__fmul_rn(v.y, v.y), w, s[1]);
+    s[2] = __fmaf_rn(-__fmul_rn(v.z, v.z), w, s[2]);
+    s[3] = __fmaf_rn(-__fmul_rn(v.x, v.y), w, s[3]);
+    s[4] = __fmaf_rn(-__fmul_rn(v.y, v.z), w, s[4]);
+    s[5] = __fmaf_rn(-__fmul_rn(v.x, v.z), w, s[5]);
+    s[6] = __fadd_rn(s[6], __fsqrt_rn(m_q2(v.x, v.y, v.z)));
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) s[k] = __fadd_rn(s[k], __shfl_xor_sync(FULL_MASK, s[k], o));
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) out8[c * 8 + k] = s[k];
+    out8[c * 8 + 7] = (float)Z;
+  }
+}
+
 __global__ void k_clear_tail(float4* QN, float* tau, const ChainState* __restrict__ cs, int n_chains, int cap) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)n_chains * cap) return;
@@ -1608,7 +1645,13 @@ cudaError_t launch_series_reduce(const EnsDev* d_ens, double* out, int n, cudaSt
   return cudaGetLastError();
 }
 cudaError_t launch_stress_reduce_dev(const EnsDev* d_ens, double* d_out9, cudaStream_t st) {
-  k_stress_reduce<<<1, 256, 0, st>>>(d_ens, d_out9);
+  k_stress_reduce<<<1, 256, 0, st>>>(d_ens, nullptr, d_out9);
+  return cudaGetLastError();
+}
+cudaError_t launch_state_stress(const EnsDev* d_ens, int n_chains, float* d_out8, double* d_out9, cudaStream_t st) {
+  const long long threads = 32LL * n_chains;
+  k_state_stress<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d_ens, d_out8);
+  k_stress_reduce<<<1, 256, 0, st>>>(d_ens, d_out8, d_out9);
   return cudaGetLastError();
 }
 

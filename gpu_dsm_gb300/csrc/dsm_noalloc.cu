@@ -49,35 +49,6 @@ constexpr size_t kOffCounters = 1056;                  // unsigned long long[4]
 constexpr size_t kOffTables = 2048;                    // float tables
 static_assert(sizeof(dsm::EnsDev) <= kOffPrefix, "descriptor block");
 
-size_t table_floats(int nmax) {
-  const size_t n = (size_t)nmax + 2;
-  return 8 * n + (8 * n + 8) + n + 4;
-}
-
-// Rate tables in the layout of dsm::make_tables (dsm_host.cu), written into a
-// caller buffer instead of a vector; same formulas, so the values are identical.
-void fill_tables(float* buf, int nmax, double beta_f, float prefact, dsm::TableOffsets* off) {
-  const size_t n = (size_t)nmax + 2;
-  const size_t nf = 8 * n + 8;
-  off->NT = 0; off->NE = 4 * n; off->FRIC = 8 * n; off->INV3N = 8 * n + nf;
-  std::memset(buf, 0, (off->INV3N + n + 4) * sizeof(float));
-  for (size_t N = 1; N < n; ++N) {
-    const double d = (double)N;
-    float* nt = &buf[off->NT + 4 * N];
-    nt[0] = (float)(0.75 / (d * (d + 1.0)));
-    nt[1] = N >= 2 ? (float)(0.75 / (d * (d - 1.0))) : 0.f;
-    nt[2] = (float)(std::sqrt(d / (d + 1.0)) * std::sqrt(std::sqrt(d / (d + 1.0))));
-    nt[3] = N >= 2 ? (float)(std::sqrt(d / (d - 1.0)) * std::sqrt(std::sqrt(d / (d - 1.0)))) : 0.f;
-    float* ne = &buf[off->NE + 4 * N];
-    ne[0] = (float)(2.0 / (beta_f * (d + 0.5)));
-    ne[1] = (float)(1.0 / (0.75 + (d + 0.25)));
-    ne[2] = (float)(1.0 / (0.75 + 0.5 * d));
-    ne[3] = (float)((double)prefact * (d - 1.0));
-    buf[off->INV3N + N] = (float)(3.0 / d);
-  }
-  for (size_t i = 1; i < nf; ++i) buf[off->FRIC + i] = (float)(4.0 / (double)i);
-}
-
 int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
@@ -102,10 +73,14 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   if (cap < 1 || cap > 4096) return fail(DSM_ERR_INVALID, "z_max must be in [1, 4096]");
   if (p->nk_chain != nullptr) return fail(DSM_ERR_INVALID, "polydisperse ensembles need per-chain tables: use dsm_create");
   if (p->pd_flag != 0) return fail(DSM_ERR_INVALID, "pd_flag=1 is not supported");
-  if (p->eq_type == 1) return fail(DSM_ERR_INVALID, "the G(t) correlator needs per-chain buffers: use dsm_create");
+  // dsm_create's rule: a G(t) or MSD correlator runs for equilibrium
+  // ensembles with eq_type 1 or 2 and positive sync_dt and t_end
+  if (!flow && (p->eq_type == 1 || p->eq_type == 2) && p->sync_dt > 0 && p->t_end > 0)
+    return fail(DSM_ERR_INVALID, "the G(t) / MSD correlator needs per-chain buffers: use dsm_create");
   if (flow && d_stress_out == nullptr) return fail(DSM_ERR_INVALID, "flow ensembles need d_stress_out (n_chains x 8 floats)");
   if (!(t_end >= 0.0) || t_end * dsm::TICKS >= 9.0e18) return fail(DSM_ERR_INVALID, "t_end out of range");
-  if (table_floats(p->nk) * sizeof(float) + kOffTables > kScratchBytes) return fail(DSM_ERR_INVALID, "tables exceed scratch");
+  if (dsm::table_floats(p->nk) * sizeof(float) + kOffTables > kScratchBytes)
+    return fail(DSM_ERR_INVALID, "tables exceed scratch");
 
   std::lock_guard<std::mutex> lock(g_mu);
   int dev = 0;
@@ -130,7 +105,7 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   std::memset(g_host_stage, 0, kOffTables);
   dsm::TableOffsets to;
   float* htab = (float*)(g_host_stage + kOffTables);
-  fill_tables(htab, p->nk, be, prefact, &to);
+  dsm::make_tables(p->nk, be, prefact, htab, to);
   const float* dtab = (const float*)(dbase + kOffTables);
   dsm::EnsDev E;
   std::memset(&E, 0, sizeof(E));
@@ -143,8 +118,10 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   E.chain_offset = p->chain_offset;
   E.t_end_ticks = (int64_t)std::llrint(t_end * dsm::TICKS);
   E.step_limit = step_limit < 0 ? INT64_MAX : step_limit;
-  // a chain that does 100x the expected events of the window (at least 2^24)
-  // stops with stall code 5, as in dsm_advance
+  // a chain that does 100x the expected events (at least 2^24) stops with
+  // stall code 5; the expectation is taken over [0, t_end], since no window
+  // start is known here, so for windows that start later the cap is looser
+  // than dsm_advance's, which counts from the window start
   const double expect = 0.25 * (double)p->nk * t_end * 100.0;
   E.watchdog_events = (int64_t)(expect > 16777216.0 ? (expect < 9.0e18 ? expect : 9.0e18) : 16777216.0);
   E.pcd = pcd.dev;
@@ -156,7 +133,7 @@ extern "C" int dsm_advance_noalloc(const dsm_params* p, dsm_float4* d_QN, float*
   std::memcpy(g_host_stage + kOffEns, &E, sizeof(E));
   const long long pre[2] = {0, (long long)p->n_chains};
   std::memcpy(g_host_stage + kOffPrefix, pre, sizeof(pre));
-  const size_t bytes = kOffTables + table_floats(p->nk) * sizeof(float);
+  const size_t bytes = kOffTables + dsm::table_floats(p->nk) * sizeof(float);
   e = cudaMemcpyAsync(dbase, g_host_stage, bytes, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return fail(DSM_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
 

@@ -166,7 +166,8 @@ int dsm_advance_batch(dsm_sim** sims, int32_t n, const double* t_end, const int6
                       uint64_t* events);
 
 /* Ensemble-average stress of the current state over non-stalled chains
- * (flow output).  Replaces calc_stress / calc_stress_call_block
+ * (the flow output; for equilibrium ensembles evaluated from the current
+ * state on call).  Replaces calc_stress / calc_stress_call_block
  * (common/ensemble.cu:210-221, common/ensemble_call_block.cu:452-505). */
 int dsm_stress(dsm_sim* sim, dsm_stress_plus* out, int32_t* chain_count);
 
@@ -276,7 +277,9 @@ int dsm_checkpoint_load(dsm_sim* sim, const char* path);
  * the chains; tables, descriptor and counters live in one static device array
  * of DSM_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * the process exits.  Limits: nk <= DSM_NOALLOC_MAX_NK (larger is rejected with
- * DSM_ERR_INVALID), z_max <= 4096, monodisperse, no G(t) correlator.  The first
+ * DSM_ERR_INVALID), z_max <= 4096, monodisperse, and no correlator: params
+ * for which dsm_create would run one (no flow, eq_type 1 or 2, sync_dt > 0 and
+ * t_end > 0) are rejected with DSM_ERR_INVALID.  The first
  * call on a device looks up the array's device address (make it before any
  * stream capture).  All calls share the array and it keeps the last call's
  * contents: calls that overlap on the GPU race and must be serialised.
@@ -305,9 +308,17 @@ typedef struct dsm_chain_state {
  * float4 {Qx,Qy,Qz,N}; d_tau: n*z_max rates; d_state: n dsm_chain_state) to
  * time t_end or step_limit events, on `stream` (a cudaStream_t, NULL = legacy
  * default stream).  Flow ensembles (kappa != 0) also need d_stress_out
- * (n*8 floats: xx yy zz xy yz zx Lpp Z of every chain at the end).  Results
- * are identical to dsm_advance on the same inputs.  If events is non-NULL the
- * call waits for the kernel and stores the number of kMC events done. */
+ * (n*8 floats: xx yy zz xy yz zx Lpp Z of every chain at the end).  d_QN,
+ * d_tau and d_state must hold chains as dsm_get_chains / dsm_get_ext report
+ * them (or as a previous call left them): in particular every state's nk must
+ * equal params->nk and Z must lie in [1, z_max]; the kernel does not check
+ * them, and a zeroed state gives infinite or NaN rates.  Results are identical
+ * to dsm_advance on the same inputs, with one exception: the runaway-chain cap
+ * (a chain doing 100x the expected events, at least 2^24, stops with stall
+ * code 5) is sized from [0, t_end] here and from the window [t_start, t_end]
+ * in dsm_advance, so a chain whose time step collapses in a window that
+ * starts after t = 0 is stopped later here.  If events is non-NULL the call
+ * waits for the kernel and stores the number of kMC events done. */
 int dsm_advance_noalloc(const dsm_params* params, dsm_float4* d_QN, float* d_tau, dsm_chain_state* d_state,
                         float* d_stress_out, double t_end, int64_t step_limit, void* stream, uint64_t* events);
 /* Message of the last failed dsm_advance_noalloc of the calling thread */
@@ -383,9 +394,14 @@ void dsm_serve_close(dsm_server* srv);
  * Reference driver entry point (common/main_cuda.cu:34), same signature and
  * return convention (0 ok, -1 aborted): reads input.dat from the working
  * directory, writes tau[_id].dat / G[_id].dat, honours -s/-l/-distr.
+ * C linkage here; dsm_reference.h declares the same function with the C++
+ * linkage of the reference's GUI (GUI/main.cpp:22) and defines
+ * DSM_NO_C_MAIN_CUDA so that one translation unit sees one of the two.
  * --------------------------------------------------------------------- */
+#ifndef DSM_NO_C_MAIN_CUDA
 int main_cuda(DSM_BOOL* run_flag, int job_ID, char* savefile, char* loadfile, int device_ID,
               DSM_BOOL distr, int* progress_bar);
+#endif
 
 #ifdef __cplusplus
 }

@@ -415,3 +415,29 @@ def gt_error_vs_fp64(g_test: np.ndarray, fp64: "Oracle", prec: float = 0.02) -> 
             "resolved_lags": int(res.sum()), "lags": int(m.sum()), "precision": prec,
             "dev_sigma": float((d[m] / np.maximum(sig[m], 1e-300)).max()),
             "rel_scale": float(d[m].max() / abs(g_ref[0, 0]))}
+
+
+def gt_points_error_vs_fp64(g_points: np.ndarray, fp64: "Oracle", prec: float = 0.02) -> dict:
+    """gt_error_vs_fp64 for a G(t) in the G.dat point order and normalisation
+    (correlator.cu:146-187, ensemble.cu:318-335): level 0 lags 0..p-1, then
+    lags p/m..p-1 of every further level, each sum / 3 / N_cha."""
+    L, p, m = fp64.p.corr_levels, fp64.p.corr_p, fp64.p.corr_m
+    n = fp64.n
+    g_ref, cnt = fp64.gt_raw()
+    per = fp64.gt_chains()
+
+    def flat(a):
+        rows = [a[..., 0, :]] + [a[..., k, p // m:] for k in range(1, L)]
+        return np.concatenate(rows, axis=-1)
+
+    npt = len(g_points)
+    ref = flat(g_ref)[:npt] / 3.0 / n
+    c = flat(cnt)[:npt]
+    sig = flat(per).std(axis=0, ddof=1)[:npt] / np.sqrt(n) / 3.0
+    d = np.abs(np.asarray(g_points, np.float64) - ref)
+    m_ = c > 0
+    res = m_ & (sig < prec * np.abs(ref))
+    return {"rel_resolved": float((d[res] / np.abs(ref[res])).max()) if res.any() else None,
+            "resolved_lags": int(res.sum()), "lags": int(m_.sum()), "precision": prec,
+            "dev_sigma": float((d[m_] / np.maximum(sig[m_], 1e-300)).max()),
+            "rel_scale": float(d[m_].max() / abs(ref[0]))}

@@ -585,3 +585,21 @@ def test_observables_independent_of_tile_width(dsm_mod):
             ga, ca = a.gt_raw()
             gb, cb = b.gt_raw()
             assert np.array_equal(ca, cb) and np.array_equal(ga, gb)
+
+
+def test_equilibrium_stress_against_oracle(dsm_mod, oracle_mod):
+    """dsm_stress of an equilibrium ensemble (evaluated from the current state,
+    as calc_stress does for any ensemble, ensemble.cu:210-221) against the
+    oracle's FP64 average of the same chains."""
+    g, o = pair(dsm_mod, oracle_mod, nk=40, n=512, seed=13, corr=True, sync_dt=1.0, t_end=60.0)
+    g.init_equilibrium()
+    o.init_equilibrium()
+    g.advance(60.0)
+    o.run(60.0)
+    assert_bitexact(gpu_state(g), o.get_state(), keys=("Z", "QN", "tau", "T", "step", "hash"), what="eq stress run")
+    sg, cg = g.stress()
+    so, co = o.stress()
+    assert cg == co == 512
+    scale = np.abs(so[:6]).max() + 1e-6
+    assert np.all(np.abs(sg[:6] - so[:6]) <= 1e-5 * scale), (sg, so)
+    assert sg[6] == pytest.approx(so[6], rel=1e-5) and sg[7] == pytest.approx(so[7], rel=1e-6)

@@ -39,6 +39,20 @@ def test_noalloc_rejects_oversize(dsm_mod):
     assert b"exceeds the no-allocation limit" in lib.dsm_noalloc_last_error()
 
 
+@pytest.mark.parametrize("eq_type", [1, 2])
+def test_noalloc_rejects_correlator(dsm_mod, eq_type):
+    """Parameters for which dsm_create would run a G(t) (eq_type 1) or MSD
+    (eq_type 2) correlator are refused before any device work."""
+    lib = _bind(dsm_mod)
+    p = dsm_mod.api.DsmParams()
+    p.beta, p.nk, p.n_chains, p.cd_flag = 1.0, 25, 8, 1
+    p.eq_type, p.sync_dt, p.t_end = eq_type, 1.0, 10.0
+    buf = C.c_void_p(1)  # never dereferenced: the correlator check comes first
+    rc = lib.dsm_advance_noalloc(C.byref(p), buf, buf, buf, None, 10.0, -1, None, None)
+    assert rc == -3
+    assert b"correlator" in lib.dsm_noalloc_last_error()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("kappa,nk,n", [((0.0,) * 9, 50, 512), ((0.0, 2.0e-3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0), 50, 512),
                                         ((0.0,) * 9, 2000, 64)])
