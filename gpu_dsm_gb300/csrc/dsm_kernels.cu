@@ -159,8 +159,33 @@ __device__ __forceinline__ int warp_max_i(int v) {
   return v;
 }
 
+// Quantisation of a rate component to 64-bit fixed point: llrint(x * sf).
 __device__ __forceinline__ unsigned long long quant(float x, float sf) {
   return (unsigned long long)__float2ll_rn(__fmul_rn(x, sf));
+}
+
+// The same rounding built from 32-bit operations, for update_pairs.  sm_103a
+// runs the 64-bit conversion instruction on its narrow FP64 pipe: about 100
+// cycles of latency and as many cycles of pipe occupancy per warp
+// instruction, so four of them in a row sat on the critical path of every
+// sliding event (measured: 2.205e9 against 2.15e9 events/s at N_K = 200).
+// Where one or two conversions stand alone, or in the flow pass that
+// converts every pair, the extra instructions of this form cost more than
+// they save, and the instruction stays.
+//
+// f2u64_rn: y in [0, 2^63) (or -0.0), the value llrint(y) takes.  Below 2^23
+// adding 2^23 rounds y to an integer (the sum's ulp is 1) and the sum's bit
+// pattern minus that of 2^23 is the integer, also across the carry into 2^24;
+// from 2^23 up y is an integer and its significand shifted by the exponent is
+// it.  NaN, infinity and y >= 2^63 give an unspecified value; update_pairs
+// flags those inputs and never uses the result.  Both forms are computed and
+// one is selected, so no branch splits the caller.
+__device__ __forceinline__ unsigned long long f2u64_rn(float y) {
+  const unsigned b = __float_as_uint(y) & 0x7fffffffu;
+  const int e = (int)(b >> 23) - 150;
+  const unsigned small = __float_as_uint(__fadd_rn(__uint_as_float(b), 8388608.0f)) - 0x4B000000u;
+  const unsigned long long big = (unsigned long long)((b & 0x7fffffu) | 0x800000u) << (e & 63);
+  return e < 0 ? (unsigned long long)small : big;
 }
 
 // Philox words (counter layout shared with the oracle)
@@ -435,9 +460,8 @@ __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, in
     const float y0 = __fmul_rn(o0, sf), y1 = __fmul_rn(w, sf), y2 = __fmul_rn(wm, sf), y3 = __fmul_rn(o3, sf);
     const float lim = 281474976710656.0f;  // 2^(LIMIT_E+1)
     bad = !(y0 < lim) || !(y1 < lim) || !(y2 < lim) || !(y3 < lim);
-    const unsigned long long v1 = (unsigned long long)__float2ll_rn(y1);
-    const unsigned long long tot = (unsigned long long)__float2ll_rn(y0) + v1 +
-                                   (unsigned long long)__float2ll_rn(y2) + (unsigned long long)__float2ll_rn(y3);
+    const unsigned long long v1 = f2u64_rn(y1);
+    const unsigned long long tot = f2u64_rn(y0) + v1 + f2u64_rn(y2) + f2u64_rn(y3);
     d = tot - sl.R[p];
     sl.R[p] = tot;
     sl.P[p] = v1;
