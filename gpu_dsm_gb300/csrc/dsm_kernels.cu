@@ -166,12 +166,13 @@ __device__ __forceinline__ unsigned long long quant(float x, float sf) {
 
 // The same rounding built from 32-bit operations, for update_pairs.  sm_103a
 // runs the 64-bit conversion instruction on its narrow FP64 pipe: about 100
-// cycles of latency and as many cycles of pipe occupancy per warp
-// instruction, so four of them in a row sat on the critical path of every
-// sliding event (measured: 2.205e9 against 2.15e9 events/s at N_K = 200).
-// Where one or two conversions stand alone, or in the flow pass that
-// converts every pair, the extra instructions of this form cost more than
-// they save, and the instruction stays.
+// cycles of latency and as many cycles of pipe occupancy per warp instruction
+// (about 31 cycles of latency for this form).  update_pairs converts the
+// components of every recomputed pair on the critical path of each event.
+// Where one or two conversions stand alone (event classification, dt), or in
+// the flow pass that converts every pair of the chain each event, the extra
+// instructions of this form cost more than they save at full occupancy, and
+// the instruction stays (each measured on the N_K = 200 melt and shear).
 //
 // f2u64_rn: y in [0, 2^63) (or -0.0), the value llrint(y) takes.  Below 2^23
 // adding 2^23 rounds y to an integer (the sum's ulp is 1) and the sum's bit
@@ -429,43 +430,46 @@ __device__ __forceinline__ float end_comp(const EnsDev& E, int q, int Z, const i
   return (q == 0) ? cdc : ((q <= 2) ? sdc : sdd);
 }
 
-// Recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 16) with two lanes
-// per pair: the even lane evaluates the shift +1 component, the odd lane the
-// shift -1 component.  Returns 4 when a component is NaN, inf or beyond the
-// fixed-point range (the caller then runs the full pass, which decides between a
-// stall and a lower scale, as the oracle does); *delta gets new - old of the
-// pair total on the even lane (0 elsewhere).
+// Recompute quantised totals of pairs [p0, p0+cnt) (cnt <= 3; every caller
+// touches at most three pairs) with four lanes per pair, one rate component
+// each: k = lane & 3 is 0 CD destruction, 1 shift +1, 2 shift -1, 3 CD
+// creation.  All four lanes run the shift-rate arithmetic (the two CD lanes
+// discard it) so that the group takes one path; each lane quantises its own
+// component, and two xor shuffles form the pair total (an integer sum, so its
+// order does not matter).  Returns 4 when a component is NaN, inf or beyond
+// the fixed-point range (the caller then runs the full pass, which decides
+// between a stall and a lower scale, as the oracle does); *delta gets new - old
+// of the pair total on the group's first lane (lanes 0, 4, 8), 0 elsewhere.
 template <int W>
 __device__ __forceinline__ int update_pairs(const EnsDev& E, Slot& sl, int Z, int S, int p0, int cnt, const Tile<W>& t,
                                             unsigned long long* delta) {
   const int lane = t.lane;
-  const int p = p0 + (lane >> 1);
-  const bool act = (lane < 2 * cnt) && p >= 0 && p < Z - 1;
-  float w = 0.0f;
-  int N1 = 1;
+  const int k = lane & 3;
+  const int p = p0 + (lane >> 2);
+  const bool act = (lane < 4 * cnt) && p >= 0 && p < Z - 1;
+  float o = 0.0f;
   if (act) {
-    N1 = sl.N[p];
+    const int N1 = sl.N[p];
     const int N2 = sl.N[p + 1];
     const float q1 = sl.Q[p].w, q2 = sl.Q[p + 1].w;
     const float4 a = __ldg(&E.NT[N1]), b = __ldg(&E.NT[N2]);
-    w = shift_comp(E, (lane & 1) != 0, N1, q1, N2, q2, a, b);
+    const float w = shift_comp(E, k == 2, N1, q1, N2, q2, a, b);
+    // the CD components, loaded by the whole group (same addresses) and selected
+    const float tp = sl.T[p], ne = __ldg(&E.NE[N1]).w;
+    const float cd = (k == 0) ? tp : ne;
+    o = (k == 1 || k == 2) ? w : (E.cd_flag ? cd : 0.0f);
   }
-  const float wm = t.shfl_xor(w, 1);
+  const float y = __fmul_rn(o, pow2f(S));
+  const bool bad = !(y < 281474976710656.0f);  // 2^(LIMIT_E+1); NaN too
+  const unsigned long long v = f2u64_rn(y);
+  unsigned long long tot = v + t.shfl_xor(v, 1);
+  tot += t.shfl_xor(tot, 2);
   unsigned long long d = 0;
-  bool bad = false;
-  if (act && !(lane & 1)) {
-    const float sf = pow2f(S);
-    const float o0 = E.cd_flag ? sl.T[p] : 0.0f;
-    const float o3 = E.cd_flag ? __ldg(&E.NE[N1]).w : 0.0f;
-    const float y0 = __fmul_rn(o0, sf), y1 = __fmul_rn(w, sf), y2 = __fmul_rn(wm, sf), y3 = __fmul_rn(o3, sf);
-    const float lim = 281474976710656.0f;  // 2^(LIMIT_E+1)
-    bad = !(y0 < lim) || !(y1 < lim) || !(y2 < lim) || !(y3 < lim);
-    const unsigned long long v1 = f2u64_rn(y1);
-    const unsigned long long tot = f2u64_rn(y0) + v1 + f2u64_rn(y2) + f2u64_rn(y3);
+  if (act && k == 0) {
     d = tot - sl.R[p];
     sl.R[p] = tot;
-    sl.P[p] = v1;
   }
+  if (act && k == 1) sl.P[p] = v;
   *delta = d;
   t.sync();
   return t.any(bad) ? 4 : 0;
@@ -1152,13 +1156,13 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         unsigned long long dl;
         pend |= update_pairs<W>(E, sl, Z, S, up0, upn, t, &dl);
         if (slide) {
-          // patch the prefix sums with the deltas of pairs j-1, j, j+1 (even
-          // lanes 0, 2, 4); pair j lies in lane L's chunk, its neighbours in L's
+          // patch the prefix sums with the deltas of pairs j-1, j, j+1 (lanes
+          // 0, 4, 8); pair j lies in lane L's chunk, its neighbours in L's
           // or the adjacent chunk (out-of-range pairs carry d == 0)
           const int jL = L * cw;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
-            const unsigned long long d = t.shfl(dl, 2 * k);
+            const unsigned long long d = t.shfl(dl, 4 * k);
             const int own = (k == 0) ? ((j == jL) ? L - 1 : L) : (k == 1) ? L : ((j + 1 == jL + cw) ? L + 1 : L);
             if (lane >= own) incl += d;
             if (lane > own) excl += d;
