@@ -21,6 +21,9 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgpudsm.so"
+# debug build with the step kernel's phase clocks (gpu_dsm_gb300/phases.py)
+BUILD_PHASES = PKG / "_build_phases"
+LIB_PHASES = PKG / "libgpudsm_phases.so"
 CLI = PKG / "gpu_DSM"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -50,23 +53,30 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile libgpudsm.so and gpu_DSM if any source is newer than them."""
-    BUILD.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, phases: bool = False) -> Path:
+    """Compile libgpudsm.so and gpu_DSM if any source is newer than them.
+    phases=True builds libgpudsm_phases.so instead: the same sources with the
+    step kernel's phase clocks (-DDSM_PHASE_CLOCKS), in a build folder of its
+    own."""
+    bdir, lib = (BUILD_PHASES, LIB_PHASES) if phases else (BUILD, LIB)
+    flags = NVFLAGS + (["-DDSM_PHASE_CLOCKS"] if phases else [])
+    bdir.mkdir(exist_ok=True)
     nv = nvcc()
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     objs = []
     jobs = []
     for src in SOURCES:
         s = CSRC / src
-        o = BUILD / (s.stem + ".o")
+        o = bdir / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nv, *ARCH, *NVFLAGS, "-c", str(s), "-o", str(o)])
+            jobs.append([nv, *ARCH, *flags, "-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", str(LIB), *map(str, objs)])
+    if force or jobs or _stale(lib, objs):
+        _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", str(lib), *map(str, objs)])
+    if phases:
+        return lib
     cli_src = CSRC / "cli_main.cpp"
     if cli_src.exists() and (force or _stale(CLI, [cli_src, LIB])):
         _run([nv, *ARCH, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(cli_src), "-o", str(CLI),

@@ -885,6 +885,39 @@ __device__ DSM_APPLY_ATTR void apply_destroy(Slot& sl, int evn, int j, int Z, co
   t.sync();
 }
 
+// ------------------------------------------------------------------ phase clocks
+// Debug build (-DDSM_PHASE_CLOCKS, library libgpudsm_phases.so, driven by
+// gpu_dsm_gb300/phases.py): SM clock cycles of the event loop per phase,
+// summed over chains.  Lane k of a tile accumulates phase k (so the counters
+// cost one register), lanes 12..14 count sliding, destroying and creating
+// events; each chain adds its sums to g_phase at the end of its launch
+// (g_phase[20]: its events).  The per-launch sums of one chain must stay below
+// 2^32 cycles (about 2 s).  The normal build compiles none of it.
+#ifdef DSM_PHASE_CLOCKS
+__device__ unsigned long long g_phase[32];
+#define DSM_PHASE_BEGIN unsigned ph_acc = 0, ph_cnt = 0, ph_prev = (unsigned)clock()
+#define DSM_PHASE(k)                          \
+  do {                                        \
+    const unsigned n_ = (unsigned)clock();    \
+    if (lane == (k)) ph_acc += n_ - ph_prev;  \
+    ph_prev = n_;                             \
+  } while (0)
+#define DSM_PHASE_COUNT(k) \
+  do {                     \
+    if (lane == (k)) ++ph_cnt; \
+  } while (0)
+#define DSM_PHASE_FLUSH()                                                                   \
+  do {                                                                                      \
+    if (lane < 12) atomicAdd(&g_phase[lane], (unsigned long long)ph_acc);                   \
+    if (lane >= 12 && lane < 15) atomicAdd(&g_phase[lane + 4], (unsigned long long)ph_cnt); \
+  } while (0)
+#else
+#define DSM_PHASE_BEGIN
+#define DSM_PHASE(k)
+#define DSM_PHASE_COUNT(k)
+#define DSM_PHASE_FLUSH()
+#endif
+
 // ------------------------------------------------------------------ step kernel
 // CK: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD (compile
 // time, so that the stress kernel carries no MSD code)
@@ -928,6 +961,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       }
       continue;
     }
+    DSM_PHASE_BEGIN;
     int Z = st.Z, S = st.S, stall = st.stall;
     long long T = st.T;
     uint64_t step = st.step;
@@ -998,6 +1032,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
 
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
     bool words = false;  // Philox words of the current batch of W events loaded
+    DSM_PHASE(10);  // chain load and first rate pass
 
     for (;;) {
       // (1) flow: deformation by the previous dt (ensemble_kernel.cu:135-146)
@@ -1030,6 +1065,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         aborted = true;
         break;
       }
+      DSM_PHASE(0);  // checks and correlator samples
       const int np = Z - 1;
       // (4) rates: flow recomputes everything; equilibrium refreshes the chain
       // ends when a strand next to an end changed
@@ -1054,6 +1090,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       }
       if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
       if (pend & 2) { stall = ST_INF; dt_prev = 0.0f; break; }
+      DSM_PHASE(1);  // chain-end rates, rate passes
       const float sf = pow2f(S);
       // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
       if (rescan) {
@@ -1074,6 +1111,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (dt == 0.0f) { stall = ST_DT_ZERO; dt_prev = 0.0f; break; }
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
+      DSM_PHASE(2);  // prefix scan, dt
       // (7) Philox words of this event (one evaluation per 32 events)
       if ((step & (uint64_t)(W - 1)) == 0 || !words) {
         const uint64_t ctr = (step & ~(uint64_t)(W - 1)) + (uint64_t)lane;
@@ -1106,6 +1144,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       }
       jj = t.shfl(jj, L);
       r = t.shfl(r, L);
+      DSM_PHASE(3);  // Philox, pick, chunk walk
       int evn, j = -1;
       unsigned long long rem = 0, wsel = 0;
       if (jj < np) {
@@ -1123,6 +1162,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         wsel = sl.R[jj];
         evn = (q == 0) ? CDC_TAIL : (q == 1) ? SDC_HEAD : (q == 2) ? SDC_TAIL : (q == 3) ? SDD_HEAD : SDD_TAIL;
       }
+      DSM_PHASE(4);  // classification
       T += dtt;
       // (9) apply
       uint32_t code = ((uint32_t)evn << 24) | (uint32_t)(j < 0 ? 0 : j);
@@ -1152,6 +1192,13 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         code |= (uint32_t)newn << 8;
       }
       t.sync();
+#ifdef DSM_PHASE_CLOCKS
+      {
+        const int k_ = (evn == SDP || evn == SDM) ? 0 : (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) ? 1 : 2;
+        DSM_PHASE(5 + k_);  // apply: slide, destruction, creation
+        DSM_PHASE_COUNT(12 + k_);
+      }
+#endif
       if (!FLOW && upn > 0) {
         unsigned long long dl;
         pend |= update_pairs<W>(E, sl, Z, S, up0, upn, t, &dl);
@@ -1174,10 +1221,13 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       } else if (upn > 0 || ends_dirty) {
         rescan = true;
       }
+      DSM_PHASE(8);  // pair-rate update, prefix patch
       if (lane == 0) sl.h->hash = (sl.h->hash ^ (uint64_t)code) * 0x100000001B3ull;
       ++step;
       dt_prev = dt;
+      DSM_PHASE(9);  // event hash, counters
     }
+    DSM_PHASE(0);
 
     // stopped early because the slot is full (an abort ends the launch anyway)
     const bool deferred = E.cap > slot_cap && Z >= slot_cap && stall == 0 && T < t_end && (long long)step < step_lim;
@@ -1231,6 +1281,9 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         cs->r1[0] = q.r1x; cs->r1[1] = q.r1y; cs->r1[2] = q.r1z;
       }
       atomicAdd(&E.counters[0], done);
+#ifdef DSM_PHASE_CLOCKS
+      atomicAdd(&g_phase[20], done);
+#endif
       if (deferred) {
         lst.defer[atomicAdd(lst.n_defer, 1u)] = (int)(prefix[e] + c);
         atomicAdd(&E.counters[2], 1ull);
@@ -1238,6 +1291,8 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         atomicAdd(&E.counters[1], 1ull);
       }
     }
+    DSM_PHASE(11);  // chain store
+    DSM_PHASE_FLUSH();
     t.sync();
   }
 }
@@ -1684,3 +1739,14 @@ cudaError_t launch_state_stress(const EnsDev* d_ens, int n_chains, float* d_out8
 }
 
 }  // namespace dsm
+
+#ifdef DSM_PHASE_CLOCKS
+// phase counters of the debug build: 32 sums (see the phase clocks above)
+extern "C" int dsm_phase_read(unsigned long long* out32) {
+  return (int)cudaMemcpyFromSymbol(out32, dsm::g_phase, sizeof(dsm::g_phase));
+}
+extern "C" int dsm_phase_clear() {
+  const unsigned long long z[32] = {};
+  return (int)cudaMemcpyToSymbol(dsm::g_phase, z, sizeof(z));
+}
+#endif
