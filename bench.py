@@ -562,8 +562,9 @@ def run_shear(args, device: int = 0) -> dict:
 def run_poly(args, device: int = 0) -> dict:
     """Batched polydisperse melt: 262144 chains, N_K log-normal (mean 150,
     PDI 1.5 = exp(sigma^2), clipped to [10, 2000], seed 7), beta=1, G(t)
-    p=64 m=8 (levels for t_end=1e6).  One persistent launch per size class,
-    the schedule chosen by the online autotuner on --poly-tune-window windows,
+    p=64 m=8 (levels for t_end=1e6).  Size classes as concurrent persistent
+    launches or as one carved launch, the schedule and form chosen by the online
+    autotuner on --poly-tune-window windows,
     then --poly-windows timed windows of --poly-window tau_K (default 4 x 250,
     1e3 tau_K as for the monodisperse workload) in one dsm_advance_series call."""
     import gpu_dsm_gb300 as dsm
@@ -578,6 +579,9 @@ def run_poly(args, device: int = 0) -> dict:
     e.init_equilibrium()
     e.advance(args.poly_tune_window)
     best = e.autotune(args.poly_tune_window)
+    if args.poly_form >= 0:  # force the class form after tuning (0 concurrent launches, 1 carved launch)
+        e.set_class_form(args.poly_form)
+    form = e.class_form()
     ev, _ = e.advance_series(args.poly_window, args.poly_windows)
     ms = e.last_window()["kernel_ms"]
     sched = e.schedule()
@@ -586,6 +590,8 @@ def run_poly(args, device: int = 0) -> dict:
                         f"max {int(nkc.max())}), beta=1, G(t) p=64 m=8",
             "events_per_s": ev / (ms / 1e3), "events": int(ev), "kernel_ms": ms,
             "windows": args.poly_windows, "window_tau": args.poly_window, "autotune": best, "schedule": sched,
+            "class_form": "one carved launch (large, middle, small) + huge class beside it" if form == 1
+                          else "concurrent launches, one per class",
             "timing": "CUDA events around the windows of one dsm_advance_series call (size-class launches + "
                       "overflow launch per window, issued without host synchronisation)"}
 
@@ -730,6 +736,8 @@ def main():
     ap.add_argument("--poly-window", type=float, default=250.0, help="tau_K per timed polydisperse window")
     ap.add_argument("--poly-windows", type=int, default=4)
     ap.add_argument("--poly-tune-window", type=float, default=5.0, help="tau_K per autotuner candidate window")
+    ap.add_argument("--poly-form", type=int, default=-1,
+                    help="size-class form after autotuning: -1 the autotuner's, 0 concurrent launches, 1 carved launch")
     ap.add_argument("--shear-chains", type=int, default=32768, help="chains per shear ensemble")
     ap.add_argument("--shear-window", type=float, default=0.0, help="tau_K per output window (0: t_end/1000)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving-stream leg")

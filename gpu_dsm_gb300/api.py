@@ -142,6 +142,10 @@ def load_library() -> C.CDLL:
     lib.dsm_set_schedule.restype = C.c_int
     lib.dsm_get_schedule.argtypes = [vp, C.POINTER(i32), vp]
     lib.dsm_get_schedule.restype = C.c_int
+    lib.dsm_set_class_form.argtypes = [vp, i32]
+    lib.dsm_set_class_form.restype = C.c_int
+    lib.dsm_get_class_form.argtypes = [vp, C.POINTER(i32)]
+    lib.dsm_get_class_form.restype = C.c_int
     lib.dsm_gex_table.argtypes = [C.c_float] * 4 + [C.c_double, vp, C.POINTER(i32), vp, C.POINTER(i32), vp]
     lib.dsm_gex_table.restype = C.c_int
     lib.dsm_pcd.argtypes = [C.c_double, i32, vp]
@@ -448,6 +452,16 @@ class Ensemble:
     def set_schedule(self, small_slot: int = 0, large_grid: int = 0, lanes: int = 0, z_margin_sd: float = 0.0) -> None:
         """Size-class launch schedule of a polydisperse ensemble (dsm_set_schedule)."""
         self._check(self._lib.dsm_set_schedule(self._h, small_slot, large_grid, lanes, z_margin_sd))
+
+    def set_class_form(self, form: int) -> None:
+        """0: size classes as concurrent launches; 1: large, middle and small
+        classes in one carved launch (dsm_set_class_form)."""
+        self._check(self._lib.dsm_set_class_form(self._h, form))
+
+    def class_form(self) -> int:
+        f = C.c_int32()
+        self._check(self._lib.dsm_get_class_form(self._h, C.byref(f)))
+        return f.value
 
     def schedule(self) -> list:
         """[{slot, warps_per_block, lanes, grid, chains}, ...]; empty for one launch over all chains."""

@@ -409,6 +409,8 @@ static int plan_single(dsm_sim* s) {
 
 int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float margin_sd) {
   s->classes.clear();
+  s->carved = false;
+  s->margin_sd = margin_sd;
   ++s->sched_version;
   const dsm_params& P = s->P;
   const int n = P.n_chains;
@@ -465,7 +467,7 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   if (!s->d_order) {
     CK(cudaMallocAsync((void**)&s->d_order, (size_t)n * sizeof(int), s->st));
     CK(cudaMallocAsync((void**)&s->d_defer, (size_t)n * sizeof(int), s->st));
-    CK(cudaMallocAsync((void**)&s->d_works, 8 * sizeof(unsigned int), s->st));
+    CK(cudaMallocAsync((void**)&s->d_works, 16 * sizeof(unsigned int), s->st));
     CK(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, s->prio));
     CK(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, s->prio));
     CK(cudaStreamCreateWithPriority(&s->side3, cudaStreamNonBlocking, s->prio));
@@ -533,6 +535,57 @@ int dsm::plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float 
   s->classes.push_back(Sm);
   s->blocks_per_sm = Sm.bps;
   s->grid = Sm.grid;
+  if (s->carve && !s->flow && sc.lanes == 16) {
+    LaunchCfg full = sc;
+    full.slot_cap = full_cap;
+    plan_carve(s, B, M, Sm, step_block_smem(full));
+  }
+  return DSM_OK;
+}
+
+// The carved form of a class plan: the large, middle and small classes run in
+// one launch of 4-warp blocks of 16-lane tiles.  Every block has the shared
+// memory of a full-occupancy block (8 slots of the largest size that keeps 4
+// blocks per SM, the register limit) and carves it into as many slots of its
+// class's size as fit (8 small, about 4 middle, 2 large).  Blocks are ordered large, middle,
+// small, so that the block scheduler starts the long chains first; each class
+// gets the blocks the concurrent launches would have (large: its tile count in
+// blocks, middle and small: up to a full persistent grid), and blocks beyond
+// the resident ones start as earlier blocks finish.  Not carved (the plan
+// stays as it is) when a class's slot does not fit the block.
+int dsm::plan_carve(dsm_sim* s, const SizeClass& B, const SizeClass& M, const SizeClass& Sm, size_t smem) {
+  const int bps = step_carved_blocks_per_sm(s->ck, smem);
+  if (bps < 1) return DSM_OK;
+  StepList l;
+  int blk = 0, k = 0;
+  auto add = [&](const SizeClass& c, int tiles_want) {
+    if (c.count <= 0) return true;
+    const int tiles = std::min(8, (int)(smem / step_slot_bytes(c.cfg.slot_cap, c.cfg.pmax)));
+    if (tiles < 1) return false;
+    const long long need = (c.count + tiles - 1) / tiles;
+    const long long want = tiles_want > 0 ? (tiles_want + tiles - 1) / tiles : (long long)bps * s->sm_count;
+    const int g = (int)std::max<long long>(1, std::min(need, want));
+    l.carve_blk[k] = blk;
+    l.carve_slot[k] = c.cfg.slot_cap;
+    l.carve_tiles[k] = tiles;
+    l.carve_first[k] = (int)c.first;
+    l.carve_count[k] = (int)c.count;
+    blk += g;
+    ++k;
+    return true;
+  };
+  // the large class's grid counts one-warp blocks, one chain each
+  if (!add(B, B.grid) || !add(M, 0) || !add(Sm, 0)) return DSM_OK;
+  l.carve_n = k;
+  l.carve_blk[k] = blk;
+  l.order = s->d_order;
+  l.defer = s->d_defer;
+  l.n_defer = s->d_works + 3;
+  l.carve_work = s->d_works + 8;
+  s->carve_list = l;
+  s->carve_grid = blk;
+  s->carve_smem = smem;
+  s->carved = true;
   return DSM_OK;
 }
 
@@ -615,6 +668,26 @@ extern "C" int dsm_set_schedule(dsm_sim* s, int32_t small_slot, int32_t large_gr
   return plan_classes(s, small_slot, large_grid, lanes, z_margin_sd);
 }
 
+extern "C" int dsm_set_class_form(dsm_sim* s, int32_t form) {
+  if (!s || !s->ready || (form != 0 && form != 1) || s->pending) return DSM_ERR_INVALID;
+  CK(cudaStreamSynchronize(s->st));
+  s->carve = form == 1;
+  if (s->classes.empty()) return DSM_OK;
+  // the same classes again, in the form asked for
+  int small = 0, grid = 0;
+  for (const SizeClass& k : s->classes) {
+    if (k.stream == 0) small = k.cfg.slot_cap;
+    if (k.stream == 1) grid = k.grid;
+  }
+  return plan_classes(s, small, grid, s->classes.back().cfg.lanes, s->margin_sd);
+}
+
+extern "C" int dsm_get_class_form(const dsm_sim* s, int32_t* form) {
+  if (!s || !form) return DSM_ERR_INVALID;
+  *form = s->carved ? 1 : 0;
+  return DSM_OK;
+}
+
 // ------------------------------------------------------------------ autotuner
 // Online: every candidate schedule runs one real window of the simulation
 // (trajectories do not depend on the schedule, so nothing is restored and no
@@ -623,7 +696,7 @@ extern "C" int dsm_set_schedule(dsm_sim* s, int32_t small_slot, int32_t large_gr
 extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* best_ms) {
   const dsm::NvtxRange nvtx_range("dsm_autotune");
   if (!s || !s->ready || !(window > 0.0) || s->pending) return DSM_ERR_INVALID;
-  struct Cand { int small, grid, lanes; };
+  struct Cand { int small, grid, lanes, carve = 0; };
   std::vector<Cand> cands;
   for (int lanes : {32, 16}) {
     if (!s->poly) cands.push_back({0, 0, lanes});  // one launch, full-capacity slots
@@ -650,14 +723,18 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
         if (k.stream == 1) g0 = k.grid;
       if (g0 == 0) { cands.push_back({sm, 0, lanes}); continue; }
       for (int g : {std::max(1, g0 / 2), g0, 2 * g0}) cands.push_back({sm, g, lanes});
+      // the carved one-launch form of the same classes
+      if (s->poly && lanes == 16 && !s->flow) cands.push_back({sm, g0, lanes, 1});
     }
   }
+  const bool carve0 = s->carve;
   int bi = -1;
   double brate = 0.0;
   float bms = 0.f;
   for (size_t i = 0; i < cands.size(); ++i) {
     const Cand& c = cands[i];
     s->cfg.lanes = c.lanes;
+    s->carve = c.carve != 0;
     int rc = (s->poly || c.small > 0) ? plan_classes(s, c.small, c.grid, c.lanes, 0.f) : plan_single(s);
     if (rc != DSM_OK) return rc;
     rc = sim_launch_window(s, s->t_done + window, -1);
@@ -668,6 +745,7 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
   }
   const Cand& b = cands[bi];
   s->cfg.lanes = b.lanes;
+  s->carve = b.carve != 0 || (carve0 && !s->poly);
   const int rc = (s->poly || b.small > 0) ? plan_classes(s, b.small, b.grid, b.lanes, 0.f) : plan_single(s);
   if (best) { best[0] = b.small; best[1] = b.grid; best[2] = b.lanes; best[3] = (int32_t)cands.size(); }
   if (best_ms) *best_ms = bms;
@@ -863,18 +941,10 @@ static int64_t window_watchdog(const dsm_sim* s, double dt_tau) {
 
 // The step launch(es) of one window on s->st (the descriptor already holds
 // the window): one launch over all chains, or the size classes
-static int enqueue_step(dsm_sim* s) {
-  if (s->classes.empty()) {
-    CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
-    CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->ck, s->cfg,
-                   s->d_abort, s->d_status, s->grid, s->st));
-    return DSM_OK;
-  }
-  // size classes: large-slot chains on the side stream first, then the
+static int enqueue_classes(dsm_sim* s) {
+  // concurrent form: large-slot chains on the side stream first, then the
   // middle class on the second side stream (their blocks are placed first),
-  // small-slot chains on the main stream; then the chains that outgrew their
-  // slot, in slots of the ensemble's full capacity
-  CK(cudaMemsetAsync(s->d_works, 0, 8 * sizeof(unsigned int), s->st));
+  // small-slot chains on the main stream, the huge class on the third
   CK(cudaEventRecord(s->ev_fork, s->st));
   CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
   CK(cudaStreamWaitEvent(s->side2, s->ev_fork, 0));
@@ -895,6 +965,41 @@ static int enqueue_step(dsm_sim* s) {
   CK(cudaStreamWaitEvent(s->st, s->ev_join, 0));
   CK(cudaStreamWaitEvent(s->st, s->ev_join2, 0));
   CK(cudaStreamWaitEvent(s->st, s->ev_join3, 0));
+  return DSM_OK;
+}
+
+static int enqueue_carved(dsm_sim* s) {
+  // carved form: the huge class on its stream, the other classes in one
+  // launch on the main stream
+  CK(cudaEventRecord(s->ev_fork, s->st));
+  CK(cudaStreamWaitEvent(s->side3, s->ev_fork, 0));
+  for (const SizeClass& k : s->classes) {
+    if (k.stream != 3) continue;
+    StepList l;
+    l.order = s->d_order + k.first;
+    l.defer = s->d_defer;
+    l.n_defer = s->d_works + 3;
+    CK(launch_step(s->d_ens, 1, s->d_prefix, k.count, s->d_works + 5, s->flow, s->ck, k.cfg, s->d_abort,
+                   s->d_status, k.grid, s->side3, l));
+  }
+  CK(launch_step_carved(s->d_ens, s->d_prefix, s->ck, s->cfg.pmax, s->carve_smem, s->d_abort, s->d_status,
+                        s->carve_grid, s->st, s->carve_list));
+  CK(cudaEventRecord(s->ev_join3, s->side3));
+  CK(cudaStreamWaitEvent(s->st, s->ev_join3, 0));
+  return DSM_OK;
+}
+
+static int enqueue_step(dsm_sim* s) {
+  if (s->classes.empty()) {
+    CK(cudaMemsetAsync(s->d_work, 0, sizeof(unsigned int), s->st));
+    CK(launch_step(s->d_ens, 1, s->d_prefix, (long long)s->P.n_chains, s->d_work, s->flow, s->ck, s->cfg,
+                   s->d_abort, s->d_status, s->grid, s->st));
+    return DSM_OK;
+  }
+  CK(cudaMemsetAsync(s->d_works, 0, 16 * sizeof(unsigned int), s->st));
+  const int rc = s->carved ? enqueue_carved(s) : enqueue_classes(s);
+  if (rc != DSM_OK) return rc;
+  // then the chains that outgrew their slot, in slots of the ensemble's full capacity
   StepList l;
   l.order = s->d_defer;
   l.dyn_total = s->d_works + 3;

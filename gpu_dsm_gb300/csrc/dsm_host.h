@@ -126,7 +126,17 @@ struct dsm_sim {
   dsm::SizeClass cleanup;
   int* d_order = nullptr;
   int* d_defer = nullptr;
-  unsigned int* d_works = nullptr;  // [0] small, [1] large, [2] cleanup, [3] deferred count, [4] middle, [5] huge
+  unsigned int* d_works = nullptr;  // [0] small, [1] large, [2] cleanup, [3] deferred count, [4] middle, [5] huge,
+                                    // [8 ..) the classes of a carved launch
+  // carved form (dsm_set_class_form): the large, middle and small classes in
+  // one launch of 16-lane tiles whose blocks carve the same shared memory into
+  // per-class slot counts; the huge class (if any) beside it on its stream
+  bool carve = false;       // asked for
+  bool carved = false;      // the current plan is carved
+  float margin_sd = 0.f;    // strand-count margin of the current class plan (0: 5 sd)
+  dsm::StepList carve_list;
+  int carve_grid = 0;
+  size_t carve_smem = 0;
   cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_join3 = nullptr;
   int prio = 0;  // CUDA stream priority of st and side
@@ -146,6 +156,9 @@ int sim_setup(dsm_sim* s);
 // Size-class plan of a polydisperse ensemble; small_cap / big_grid / lanes
 // <= 0 pick the defaults (full-occupancy small slot, large-class grid by work share)
 int plan_classes(dsm_sim* s, int small_cap, int big_grid, int lanes, float margin_sd);
+// carved form of a class plan (dsm_set_class_form) in blocks of block_smem
+// bytes; leaves the plan as it is if a class's slot does not fit the block
+int plan_carve(dsm_sim* s, const SizeClass& big, const SizeClass& mid, const SizeClass& small, size_t block_smem);
 int sim_launch_window(dsm_sim* s, double t_end, int64_t step_limit);
 int sim_finish_window(dsm_sim* s, uint64_t* events);
 }  // namespace dsm

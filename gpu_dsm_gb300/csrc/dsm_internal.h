@@ -95,6 +95,8 @@ struct EnsDev {
   int32_t n_win, win_stride;
 };
 
+constexpr int kCarveMax = 4;  // size classes of one carved launch
+
 struct LaunchCfg {
   int warps_per_block;
   int slot_cap;        // strands per SMEM slot (max cap of the ensembles launched)
@@ -115,9 +117,28 @@ struct StepList {
   const unsigned int* dyn_total = nullptr;
   int* defer = nullptr;
   unsigned int* n_defer = nullptr;
+  // Carved launch (k_step_carved, carve_n > 0): several size classes in one
+  // launch.  Blocks
+  // [carve_blk[k], carve_blk[k+1]) run class k: the block's shared memory
+  // holds carve_tiles[k] slots of carve_slot[k] strands (its other tiles stay
+  // idle), and its tiles take the items order[carve_first[k] ..
+  // carve_first[k] + carve_count[k]) from the work counter carve_work + k.
+  int carve_n = 0;
+  int carve_blk[kCarveMax + 1] = {};
+  int carve_slot[kCarveMax] = {};
+  int carve_tiles[kCarveMax] = {};
+  int carve_first[kCarveMax] = {};
+  int carve_count[kCarveMax] = {};
+  unsigned int* carve_work = nullptr;
 };
 
 // kernels (dsm_kernels.cu)
+// carved launch of equilibrium size classes in 16-lane tiles (lst.carve_*),
+// block shared memory smem_bytes; resident blocks per SM of that kernel
+cudaError_t launch_step_carved(const EnsDev* d_ens, const long long* d_prefix, int corr, int pmax, size_t smem_bytes,
+                               const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
+                               const StepList& lst);
+int step_carved_blocks_per_sm(int corr, size_t smem_bytes);
 cudaError_t launch_init(const EnsDev* d_ens, const EnsDev& h_ens, int slot_cap, cudaStream_t st);
 // zero the slots a chain does not use (strands >= Z, entanglements >= Z-1)
 cudaError_t launch_clear_tail(float4* d_QN, float* d_tau, const ChainState* d_cs, int n_chains, int cap,

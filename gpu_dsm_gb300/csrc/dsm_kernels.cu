@@ -921,18 +921,21 @@ __device__ unsigned long long g_phase[32];
 // ------------------------------------------------------------------ step kernel
 // CK: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD (compile
 // time, so that the stress kernel carries no MSD code)
-template <bool FLOW, int CK, int W, int MB>
-__global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens, int n_ens,
-                                                 const long long* __restrict__ prefix, long long total,
-                                                 unsigned int* work, int slot_cap, int pmax,
-                                                 const volatile int* abort_flag, int* status, StepList lst) {
+// The persistent chain loop of a step launch: tiles of W lanes pull items
+// (chains) order[0 .. n_items) from *work and run each in a slot of slot_cap
+// strands.  Inlined into k_step, whose arguments it takes as they are, and
+// into k_step_carved, which first picks its block's size class.
+template <bool FLOW, int CK, int W>
+__device__ __forceinline__ void step_chains(const EnsDev* __restrict__ ens, int n_ens,
+                                            const long long* __restrict__ prefix, long long n_items,
+                                            const int* order, unsigned int* work, int slot_cap, int pmax,
+                                            const volatile int* abort_flag, int* status, const StepList& lst) {
   constexpr bool CORR = CK != 0, MSD = CK == 2;
   extern __shared__ __align__(16) unsigned char smem[];
   const Tile<W> t;
   const int lane = t.lane;
   const int tib = threadIdx.x / W;
   Slot sl = make_slot(smem + (size_t)tib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
-  const long long n_items = lst.dyn_total != nullptr ? (long long)*lst.dyn_total : total;
 
   for (;;) {
     unsigned int item = 0;
@@ -943,7 +946,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (lane == 0) atomicOr(status, 1);
       break;
     }
-    const long long gid = lst.order != nullptr ? (long long)lst.order[item] : (long long)item;
+    const long long gid = order != nullptr ? (long long)order[item] : (long long)item;
     int e = 0;
     while (e + 1 < n_ens && prefix[e + 1] <= gid) ++e;
     const EnsDev& E = ens[e];
@@ -1295,6 +1298,43 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
     DSM_PHASE_FLUSH();
     t.sync();
   }
+}
+
+template <bool FLOW, int CK, int W, int MB>
+__global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens, int n_ens,
+                                                 const long long* __restrict__ prefix, long long total,
+                                                 unsigned int* work, int slot_cap, int pmax,
+                                                 const volatile int* abort_flag, int* status, StepList lst) {
+  step_chains<FLOW, CK, W>(ens, n_ens, prefix, lst.dyn_total != nullptr ? (long long)*lst.dyn_total : total,
+                           lst.order, work, slot_cap, pmax, abort_flag, status, lst);
+}
+
+// Several size classes in one launch (StepList::carve_*): the block finds its
+// class among the block ranges and carves its shared memory into that class's
+// slots.  Tiles beyond the class's slot count leave at once (the chain loop
+// has no block-wide barrier).  The class fields are read with static indices
+// only, so they stay in the parameter space.
+template <bool FLOW, int CK, int W, int MB>
+__global__ void __launch_bounds__(128, MB) k_step_carved(const EnsDev* __restrict__ ens, int n_ens,
+                                                        const long long* __restrict__ prefix, long long total,
+                                                        unsigned int* work, int slot_cap, int pmax,
+                                                        const volatile int* abort_flag, int* status, StepList lst) {
+  int k = 0;
+#pragma unroll
+  for (int i = 1; i < kCarveMax; ++i)
+    if (i < lst.carve_n && (int)blockIdx.x >= lst.carve_blk[i]) k = i;
+  int cap = 0, tiles = 0, first = 0, count = 0;
+#pragma unroll
+  for (int i = 0; i < kCarveMax; ++i)
+    if (i == k) {
+      cap = lst.carve_slot[i];
+      tiles = lst.carve_tiles[i];
+      first = lst.carve_first[i];
+      count = lst.carve_count[i];
+    }
+  if ((int)(threadIdx.x / W) >= tiles) return;
+  step_chains<FLOW, CK, W>(ens, n_ens, prefix, count, lst.order + first, lst.carve_work + k, cap, pmax, abort_flag,
+                           status, lst);
 }
 
 // ------------------------------------------------------------------ initialiser
@@ -1675,6 +1715,34 @@ static StepChoice choose_step(bool flow, int ck, const LaunchCfg& cfg) {
 }
 
 int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg) { return choose_step(flow, corr, cfg).bps; }
+
+// carved launches: equilibrium kinds, 16-lane tiles, the standard build
+template <int CK>
+static void* carved_fn() { return (void*)k_step_carved<false, CK, 16, DSM_MINB>; }
+static void* pick_carved(int ck) { return ck == 0 ? carved_fn<0>() : ck == 2 ? carved_fn<2>() : carved_fn<1>(); }
+
+int step_carved_blocks_per_sm(int corr, size_t smem_bytes) {
+  void* fn = pick_carved(corr);
+  if (prep_step(fn, smem_bytes) != cudaSuccess) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem_bytes) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_step_carved(const EnsDev* d_ens, const long long* d_prefix, int corr, int pmax, size_t smem_bytes,
+                               const volatile int* abort_flag, int* d_status, int grid, cudaStream_t st,
+                               const StepList& lst) {
+  void* fn = pick_carved(corr);
+  cudaError_t err = prep_step(fn, smem_bytes);
+  if (err != cudaSuccess) return err;
+  int n_ens = 1, slot_cap = 0;
+  long long total = 0;
+  unsigned int* work = nullptr;
+  StepList l = lst;
+  void* args[] = {(void*)&d_ens, (void*)&n_ens, (void*)&d_prefix, (void*)&total, (void*)&work,
+                  (void*)&slot_cap, (void*)&pmax, (void*)&abort_flag, (void*)&d_status, (void*)&l};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(128), args, smem_bytes, st);
+}
 
 size_t step_block_smem(const LaunchCfg& cfg) { return step_smem(cfg); }
 

@@ -216,10 +216,24 @@ int dsm_set_schedule(dsm_sim* sim, int32_t small_slot, int32_t large_grid, int32
 #define DSM_SCHEDULE_INFO 25
 int dsm_get_schedule(const dsm_sim* sim, int32_t* n_classes, int32_t* info);
 
+/* How size classes launch (equilibrium ensembles whose small class runs 16
+ * lanes per chain).  form 0 (default): each class its own persistent launch,
+ * the four launched concurrently on four streams.  form 1: the large, middle
+ * and small classes in one launch whose blocks carve the same shared memory
+ * into per-class slot counts (8 small, about 4 middle, 2 large slots per
+ * block, all in 16-lane tiles), the huge class beside it on its stream.
+ * Trajectories do not depend on the form.  The plan is made again; a form
+ * that does not apply leaves the concurrent launches.  dsm_get_class_form
+ * reports the form of the current plan. */
+int dsm_set_class_form(dsm_sim* sim, int32_t form);
+int dsm_get_class_form(const dsm_sim* sim, int32_t* form);
+
 /* Autotuner (online): runs one real window of `window` tau_K with each
  * candidate schedule (lanes per chain 32/16; the small slot at 4/3/2 blocks per
  * SM when the strand-count bound fits it; for polydisperse ensembles the
- * large-class grid at 1/2, 1 and 2 times its default) and keeps the one with
+ * large-class grid at 1/2, 1 and 2 times its default, and with 16 lanes each
+ * small slot also in the carved one-launch form of dsm_set_class_form) and
+ * keeps the one with
  * the most kMC events per kernel millisecond.  The ensemble advances by
  * candidates x window; its trajectory is the one it would have had without
  * the autotuner.  best (may be NULL) receives {small_slot, large_grid, lanes,

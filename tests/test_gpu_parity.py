@@ -320,6 +320,43 @@ def test_size_classes_bitexact(dsm_mod, oracle_mod, small_slot, margin, kappa, l
         assert np.all(np.abs(sg[:6] - so[:6]) <= 1e-4 * scale + 1e-6)
 
 
+@pytest.mark.parametrize("corr", [False, True])
+def test_carved_classes_bitexact(dsm_mod, oracle_mod, corr):
+    """The carved one-launch form (dsm_set_class_form(1)): large, middle and
+    small classes in one launch whose blocks carve their shared memory per
+    class, the longest chains beside it, the overflow launch after it.  Same
+    trajectories as the oracle (and so as the concurrent launches), with and
+    without the G(t) correlator."""
+    nkc = _lognormal_nk(400, 21, 120, 0.9, 10, 1200)
+    kw = dict(sync_dt=1.0, t_end=1.0e4, corr_p=16, corr_m=2) if corr else {}
+    g, o = pair(dsm_mod, oracle_mod, nk=int(nkc.max()), n=400, seed=17, nk_chain=nkc, corr=corr, **kw)
+    g.set_schedule(small_slot=40, z_margin_sd=0.01, lanes=16)
+    assert g.class_form() == 0
+    g.set_class_form(1)
+    assert g.class_form() == 1
+    sch = g.schedule()
+    assert sum(k["chains"] for k in sch[:-1]) == 400
+    g.init_equilibrium()
+    o.init_equilibrium()
+    deferred = 0
+    for t in (4.0, 10.0):
+        g.advance(t)
+        o.run(t)
+        deferred += g.window_stats()["deferred"]
+    assert deferred > 0  # chains outgrew their carved slot and finished in the overflow launch
+    st = gpu_state(g)
+    assert np.all(st["QN"][:, :, 3].sum(axis=1) == nkc)
+    assert_bitexact(st, o.get_state(), what="carved classes")
+    if corr:
+        gs, gc = g.gt_raw()
+        os_, oc = o.gt_raw()
+        assert np.array_equal(gc, oc)
+        m = oc > 0
+        assert np.max(np.abs(gs[m] - os_[m])) <= 1e-5 * np.abs(os_[m]).max()
+    g.set_class_form(0)
+    assert g.class_form() == 0
+
+
 def test_autotune_keeps_trajectory(dsm_mod, oracle_mod):
     """The autotuner's trial windows are ordinary windows under different
     schedules: the run stays on the oracle's trajectory."""
