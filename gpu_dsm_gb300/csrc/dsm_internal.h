@@ -117,7 +117,7 @@ struct StepList {
   const unsigned int* dyn_total = nullptr;
   int* defer = nullptr;
   unsigned int* n_defer = nullptr;
-  // Carved launch (k_step_carved, carve_n > 0): several size classes in one
+  // Carved launch (k_step with CARVED, carve_n > 0): several size classes in one
   // launch.  Blocks
   // [carve_blk[k], carve_blk[k+1]) run class k: the block's shared memory
   // holds carve_tiles[k] slots of carve_slot[k] strands (its other tiles stay

@@ -921,20 +921,44 @@ __device__ unsigned long long g_phase[32];
 // ------------------------------------------------------------------ step kernel
 // CK: correlator kind, 0 none, 1 stress G(t), 2 centre-of-mass MSD (compile
 // time, so that the stress kernel carries no MSD code)
-// The persistent chain loop of a step launch: tiles of W lanes pull items
-// (chains) order[0 .. n_items) from *work and run each in a slot of slot_cap
-// strands.  Inlined into k_step, whose arguments it takes as they are, and
-// into k_step_carved, which first picks its block's size class.
-template <bool FLOW, int CK, int W>
-__device__ __forceinline__ void step_chains(const EnsDev* __restrict__ ens, int n_ens,
-                                            const long long* __restrict__ prefix, long long n_items,
-                                            const int* order, unsigned int* work, int slot_cap, int pmax,
-                                            const volatile int* abort_flag, int* status, const StepList& lst) {
+// Step kernel: persistent tiles of W lanes pull items (chains) order[0 ..
+// n_items) from *work and run each in a slot of slot_cap strands; chains that
+// outgrow it are appended to lst.defer (count *lst.n_defer).
+// CARVED: several size classes in one launch (StepList::carve_*).  The block
+// finds its class among the block ranges and carves its shared memory into
+// that class's slots; tiles beyond the class's slot count leave at once (the
+// chain loop has no block-wide barrier).  The class fields are read with
+// static indices only, so they stay in the parameter space.
+template <bool FLOW, int CK, int W, int MB, bool CARVED>
+__global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens, int n_ens,
+                                                 const long long* __restrict__ prefix, long long total,
+                                                 unsigned int* work, int slot_cap, int pmax,
+                                                 const volatile int* abort_flag, int* status, StepList lst) {
   constexpr bool CORR = CK != 0, MSD = CK == 2;
   extern __shared__ __align__(16) unsigned char smem[];
   const Tile<W> t;
   const int lane = t.lane;
   const int tib = threadIdx.x / W;
+  long long n_items = lst.dyn_total != nullptr ? (long long)*lst.dyn_total : total;
+  const int* order = lst.order;
+  if constexpr (CARVED) {
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < kCarveMax; ++i)
+      if (i < lst.carve_n && (int)blockIdx.x >= lst.carve_blk[i]) k = i;
+    int tiles = 0, first = 0;
+#pragma unroll
+    for (int i = 0; i < kCarveMax; ++i)
+      if (i == k) {
+        slot_cap = lst.carve_slot[i];
+        tiles = lst.carve_tiles[i];
+        first = lst.carve_first[i];
+        n_items = lst.carve_count[i];
+      }
+    if (tib >= tiles) return;
+    order += first;
+    work = lst.carve_work + k;
+  }
   Slot sl = make_slot(smem + (size_t)tib * step_slot_bytes(slot_cap, pmax), slot_cap, pmax);
 
   for (;;) {
@@ -1300,43 +1324,6 @@ __device__ __forceinline__ void step_chains(const EnsDev* __restrict__ ens, int 
   }
 }
 
-template <bool FLOW, int CK, int W, int MB>
-__global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens, int n_ens,
-                                                 const long long* __restrict__ prefix, long long total,
-                                                 unsigned int* work, int slot_cap, int pmax,
-                                                 const volatile int* abort_flag, int* status, StepList lst) {
-  step_chains<FLOW, CK, W>(ens, n_ens, prefix, lst.dyn_total != nullptr ? (long long)*lst.dyn_total : total,
-                           lst.order, work, slot_cap, pmax, abort_flag, status, lst);
-}
-
-// Several size classes in one launch (StepList::carve_*): the block finds its
-// class among the block ranges and carves its shared memory into that class's
-// slots.  Tiles beyond the class's slot count leave at once (the chain loop
-// has no block-wide barrier).  The class fields are read with static indices
-// only, so they stay in the parameter space.
-template <bool FLOW, int CK, int W, int MB>
-__global__ void __launch_bounds__(128, MB) k_step_carved(const EnsDev* __restrict__ ens, int n_ens,
-                                                        const long long* __restrict__ prefix, long long total,
-                                                        unsigned int* work, int slot_cap, int pmax,
-                                                        const volatile int* abort_flag, int* status, StepList lst) {
-  int k = 0;
-#pragma unroll
-  for (int i = 1; i < kCarveMax; ++i)
-    if (i < lst.carve_n && (int)blockIdx.x >= lst.carve_blk[i]) k = i;
-  int cap = 0, tiles = 0, first = 0, count = 0;
-#pragma unroll
-  for (int i = 0; i < kCarveMax; ++i)
-    if (i == k) {
-      cap = lst.carve_slot[i];
-      tiles = lst.carve_tiles[i];
-      first = lst.carve_first[i];
-      count = lst.carve_count[i];
-    }
-  if ((int)(threadIdx.x / W) >= tiles) return;
-  step_chains<FLOW, CK, W>(ens, n_ens, prefix, count, lst.order + first, lst.carve_work + k, cap, pmax, abort_flag,
-                           status, lst);
-}
-
 // ------------------------------------------------------------------ initialiser
 // Equilibrium chains (role of chain.cu:199-283): each of the NK-1 bonds between
 // Kuhn steps carries an entanglement with probability 1/(1+beta), which gives
@@ -1613,7 +1600,7 @@ __global__ void k_window_begin(EnsDev* ens, const long long* __restrict__ d_win,
 
 // ------------------------------------------------------------------ launchers
 template <bool FLOW, int CK, int W, int MB>
-static void* step_fn() { return (void*)k_step<FLOW, CK, W, MB>; }
+static void* step_fn() { return (void*)k_step<FLOW, CK, W, MB, false>; }
 
 // hi: the variant compiled for DSM_MINB_HI blocks per SM
 template <int W>
@@ -1718,7 +1705,7 @@ int step_max_blocks_per_sm(bool flow, int corr, const LaunchCfg& cfg) { return c
 
 // carved launches: equilibrium kinds, 16-lane tiles, the standard build
 template <int CK>
-static void* carved_fn() { return (void*)k_step_carved<false, CK, 16, DSM_MINB>; }
+static void* carved_fn() { return (void*)k_step<false, CK, 16, DSM_MINB, true>; }
 static void* pick_carved(int ck) { return ck == 0 ? carved_fn<0>() : ck == 2 ? carved_fn<2>() : carved_fn<1>(); }
 
 int step_carved_blocks_per_sm(int corr, size_t smem_bytes) {
