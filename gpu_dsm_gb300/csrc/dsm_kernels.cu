@@ -1177,8 +1177,11 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (jj < np) {
         // inside pair j: CD destruction, shift +1, shift -1, CD creation
         j = jj;
-        const unsigned long long q0 = E.cd_flag ? quant(sl.T[j], sf) : 0ull;
-        const unsigned long long q3 = E.cd_flag ? quant(__ldg(&E.NE[sl.N[j]]).w, sf) : 0ull;
+        // the CD components selected as floats (0 without CD) and always quantised
+        const bool cd = E.cd_flag != 0;
+        const float tq = sl.T[j], eq = __ldg(&E.NE[sl.N[j]]).w;
+        const unsigned long long q0 = quant(cd ? tq : 0.0f, sf);
+        const unsigned long long q3 = quant(cd ? eq : 0.0f, sf);
         const unsigned long long lim = sl.R[j] - q3;
         if (r < q0) evn = CDD;
         else if (r >= lim) { evn = CDC_MID; rem = r - lim; wsel = q3; }
