@@ -50,7 +50,6 @@ constexpr Probe kProbes[] = {
     {"fp64 add (dependent)", ND},
     {"fp64 fma (dependent)", ND},
     {"fp64 div_rn (+fp64 add)", ND},
-    {"fp64 -> u64 -> fp64 conversions (+int mul, add)", ND},
 };
 constexpr int kNumProbes = sizeof(kProbes) / sizeof(kProbes[0]);
 
@@ -116,7 +115,6 @@ __global__ void probe(const int* __restrict__ gtab, long long* out, float seedf,
   PROBE_ALL(for (int i = 0; i < ND; ++i) dd = __dadd_rn(dd, 1.0));
   PROBE_ALL(for (int i = 0; i < ND; ++i) dd = __fma_rn(dd, 0.999, 1.0));
   PROBE_ALL(for (int i = 0; i < ND; ++i) dd = __ddiv_rn(1.0, __dadd_rn(dd, 1.5)));
-  PROBE_ALL(for (int i = 0; i < ND; ++i) dd = __ull2double_rn(__double2ull_rn(dd) * 3ull + 1ull));
 #undef PROBE_ALL
 #undef PROBE
   // keep every chain live
