@@ -765,6 +765,44 @@ __device__ __forceinline__ void corr_samples(const EnsDev& E, Slot& sl, int Z, i
 }
 
 // ------------------------------------------------------------------ creation events
+// Position of a CD creation inside a strand of N1 Kuhn steps
+// (ensemble_kernel.cu:386: newn = floor(0.5 + pr (N1 - 2) / w) + 1) on the
+// quantised values r < w: x = floor((2 r (N1 - 2) + w) / (2 w)), exactly.  An
+// FP32 estimate from the leading 24 bits of r and w (32-bit conversions only)
+// is corrected with 128-bit integer products, so no FP64 operation is needed
+// (sm_103a's FP64 divide costs about 430 cycles).  x stays in [0, N1 - 2]; the
+// estimate is within one of it, and each correction loop moves x towards it.
+__device__ __forceinline__ int split_pos(unsigned long long r, unsigned long long w, int N1) {
+  const unsigned m = (unsigned)max(N1 - 2, 0);
+  if (m == 0u || w == 0ull) return 0;
+  // numerator 2 r m + w as nh:nl
+  unsigned long long nl = r * m, nh = __umul64hi(r, (unsigned long long)m);
+  nh = (nh << 1) | (nl >> 63);
+  nl <<= 1;
+  nl += w;
+  nh += (nl < w) ? 1ull : 0ull;
+  const unsigned long long d = w << 1;  // w < 2^62
+  const int sh = max(0, 40 - __clzll((long long)w));  // w >> sh < 2^24, r >> sh <= w >> sh
+  const float ratio = __fdiv_rn((float)(unsigned)(r >> sh), (float)(unsigned)(w >> sh));
+  int q = (int)__fmaf_rn(ratio, (float)m, 0.5f);
+  q = min(max(q, 0), (int)m);
+  // q d as ph:pl; step q down while q d > num, then up while (q + 1) d <= num
+  unsigned long long pl = (unsigned long long)q * d, ph = __umul64hi((unsigned long long)q, d);
+  while (ph > nh || (ph == nh && pl > nl)) {
+    ph -= (pl < d) ? 1ull : 0ull;
+    pl -= d;
+    --q;
+  }
+  for (;;) {
+    const unsigned long long l2 = pl + d, h2 = ph + ((l2 < pl) ? 1ull : 0ull);
+    if (h2 > nh || (h2 == nh && l2 > nl)) break;
+    pl = l2;
+    ph = h2;
+    ++q;
+  }
+  return q;
+}
+
 // Apply a creation (CD inside strand j / CD at the tail / SD at head or tail):
 // returns newn and the pairs to recompute (up0, upn).
 template <int W>
@@ -775,9 +813,7 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
   int newn = 0;
   if (evn == CDC_MID || evn == CDC_TAIL) {
     const int N1 = (evn == CDC_MID) ? sl.N[j] : sl.N[Z - 1];
-    const double x = floor(__dadd_rn(0.5, __ddiv_rn(__dmul_rn(__ull2double_rn(rem), (double)(N1 - 2)),
-                                                  __ull2double_rn(wsel))));
-    newn = (int)x + 1;
+    newn = split_pos(rem, wsel, N1) + 1;
     newn = max(1, min(N1 - 1, newn));
   }
   const U4 gr = rng_at(E, P_CREATE, step, (uint32_t)(step >> 32), (uint32_t)c);

@@ -669,6 +669,19 @@ static inline float pow2f(int s) {  // 2^s, s in [-126, 127]
 
 // One kMC event of a chain in FP32-mirror arithmetic.  Returns false when the
 // chain stalls (the event is then not applied).
+// Position of a CD creation inside a strand of N1 Kuhn steps
+// (common/ensemble_kernel.cu:386: newn = floor(0.5 + pr (N1 - 2) / w) + 1) on the
+// quantised values rem < wsel: x = floor((2 rem (N1 - 2) + wsel) / (2 wsel)),
+// exactly, in 128-bit integers (the sm_103a kernel gets the same x from an FP32
+// estimate and an exact integer correction).
+static int split_exact(uint64_t rem, uint64_t wsel, int N1) {
+  const uint64_t m = (uint64_t)std::max(N1 - 2, 0);
+  if (m == 0 || wsel == 0) return 0;
+  const unsigned __int128 num = (unsigned __int128)rem * m * 2u + wsel;
+  const unsigned __int128 den = (unsigned __int128)wsel * 2u;
+  return (int)(num / den);
+}
+
 bool step_mirror(const Ensemble& E, Chain<float>& c, uint32_t ci) {
   const int Z = c.Z;
   const int cd = E.P.cd_flag;
@@ -753,8 +766,7 @@ bool step_mirror(const Ensemble& E, Chain<float>& c, uint32_t ci) {
     int newn = 0;
     if (ev == CDC_MID || ev == CDC_TAIL) {
       const int N1 = (ev == CDC_MID) ? c.N[j] : c.N[Z - 1];
-      const double x = std::floor(0.5 + (double)rem * (double)(N1 - 2) / (double)wsel);
-      newn = (int)x + 1;
+      newn = split_exact(rem, wsel, N1) + 1;
       if (newn < 1) newn = 1;
       if (newn > N1 - 1) newn = N1 - 1;
     }
@@ -1599,6 +1611,9 @@ int orc_ref_params(void* h, float* prefact, double* law) {
   for (int q = 0; q < 9; ++q) law[q] = v[q];
   return 0;
 }
+
+// the CD creation split of the FP32 mirror (for the tests)
+int orc_split(uint64_t rem, uint64_t wsel, int n1) { return split_exact(rem, wsel, n1); }
 
 int orc_num_threads(void) {
 #ifdef _OPENMP

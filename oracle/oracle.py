@@ -68,6 +68,8 @@ def lib() -> C.CDLL:
         L.orc_gt.argtypes = [vp, vp, vp]
         L.orc_pcd.argtypes = [C.c_double, C.c_double, vp, vp]
         L.orc_philox.argtypes = [vp, vp, vp]
+        L.orc_split.argtypes = [C.c_uint64, C.c_uint64, C.c_int]
+        L.orc_split.restype = C.c_int
         L.orc_math.argtypes = [C.c_int, vp, vp, vp, C.c_int]
         L.orc_tau_sample.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, vp, vp, C.c_int]
         L.orc_num_threads.restype = C.c_int
