@@ -1135,24 +1135,31 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (FLOW) {
         S = full_rates_body<true, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
-      } else if (ends_dirty) {
-        int over = 0;
-        if (lane < NEND) {
-          const float ev = end_comp(E, lane, Z, sl.N, wz1);
-          over = (fexp(ev) + S > LIMIT_E) ? 4 : 0;
-          sl.R[np + lane] = quant(ev, pow2f(S));
+      } else if (ends_dirty | ((pend & 4) != 0)) {
+        // one branch in the common case (neither): the chain-end refresh, or
+        // the full pass that a pending scale overflow asks for
+        if (ends_dirty) {
+          int over = 0;
+          if (lane < NEND) {
+            const float ev = end_comp(E, lane, Z, sl.N, wz1);
+            over = (fexp(ev) + S > LIMIT_E) ? 4 : 0;
+            sl.R[np + lane] = quant(ev, pow2f(S));
+          }
+          pend |= t.or_(over);
+          if (pend & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
+          ends_dirty = false;
+          rescan = true;
+          t.sync();
+        } else {
+          S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
+          rescan = true;
         }
-        pend |= t.or_(over);
-        if (pend & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
-        ends_dirty = false;
-        rescan = true;
-        t.sync();
-      } else if (pend & 4) {
-        S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
-        rescan = true;
       }
-      if (pend & 1) { stall = ST_NAN; dt_prev = 0.0f; break; }
-      if (pend & 2) { stall = ST_INF; dt_prev = 0.0f; break; }
+      if (pend & 3) {
+        stall = (pend & 1) ? ST_NAN : ST_INF;
+        dt_prev = 0.0f;
+        break;
+      }
       DSM_PHASE(1);  // chain-end rates, rate passes
       const float sf = pow2f(S);
       // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
