@@ -184,8 +184,10 @@ def fp64_accuracy(args, device: int, shear: dict | None, serve: dict | None) -> 
     event), compared with the GPU's results against the FP64 estimate's own
     chain-to-chain error (oracle.gt_error_vs_fp64):
       headline  G(t) of chains 30000-30511 of the headline ensemble over 500 tau_K;
-      shear     sigma_xy of 256 chains at Wi 10 and 100 (N_K=100) at five
-                outputs, deviation in units of sigma;
+      shear     sigma_xy of 256 chains at Wi 0.1, 1, 10 and 100 (N_K=100) at
+                five outputs, deviation in units of sigma; with the FP64
+                sigma_xy at the last output and its standard error, for 256
+                chains and scaled to the 32768 chains per Wi of the timed leg;
       serve     G(t) of the two cheapest G(t) requests of the served stream,
                 re-run on the CPU with the request's parameters."""
     import gpu_dsm_gb300 as dsm
@@ -206,7 +208,7 @@ def fp64_accuracy(args, device: int, shear: dict | None, serve: dict | None) -> 
     if shear is not None and "failed" not in shear:
         tau_d = dsm.pcd(1.0, 100)["tau_d"]
         rows = []
-        for wi in (10.0, 100.0):
+        for wi in (0.1, 1.0, 10.0, 100.0):
             kap = (0.0, wi / tau_d, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
             skw = dict(nk=100, n_chains=256, kappa=kap, seed=4, stream=3)
             ge = dsm.Ensemble(sync_dt=100.0, t_end=5.0e5, device=device, **skw)
@@ -225,10 +227,14 @@ def fp64_accuracy(args, device: int, shear: dict | None, serve: dict | None) -> 
                 per = -3.0 * np.where(idx, q[:, :, 0] * q[:, :, 1] / np.where(idx, q[:, :, 3], 1.0), 0.0).sum(axis=1)
                 worst = max(worst, abs(sg - sf) / (per.std(ddof=1) / math.sqrt(len(per))))
             ge.close()
-            rows.append({"wi": wi, "dev_sigma": worst})
+            sd = float(per.std(ddof=1))
+            rows.append({"wi": wi, "dev_sigma": worst, "sigma_xy_fp64_at_500": float(sf),
+                         "se_256_chains": sd / math.sqrt(len(per)),
+                         "se_at_timed_leg_chains": sd / math.sqrt(args.shear_chains)})
         shear["stress_err_vs_fp64"] = {"rows": rows, "sample": "256 chains, N_K=100, outputs every 100 tau_K "
                                        "to 500 tau_K; |sigma_xy(GPU) - sigma_xy(FP64)| / sigma of the FP64 "
-                                       "estimate; consistent when below 3 sqrt(2)"}
+                                       "estimate; consistent when below 3 sqrt(2). se_at_timed_leg_chains: "
+                                       "the chain-to-chain error of sigma_xy_per_window in the timed leg"}
         out["shear"] = shear["stress_err_vs_fp64"]
     if serve is not None and serve.get("_samples"):
         rows = []
