@@ -823,20 +823,23 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
   const PcdDev pp = partner_pcd(E, w3, evn == CDC_MID || evn == CDC_TAIL);
   const float u = u01(w2);
   const float trate = E.cd_flag ? ((evn == CDC_MID || evn == CDC_TAIL) ? rate_f_dt(pp, u) : rate_f_t(pp, u)) : 0.0f;
+  // The new strands are computed by every lane before the strands move (their
+  // latency overlaps the move), and lane 0 stores them after it.
   if (evn == CDC_MID && j > 0) {
     const int N1 = sl.N[j];
     const float4 q1 = sl.Q[j];
+    const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
+    const float ra = __fdiv_rn((float)newn, (float)N1);
+    const float x = __fmaf_rn(q1.x, ra, __fmul_rn(g0, sg));
+    const float y = __fmaf_rn(q1.y, ra, __fmul_rn(g1, sg));
+    const float z = __fmaf_rn(q1.z, ra, __fmul_rn(g2, sg));
+    const float x2 = __fsub_rn(q1.x, x), y2 = __fsub_rn(q1.y, y), z2 = __fsub_rn(q1.z, z);
+    const float4 qa = make_float4(x, y, z, m_q2(x, y, z)), qb = make_float4(x2, y2, z2, m_q2(x2, y2, z2));
     t.sync();
     move_strands_up(sl, j, Z, t);
     if (lane == 0) {
-      const float sg = __fsqrt_rn(__fdiv_rn((float)(newn * (N1 - newn)), (float)(3 * N1)));
-      const float ra = __fdiv_rn((float)newn, (float)N1);
-      const float x = __fmaf_rn(q1.x, ra, __fmul_rn(g0, sg));
-      const float y = __fmaf_rn(q1.y, ra, __fmul_rn(g1, sg));
-      const float z = __fmaf_rn(q1.z, ra, __fmul_rn(g2, sg));
-      sl.N[j] = newn; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
-      const float x2 = __fsub_rn(q1.x, x), y2 = __fsub_rn(q1.y, y), z2 = __fsub_rn(q1.z, z);
-      sl.N[j + 1] = N1 - newn; sl.Q[j + 1] = make_float4(x2, y2, z2, m_q2(x2, y2, z2));
+      sl.N[j] = newn; sl.Q[j] = qa;
+      sl.N[j + 1] = N1 - newn; sl.Q[j + 1] = qb;
       sl.T[j] = trate;
     }
     *up0_out = j - 1; *upn_out = 3;
@@ -844,13 +847,14 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
     const int N0 = sl.N[0];
     const int nn = (evn == SDC_HEAD) ? N0 - 1 : N0 - newn;
     const int nd = (evn == SDC_HEAD) ? 1 : newn;
+    const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+    const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+    const float4 qn = make_float4(x, y, z, m_q2(x, y, z));
     t.sync();
     move_strands_up(sl, 0, Z, t);
     if (lane == 0) {
-      const float sg = (evn == SDC_HEAD && Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
-      const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
       sl.N[0] = nd; sl.Q[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-      sl.N[1] = nn; sl.Q[1] = make_float4(x, y, z, m_q2(x, y, z));
+      sl.N[1] = nn; sl.Q[1] = qn;
       sl.T[0] = trate;
       if (E.corr_type == 1) {  // MSD: the new first entanglement (eq_ensemble_kernel.cu:531-539,606-614)
         Corr0& k0 = *sl.k0;
@@ -862,12 +866,13 @@ __device__ DSM_APPLY_ATTR int apply_create(const EnsDev& E, Slot& sl, int evn, i
     const int Nt = sl.N[Z - 1];
     const int nn = (evn == SDC_TAIL) ? Nt - 1 : newn;
     const int nd = (evn == SDC_TAIL) ? 1 : Nt - newn;
+    const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
+    const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
+    const float4 qn = make_float4(x, y, z, m_q2(x, y, z));
     t.sync();
     if (lane == 0) {
-      const float sg = (Z == 1) ? 0.0f : __fsqrt_rn(__fdiv_rn((float)nn, 3.0f));
-      const float x = __fmul_rn(g0, sg), y = __fmul_rn(g1, sg), z = __fmul_rn(g2, sg);
       sl.N[Z] = nd; sl.Q[Z] = make_float4(0.f, 0.f, 0.f, 0.f);
-      sl.N[Z - 1] = nn; sl.Q[Z - 1] = make_float4(x, y, z, m_q2(x, y, z));
+      sl.N[Z - 1] = nn; sl.Q[Z - 1] = qn;
       sl.T[Z - 1] = trate;
     }
     *up0_out = Z - 2; *upn_out = 2;
@@ -887,13 +892,15 @@ __device__ DSM_APPLY_ATTR void apply_destroy(Slot& sl, int evn, int j, int Z, co
     const int n = sl.N[j] + sl.N[j + 1];
     const float4 a = sl.Q[j], b = sl.Q[j + 1];
     const bool endp = (j == Z - 2) || (j == 0);
+    // the merged strand, computed by every lane before the move, stored by lane 0 after it
+    const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
+    const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
+    const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
+    const float4 qm = make_float4(x, y, z, m_q2(x, y, z));
     t.sync();
     move_strands_down(sl, j + 2, j + 1, Z, t);
     if (lane == 0) {
-      const float x = endp ? 0.f : __fadd_rn(a.x, b.x);
-      const float y = endp ? 0.f : __fadd_rn(a.y, b.y);
-      const float z = endp ? 0.f : __fadd_rn(a.z, b.z);
-      sl.N[j] = n; sl.Q[j] = make_float4(x, y, z, m_q2(x, y, z));
+      sl.N[j] = n; sl.Q[j] = qm;
       if (msd && j == 0) {  // the first entanglement is now the old second one (eq_ensemble_kernel.cu:447-455)
         Corr0& k0 = *sl.k0;
         k0.r1x = __fadd_rn(k0.r1x, b.x); k0.r1y = __fadd_rn(k0.r1y, b.y); k0.r1z = __fadd_rn(k0.r1z, b.z);
@@ -1243,9 +1250,11 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       bool slide = false;
       if (evn == SDP || evn == SDM) {
         t.sync();
-        if (lane == 0) {
+        {
+          // every lane computes (broadcast loads), lane 0 stores
           const int d = (evn == SDP) ? 1 : -1;
-          sl.N[j] += d; sl.N[j + 1] -= d;
+          const int na = sl.N[j] + d, nb = sl.N[j + 1] - d;
+          if (lane == 0) { sl.N[j] = na; sl.N[j + 1] = nb; }
         }
         up0 = j - 1; upn = 3;
         ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
