@@ -1104,7 +1104,10 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
     bool words = false;  // Philox words of the current batch of W events loaded
     DSM_PHASE(10);  // chain load and first rate pass
 
-    for (;;) {
+    // a chain that stalled in an earlier launch stays put (inside the loop a
+    // stall always ends it at once, so the loop tests no stall code)
+    if (stall != 0) dt_prev = 0.0f;
+    else for (;;) {
       // (1) flow: deformation by the previous dt (ensemble_kernel.cu:135-146)
       if (FLOW && dt_prev != 0.0f) flow_deform<W>(E, sl, Z, dt_prev, t);
       // (2) equilibrium stress samples due (eq_ensemble_kernel.cu:281-331)
@@ -1112,7 +1115,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       // (3) reach / stall / window checks (ensemble_kernel.cu:199-207); a full
       // slot (a creation could need strand Z+1) ends the launch for this chain
       // at this step boundary, exactly like a window end
-      if (stall != 0 || T >= t_end || (long long)step >= step_lim || Z >= zlim) {
+      if (T >= t_end || (long long)step >= step_lim || Z >= zlim) {
         if (stall == 0 && T < t_end && (long long)step >= step_lim && step_lim != E.step_limit) stall = ST_WATCHDOG;
         dt_prev = 0.0f;
         // a window of a flow series ends: record the stress and go on with
@@ -1127,12 +1130,6 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
             continue;
           }
         }
-        break;
-      }
-      if (abort_flag != nullptr && (step & 4095) == 4095 && *abort_flag != 0) {
-        if (lane == 0) atomicOr(status, 1);
-        dt_prev = 0.0f;
-        aborted = true;
         break;
       }
       DSM_PHASE(0);  // checks and correlator samples
@@ -1191,6 +1188,13 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       DSM_PHASE(2);  // prefix scan, dt
       // (7) Philox words of this event (one evaluation per 32 events)
       if ((step & (uint64_t)(W - 1)) == 0 || !words) {
+        // the run flag, polled every 4096 events (nothing of the event is applied yet)
+        if (abort_flag != nullptr && (step & 4095) == 0 && *abort_flag != 0) {
+          if (lane == 0) atomicOr(status, 1);
+          dt_prev = 0.0f;
+          aborted = true;
+          break;
+        }
         const uint64_t ctr = (step & ~(uint64_t)(W - 1)) + (uint64_t)lane;
         const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
         r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
