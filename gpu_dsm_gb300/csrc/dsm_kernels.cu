@@ -1083,15 +1083,20 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
     }
     t.sync();
 
-    // bit0 NaN, bit1 inf, bit2 scale overflow (pending from incremental updates)
+    // NaN (bit 0) and inf (bit 1) from a full rate pass
     int pend = 0;
+    // rate work due before the next event: bit 0 the chain-end rates, bit 2 a
+    // full pass (scale overflow of an incremental update)
+    int dirty = 0;
     if (!FLOW) {
       // equilibrium keeps quantised rates in the slot; the overflow rule can
       // only lower the scale, and is kept only if an event follows (the oracle
       // applies it inside a step)
       S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
+      // a NaN or inf found here stalls the chain at its first step, after that
+      // step's checks: the pending pass repeats the rates and sets them again
+      if (pend & 3) dirty = 4;
     }
-    bool ends_dirty = false;
     // per-lane exclusive/inclusive prefix of the element array and its total;
     // rebuilt by a chunk sum + warp scan only after structural events, end or
     // scale changes and in flow; sliding events patch them with the deltas of
@@ -1101,7 +1106,14 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
     int cw = 1, j0 = 0;
 
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-    bool words = false;  // Philox words of the current batch of W events loaded
+    // equilibrium: the Philox words of the current batch of W events are
+    // loaded here; flow loads them at its first event
+    bool words = !FLOW;
+    if (!FLOW) {
+      const uint64_t ctr = (step & ~(uint64_t)(W - 1)) + (uint64_t)lane;
+      const U4 q = rng_at(E, P_EVENT, ctr, (uint32_t)(ctr >> 32), (uint32_t)c);
+      r0 = q.x; r1 = q.y; r2 = q.z; r3 = q.w;
+    }
     DSM_PHASE(10);  // chain load and first rate pass
 
     // a chain that stalled in an earlier launch stays put (inside the loop a
@@ -1139,30 +1151,36 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (FLOW) {
         S = full_rates_body<true, W>(E, sl, Z, S, wz1, t, &pend);
         rescan = true;
-      } else if (ends_dirty | ((pend & 4) != 0)) {
-        // one branch in the common case (neither): the chain-end refresh, or
-        // the full pass that a pending scale overflow asks for
-        if (ends_dirty) {
+        if (pend & 3) {
+          stall = (pend & 1) ? ST_NAN : ST_INF;
+          dt_prev = 0.0f;
+          break;
+        }
+      } else if (dirty != 0) {
+        // one branch in the common case (nothing due): the chain-end refresh,
+        // or the full pass that a scale overflow asks for
+        if (dirty & 1) {
           int over = 0;
           if (lane < NEND) {
             const float ev = end_comp(E, lane, Z, sl.N, wz1);
             over = (fexp(ev) + S > LIMIT_E) ? 4 : 0;
             sl.R[np + lane] = quant(ev, pow2f(S));
           }
-          pend |= t.or_(over);
-          if (pend & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
-          ends_dirty = false;
+          dirty |= t.or_(over);
+          if (dirty & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
           rescan = true;
           t.sync();
         } else {
           S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
           rescan = true;
         }
-      }
-      if (pend & 3) {
-        stall = (pend & 1) ? ST_NAN : ST_INF;
-        dt_prev = 0.0f;
-        break;
+        dirty = 0;
+        // NaN and inf come only from a full pass
+        if (pend & 3) {
+          stall = (pend & 1) ? ST_NAN : ST_INF;
+          dt_prev = 0.0f;
+          break;
+        }
       }
       DSM_PHASE(1);  // chain-end rates, rate passes
       const float sf = pow2f(S);
@@ -1186,8 +1204,8 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
       DSM_PHASE(2);  // prefix scan, dt
-      // (7) Philox words of this event (one evaluation per 32 events)
-      if ((step & (uint64_t)(W - 1)) == 0 || !words) {
+      // (7) Philox words of this event (one evaluation per W events)
+      if ((step & (uint64_t)(W - 1)) == 0 || (FLOW && !words)) {
         // the run flag, polled every 4096 events (nothing of the event is applied yet)
         if (abort_flag != nullptr && (step & 4095) == 0 && *abort_flag != 0) {
           if (lane == 0) atomicOr(status, 1);
@@ -1261,20 +1279,32 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
           if (lane == 0) { sl.N[j] = na; sl.N[j + 1] = nb; }
         }
         up0 = j - 1; upn = 3;
-        ends_dirty = (j <= 1) || (j + 1 >= Z - 2);
-        slide = !ends_dirty;
+        slide = !((j <= 1) || (j + 1 >= Z - 2));
+        dirty = slide ? 0 : 1;
       } else if (evn == CDD || evn == SDD_HEAD || evn == SDD_TAIL) {
+        // away from both chain ends (pair 2 <= j < Z - 3) a destruction keeps
+        // what the end rates depend on (Z >= 3, the two strands at each end):
+        // their quantised values move down with the pairs, not recomputed
+        const bool mid = !FLOW && j >= 2 && j + 3 < Z;
+        unsigned long long ev = 0;
+        if (mid && lane < NEND) ev = sl.R[np + lane];
         apply_destroy<W, MSD>(sl, evn, j, Z, t, &up0, &upn);
+        if (mid && lane < NEND) sl.R[np - 1 + lane] = ev;
         Z -= 1;
-        ends_dirty = true;
+        dirty = mid ? 0 : 1;
       } else if (Z >= cap) {
         code |= (uint32_t)NULL_FLAG << 24;  // creation refused at capacity (ensemble_kernel.cu:380,423,451)
       } else {
         const uint32_t w2 = t.shfl(r2, src);
         const uint32_t w3 = t.shfl(r3, src);
+        // the same for a creation inside a strand away from both ends
+        const bool mid = !FLOW && j >= 2 && j + 3 < Z;
+        unsigned long long ev = 0;
+        if (mid && lane < NEND) ev = sl.R[np + lane];
         const int newn = apply_create<W>(E, sl, evn, j, Z, c, step, rem, wsel, w2, w3, t, &up0, &upn);
+        if (mid && lane < NEND) sl.R[np + 1 + lane] = ev;
         Z += 1;
-        ends_dirty = true;
+        dirty = mid ? 0 : 1;
         code |= (uint32_t)newn << 8;
       }
       t.sync();
@@ -1287,7 +1317,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
 #endif
       if (!FLOW && upn > 0) {
         unsigned long long dl;
-        pend |= update_pairs<W>(E, sl, Z, S, up0, upn, t, &dl);
+        dirty |= update_pairs<W>(E, sl, Z, S, up0, upn, t, &dl);
         if (slide) {
           // patch the prefix sums with the deltas of pairs j-1, j, j+1 (lanes
           // 0, 4, 8); pair j lies in lane L's chunk, its neighbours in L's
@@ -1304,7 +1334,7 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
         } else {
           rescan = true;
         }
-      } else if (upn > 0 || ends_dirty) {
+      } else if (upn > 0 || dirty != 0) {
         rescan = true;
       }
       DSM_PHASE(8);  // pair-rate update, prefix patch
