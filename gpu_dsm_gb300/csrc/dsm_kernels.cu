@@ -1085,8 +1085,8 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
 
     // NaN (bit 0) and inf (bit 1) from a full rate pass
     int pend = 0;
-    // rate work due before the next event: bit 0 the chain-end rates, bit 2 a
-    // full pass (scale overflow of an incremental update)
+    // rate work due before the next event: bit 0 the chain-end rates, bit 1 the
+    // prefix rebuild, bit 2 a full pass (scale overflow of an incremental update)
     int dirty = 0;
     if (!FLOW) {
       // equilibrium keeps quantised rates in the slot; the overflow rule can
@@ -1096,14 +1096,26 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       // a NaN or inf found here stalls the chain at its first step, after that
       // step's checks: the pending pass repeats the rates and sets them again
       if (pend & 3) dirty = 4;
+      dirty |= 2;
     }
-    // per-lane exclusive/inclusive prefix of the element array and its total;
-    // rebuilt by a chunk sum + warp scan only after structural events, end or
-    // scale changes and in flow; sliding events patch them with the deltas of
-    // the <=3 recomputed pairs
-    bool rescan = true;
+    // (5) per-lane exclusive/inclusive prefix of the element array (contiguous
+    // odd-width chunks over pairs + ends) and its total;
+    // rebuilt by a chunk sum + warp scan every event in flow, and in
+    // equilibrium inside the rate-pass dispatch, after structural events, end
+    // or scale changes; sliding events patch them with the deltas of the <=3
+    // recomputed pairs
     unsigned long long incl = 0, excl = 0, tot = 0;
     int cw = 1, j0 = 0;
+    auto rebuild = [&](int ne) {
+      cw = ((ne + W - 1) / W) | 1;
+      j0 = lane * cw;
+      const int j1 = min(j0 + cw, ne);
+      unsigned long long part = 0;
+      for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
+      incl = tile_scan(t, part);
+      excl = incl - part;
+      tot = t.shfl(incl, W - 1);
+    };
 
     uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
     // equilibrium: the Philox words of the current batch of W events are
@@ -1150,15 +1162,16 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
       // ends when a strand next to an end changed
       if (FLOW) {
         S = full_rates_body<true, W>(E, sl, Z, S, wz1, t, &pend);
-        rescan = true;
         if (pend & 3) {
           stall = (pend & 1) ? ST_NAN : ST_INF;
           dt_prev = 0.0f;
           break;
         }
+        rebuild(np + NEND);
       } else if (dirty != 0) {
-        // one branch in the common case (nothing due): the chain-end refresh,
-        // or the full pass that a scale overflow asks for
+        // one branch in the common case (nothing due): the chain-end refresh
+        // (bit 0), the full pass that a scale overflow asks for (bit 2), then
+        // the prefix rebuild that these and structural events (bit 1) need
         if (dirty & 1) {
           int over = 0;
           if (lane < NEND) {
@@ -1168,11 +1181,9 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
           }
           dirty |= t.or_(over);
           if (dirty & 4) S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
-          rescan = true;
           t.sync();
-        } else {
+        } else if (dirty & 4) {
           S = full_rates<false, W>(E, sl, Z, S, wz1, t, &pend);
-          rescan = true;
         }
         dirty = 0;
         // NaN and inf come only from a full pass
@@ -1181,29 +1192,17 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
           dt_prev = 0.0f;
           break;
         }
+        rebuild(np + NEND);
       }
-      DSM_PHASE(1);  // chain-end rates, rate passes
+      DSM_PHASE(1);  // chain-end rates, rate passes, prefix rebuild
       const float sf = pow2f(S);
-      // (5) sums: contiguous odd-width chunk per lane over pairs + ends, warp scan
-      if (rescan) {
-        const int ne = np + NEND;
-        cw = ((ne + W - 1) / W) | 1;
-        j0 = lane * cw;
-        const int j1 = min(j0 + cw, ne);
-        unsigned long long part = 0;
-        for (int jj = j0; jj < j1; ++jj) part += sl.R[jj];
-        incl = tile_scan(t, part);
-        excl = incl - part;
-        tot = t.shfl(incl, W - 1);
-        rescan = false;
-      }
       // (6) dt = 1/sum W (ensemble_kernel.cu:262-272)
       const float sumw = __fmul_rn(__ll2float_rn((long long)tot), pow2f(-S));
       const float dt = __fdiv_rn(1.0f, sumw);
       if (dt == 0.0f) { stall = ST_DT_ZERO; dt_prev = 0.0f; break; }
       if (!(dt < 2.0e9f)) { stall = ST_INF; dt_prev = 0.0f; break; }
       const long long dtt = __float2ll_rn(__fmul_rn(dt, 4294967296.0f));
-      DSM_PHASE(2);  // prefix scan, dt
+      DSM_PHASE(2);  // dt
       // (7) Philox words of this event (one evaluation per W events)
       if ((step & (uint64_t)(W - 1)) == 0 || (FLOW && !words)) {
         // the run flag, polled every 4096 events (nothing of the event is applied yet)
@@ -1332,10 +1331,8 @@ __global__ void __launch_bounds__(128, MB) k_step(const EnsDev* __restrict__ ens
             tot += d;
           }
         } else {
-          rescan = true;
+          dirty |= 2;
         }
-      } else if (upn > 0 || dirty != 0) {
-        rescan = true;
       }
       DSM_PHASE(8);  // pair-rate update, prefix patch
       if (lane == 0) sl.h->hash = (sl.h->hash ^ (uint64_t)code) * 0x100000001B3ull;

@@ -35,7 +35,7 @@ import sys
 
 from . import build as native
 
-NAMES = ["checks and correlator samples", "chain-end rates, rate passes", "prefix scan, dt",
+NAMES = ["checks and correlator samples", "chain-end rates, rate passes, prefix rebuild", "dt",
          "Philox, pick, chunk walk", "classification", "apply: slide", "apply: destruction", "apply: creation",
          "pair-rate update, prefix patch", "event hash, counters", "chain load, first rate pass", "chain store"]
 TYPES = ["slide", "destruction", "creation"]
