@@ -741,7 +741,17 @@ extern "C" int dsm_autotune(dsm_sim* s, double window, int32_t* best, float* bes
     if (rc == DSM_OK) rc = sim_finish_window(s, nullptr);
     if (rc != DSM_OK) return rc;
     const double rate = (double)s->last_events / std::max(1e-6, (double)s->last_kernel_ms);
-    if (bi < 0 || rate > brate) { bi = (int)i; brate = rate; bms = s->last_kernel_ms; }
+    // A short window tells schedules of different tile widths apart only
+    // coarsely: over whole windows two 16-lane tiles per warp ran the
+    // polydisperse melt 1.5x faster than one 32-lane tile, while single trial
+    // windows of a few tau_K came out within a few percent of each other.  So
+    // a change of tile width must win its trial by kLaneMargin: 32 lanes must
+    // be that much faster than the best 16-lane schedule, and 16 lanes may be
+    // that much slower than the best 32-lane one.
+    constexpr double kLaneMargin = 0.03;
+    double need = brate;
+    if (bi >= 0 && c.lanes != cands[bi].lanes) need = brate * (c.lanes == 16 ? 1.0 - kLaneMargin : 1.0 + kLaneMargin);
+    if (bi < 0 || rate > need) { bi = (int)i; brate = rate; bms = s->last_kernel_ms; }
   }
   const Cand& b = cands[bi];
   s->cfg.lanes = b.lanes;

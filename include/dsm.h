@@ -234,7 +234,10 @@ int dsm_get_class_form(const dsm_sim* sim, int32_t* form);
  * large-class grid at 1/2, 1 and 2 times its default, and with 16 lanes each
  * small slot also in the carved one-launch form of dsm_set_class_form) and
  * keeps the one with
- * the most kMC events per kernel millisecond.  The ensemble advances by
+ * the most kMC events per kernel millisecond; a change of lanes per chain must
+ * win by 3 % (32 lanes over the best 16-lane schedule; 16 lanes within 3 % of
+ * the best 32-lane one), since trial windows resolve tile widths only
+ * coarsely.  The ensemble advances by
  * candidates x window; its trajectory is the one it would have had without
  * the autotuner.  best (may be NULL) receives {small_slot, large_grid, lanes,
  * candidates}; best_ms the winner's kernel time.  No counterpart in the
